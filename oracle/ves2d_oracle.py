@@ -1,0 +1,716 @@
+"""CPU FP64 oracle for the Ves2Dpy boundary-integral (BIEM) vesicle step.
+
+TEST INFRASTRUCTURE ONLY.  This module is the checker that the CUDA path is
+compared against.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
+``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` may import it;
+the ``ves2dpy_gb300`` package never does, and nothing it computes is shipped.
+
+It restates, in NumPy/SciPy double precision, the algorithm of the reference
+``mytorch/`` BIEM path (file:line cited per function, paths relative to the
+reference project root).  Parity of this restatement is pinned by
+``tests/test_oracle_golden.py`` against fixtures recorded from the reference
+itself (``tests/golden/make_golden.py``), with the reference's FP32 casts
+promoted to FP64 by the test-only import shim.
+
+Deliberate, documented deviations from the literal reference:
+
+* ``exactStokesSL_`` (``mytorch/biem_support.py:334-389``) raises a shape
+  error for any multi-column target set, which is exactly how
+  ``nearSingInt_hh`` (``mytorch/poten.py:571``) calls it; the reference BIEM
+  step therefore crashes as soon as one near pair exists.  The oracle
+  evaluates the single layer of the listed source vesicles at every target
+  column (the evident intent).  Its value never reaches the output of
+  ``nearSingInt_hh`` because the last row of the Lagrange matrix is
+  ``[1, 0, ..., 0]`` (``mytorch/poten.py:987``), so ``nearSingInt_hh`` is
+  restated as the gather it reduces to.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+import scipy.linalg as sla
+import scipy.sparse.linalg as spla
+
+# --------------------------------------------------------------------------
+# Spectral helpers (mytorch/fft1.py, mytorch/filter.py, curve_batch_compile.py)
+# --------------------------------------------------------------------------
+
+
+def ik_modes(N: int) -> np.ndarray:
+    """1j*[0..N/2-1, 0, -N/2+1..-1] (fft1.py:185-196, curve_batch_compile.py:389)."""
+    return 1j * np.concatenate((np.arange(0, N // 2), [0.0], np.arange(-N // 2 + 1, 0)))
+
+
+def get_xy(X):
+    N = X.shape[0] // 2
+    return X[:N], X[N:]
+
+
+def get_dxy(X):
+    """Parametric derivatives by FFT (curve_batch_compile.py:379-397)."""
+    x, y = get_xy(X)
+    ik = ik_modes(x.shape[0])[:, None]
+    Dx = np.real(np.fft.ifft(ik * np.fft.fft(x, axis=0), axis=0))
+    Dy = np.real(np.fft.ifft(ik * np.fft.fft(y, axis=0), axis=0))
+    return Dx, Dy
+
+
+def arc_deriv(f, m, isa):
+    """Arclength derivative of order m (curve_batch_compile.py:1188-1200)."""
+    ik = ik_modes(f.shape[0])[:, None]
+    g = f.astype(np.complex128)
+    for _ in range(m):
+        g = isa * np.fft.ifft(ik * np.fft.fft(g, axis=0), axis=0)
+    return np.real(g)
+
+
+def diff_prop(X):
+    """Jacobian, unit tangent, curvature (curve_batch_compile.py:400-423)."""
+    N, nv = X.shape[0] // 2, X.shape[1]
+    Dx, Dy = get_dxy(X)
+    jac = np.sqrt(Dx ** 2 + Dy ** 2)
+    tang = np.vstack((Dx / jac, Dy / jac))
+    ones = np.ones((N, nv))
+    DDx = arc_deriv(Dx, 1, ones)
+    DDy = arc_deriv(Dy, 1, ones)
+    cur = (Dx * DDy - Dy * DDx) / jac ** 3
+    return jac, tang, cur
+
+
+def geom_prop(X):
+    """Reduced area, area, length (curve_batch_compile.py:455-473)."""
+    x, y = get_xy(X)
+    N = x.shape[0]
+    Dx, Dy = get_dxy(X)
+    length = np.sum(np.sqrt(Dx ** 2 + Dy ** 2), axis=0) * 2 * np.pi / N
+    area = np.sum(x * Dy - y * Dx, axis=0) * np.pi / N
+    return 4 * np.pi * area / length ** 2, area, length
+
+
+def interpft(x, N_new: int):
+    """Fourier resampling along axis 0 (filter.py:221-249)."""
+    N = x.shape[0]
+    if N == N_new:
+        return x.copy()
+    Xh = np.fft.fft(x, axis=0)
+    if N_new > N:
+        Xn = np.zeros((N_new,) + x.shape[1:], dtype=np.complex128)
+        Xn[: N // 2] = Xh[: N // 2]
+        Xn[-(N // 2):] = Xh[-(N // 2):]
+    else:
+        Xn = np.concatenate([Xh[: N_new // 2], Xh[-(N_new // 2):]])
+    return np.real(np.fft.ifft(Xn, axis=0)) * (N_new / N)
+
+
+def interpft_vec(X, N_new: int):
+    """Resample both coordinates (filter.py:192-194)."""
+    N = X.shape[0] // 2
+    return np.concatenate((interpft(X[:N], N_new), interpft(X[N:], N_new)), axis=0)
+
+
+def filter_shape(X, mode_cut: int):
+    """Hard Fourier cut of z = x + iy (filter.py:287-311)."""
+    N = X.shape[0] // 2
+    modes = np.concatenate([np.arange(0, N // 2), np.arange(-N // 2, 0)])
+    z = X[:N] + 1j * X[N:]
+    zh = np.fft.fft(z, axis=0)
+    zh[np.abs(modes) > mode_cut] = 0
+    zi = np.fft.ifft(zh, axis=0)
+    return np.vstack((zi.real, zi.imag))
+
+
+def fourier_int(N: int):
+    """FF, FFI with modes [-N/2 .. N/2-1] (fft1.py:233-249)."""
+    theta = np.arange(N) * 2 * np.pi / N
+    modes = np.concatenate(([-N / 2], np.arange(-N / 2 + 1, N / 2)))
+    FF = np.exp(-1j * np.outer(modes, theta)) / N
+    FFI = np.exp(1j * np.outer(theta, modes))
+    return FF, FFI
+
+
+def fourier_diff(N: int):
+    """Complex Fourier differentiation matrix (fft1.py:198-207)."""
+    FF = fourier_int(N)[0]
+    modes = np.arange(-N // 2, N // 2)
+    return np.conj(FF.T) @ np.diag(1j * N * modes) @ FF
+
+
+def fourier_r_and_p(N: int, Nup: int):
+    """Restriction R (N x Nup) and prolongation P (Nup x N) (fft1.py:209-231)."""
+    FF1, FFI1 = fourier_int(N)
+    FF2, _ = fourier_int(Nup)
+    pad = np.hstack((np.zeros((N, (Nup - N) // 2)), np.eye(N), np.zeros((N, (Nup - N) // 2))))
+    R = np.real(FFI1 @ pad @ FF2)
+    P = R.T * Nup / N
+    return R, P
+
+
+def sinterp_rows(N: int, y):
+    """Trig interpolation rows on an N-grid at points y (fft1.py:58-88)."""
+    modes = np.concatenate((np.arange(0, N // 2), [0.0], np.arange(-N // 2 + 1, 0)))
+    fhat = np.fft.fft(np.eye(N), axis=0) / N
+    return np.real(np.exp(1j * np.outer(y, modes)) @ fhat)
+
+
+# --------------------------------------------------------------------------
+# Alpert log-singular self quadrature (mytorch/poten.py:40-99, 899-974)
+# --------------------------------------------------------------------------
+
+ALPERT_V = np.array([6.531815708567918e-3, 9.086744584657729e-2, 3.967966533375878e-1,
+                     1.027856640525646e+0, 1.945288592909266e+0, 2.980147933889640e+0,
+                     3.998861349951123e+0])
+ALPERT_U = np.array([2.462194198995203e-2, 1.701315866854178e-1, 4.609256358650077e-1,
+                     7.947291148621895e-1, 1.008710414337933e+0, 1.036093649726216e+0,
+                     1.004787656533285e+0])
+ALPERT_A = 5
+
+LAGRANGE_INTERP = np.array([
+    [64.80, -388.80, 972.00, -1296.00, 972.00, -388.80, 64.80],
+    [-226.80, 1296.00, -3078.00, 3888.00, -2754.00, 1036.80, -162.00],
+    [315.00, -1674.00, 3699.00, -4356.00, 2889.00, -1026.00, 153.00],
+    [-220.50, 1044.00, -2074.50, 2232.00, -1381.50, 468.00, -67.50],
+    [81.20, -313.20, 526.50, -508.00, 297.00, -97.20, 13.70],
+    [-14.70, 36.00, -45.00, 40.00, -22.50, 7.20, -1.00],
+    [1.00, 0.00, 0.00, 0.00, 0.00, 0.00, 0.00]])  # poten.py:977-990
+
+
+def sing_quad_weights(Nup: int):
+    """qw (Nquad,), qp (Nquad, Nup) of the order-7 Alpert rule (poten.py:899-945)."""
+    a = ALPERT_A
+    h = 2 * np.pi / Nup
+    n = Nup - 2 * a + 1
+    wt = np.concatenate([h * ALPERT_U, h * np.ones(n), h * ALPERT_U[::-1]]) / (4 * np.pi)
+    B = np.zeros((n, Nup))
+    B[np.arange(n), np.arange(a, n + a)] = 1
+    A1 = sinterp_rows(Nup, ALPERT_V * h)
+    A2 = sinterp_rows(Nup, 2 * np.pi - (ALPERT_V * h)[::-1])
+    qp = np.vstack([A1, B, A2])
+    return wt, qp
+
+
+def upsample_factor(N: int) -> int:
+    return N * math.ceil(math.sqrt(N))
+
+
+class PotenTables:
+    """Per-N constant tables (poten.py:15-37)."""
+
+    def __init__(self, N: int):
+        self.N = N
+        self.Nup = upsample_factor(N)
+        self.qw, self.qp = sing_quad_weights(self.Nup)
+        self.R, self.P = fourier_r_and_p(N, self.Nup)
+        self.interp = LAGRANGE_INTERP.copy()
+
+
+def stokes_sl_matrix(X, tab: PotenTables):
+    """Alpert single-layer matrix G (2N, 2N, nv) (poten.py:40-99)."""
+    N, nv = X.shape[0] // 2, X.shape[1]
+    Nup = tab.Nup
+    Xup = interpft_vec(X, Nup)
+    sa_up, _, _ = diff_prop(Xup)
+    x, y = Xup[:Nup], Xup[Nup:]
+    idx = np.arange(Nup)
+    shift = (idx[:, None] + idx[None, :]) % Nup            # [i, s] -> (i + s) % Nup
+    G = np.zeros((2 * N, 2 * N, nv))
+    for k in range(nv):
+        xs = x[shift, k]
+        ys = y[shift, k]
+        dx = x[None, :, k] - tab.qp @ xs                     # (Nquad, Nup_s)
+        dy = y[None, :, k] - tab.qp @ ys
+        rho2 = 1.0 / (dx ** 2 + dy ** 2 + 1e-7)
+        qwc = tab.qw[:, None]
+        logpart = 0.5 * tab.qp.T @ (qwc * np.log(rho2))      # [i, s]
+        g11 = logpart + tab.qp.T @ (qwc * dx ** 2 * rho2)
+        g22 = logpart + tab.qp.T @ (qwc * dy ** 2 * rho2)
+        g12 = tab.qp.T @ (qwc * dx * dy * rho2)
+        # G[b, a] = Gpre[(a - b) % Nup, b] * sa[a]
+        rows = idx[:, None]
+        cols = idx[None, :]
+        ii = (cols - rows) % Nup
+        G11 = g11[ii, rows] * sa_up[None, :, k]
+        G22 = g22[ii, rows] * sa_up[None, :, k]
+        G12 = g12[ii, rows] * sa_up[None, :, k]
+        G[:N, :N, k] = tab.R @ G11 @ tab.P
+        G[:N, N:, k] = tab.R @ G12 @ tab.P
+        G[N:, :N, k] = G[:N, N:, k]
+        G[N:, N:, k] = tab.R @ G22 @ tab.P
+    return G
+
+
+def exact_stokes_sl_diag(G, f):
+    """Per-vesicle G @ f (poten.py:213-224)."""
+    return np.einsum('ijk,jk->ik', G, f)
+
+
+# --------------------------------------------------------------------------
+# Vesicle operators (mytorch/capsules.py)
+# --------------------------------------------------------------------------
+
+
+class Capsule:
+    """capsules.__init__ (capsules.py:19-52)."""
+
+    def __init__(self, X, kappa=1.0):
+        self.X = X
+        self.N = X.shape[0] // 2
+        self.nv = X.shape[1]
+        self.sa, self.xt, self.cur = diff_prop(X)
+        self.isa = 1.0 / self.sa
+        self.kappa = kappa
+        _, _, length = geom_prop(X)
+        self.length = float(np.min(length))
+
+    def bending_term(self, f):
+        """capsules.py:62-68."""
+        N = self.N
+        return np.vstack([-self.kappa * arc_deriv(f[:N], 4, self.isa),
+                          -self.kappa * arc_deriv(f[N:], 4, self.isa)])
+
+    def tension_term(self, sig):
+        """capsules.py:70-80."""
+        N = self.N
+        return np.vstack([arc_deriv(sig * self.xt[:N], 1, self.isa),
+                          arc_deriv(sig * self.xt[N:], 1, self.isa)])
+
+    def trac_jump(self, f, sigma):
+        """capsules.py:54-60."""
+        return self.bending_term(f) + self.tension_term(sigma)
+
+    def surface_div(self, f):
+        """capsules.py:82-89."""
+        fx, fy = get_xy(f)
+        tx, ty = get_xy(self.xt)
+        return arc_deriv(fx, 1, self.isa) * tx + arc_deriv(fy, 1, self.isa) * ty
+
+    def compute_derivs(self):
+        """Dense Ben (2N,2N,nv), Ten (2N,N,nv), Div (N,2N,nv) (capsules.py:91-206)."""
+        N, nv = self.N, self.nv
+        D1 = fourier_diff(N)
+        Ben = np.zeros((2 * N, 2 * N, nv))
+        Ten = np.zeros((2 * N, N, nv))
+        Div = np.zeros((N, 2 * N, nv))
+        for k in range(nv):
+            A = self.isa[:, k][:, None] * D1
+            D2 = A @ A
+            D4 = np.real(D2 @ D2)
+            Ar = np.real(A)
+            Ben[:N, :N, k] = D4
+            Ben[N:, N:, k] = D4
+            Ten[:N, :, k] = Ar @ np.diag(self.xt[:N, k])
+            Ten[N:, :, k] = Ar @ np.diag(self.xt[N:, k])
+            Div[:, :N, k] = np.diag(self.xt[:N, k]) @ Ar
+            Div[:, N:, k] = np.diag(self.xt[N:, k]) @ Ar
+        return Ben, Ten, Div
+
+
+# --------------------------------------------------------------------------
+# Far field and near-zone bookkeeping (mytorch/biem_support.py)
+# --------------------------------------------------------------------------
+
+
+def other_indices(nv: int):
+    """Row t lists source vesicles != t in ascending order (biem_support.py:141-145)."""
+    return np.array([[j for j in range(nv) if j != t] for t in range(nv)], dtype=np.int64).reshape(nv, max(nv - 1, 0))
+
+
+def naive_near_zone_info(X, Xup, max_layer_dist=None):
+    """Brute-force near-zone lists (biem_support.py:520-613).
+
+    Returns (closest_dist[nv,nv,Nup], idx_closest[nv,nv,Nup], (id1,id2),
+    (id1_hh,id2_hh), (ids0,ids1,ids2)) with the reference's index meaning.
+    """
+    N, nv = X.shape[0] // 2, X.shape[1]
+    Nup = Xup.shape[0] // 2
+    thr = 1.0 / N if max_layer_dist is None else max_layer_dist
+    P = np.stack([X[:N].T.reshape(-1), X[N:].T.reshape(-1)], axis=1)
+    Q = np.stack([Xup[:Nup].T.reshape(-1), Xup[Nup:].T.reshape(-1)], axis=1)
+    d = np.sqrt((P[:, None, 0] - Q[None, :, 0]) ** 2 + (P[:, None, 1] - Q[None, :, 1]) ** 2)
+    mask = (d < thr).reshape(nv, N, nv, Nup)
+    for v in range(nv):
+        mask[v, :, v, :] = False
+    rows = mask.reshape(nv * N, nv, Nup).max(axis=-1)
+    id1, id2 = np.nonzero(rows)
+    ids1, ids2 = id1 % N, id1 // N
+    ids0 = id2 - (ids2 <= id2).astype(np.int64)
+    rows_hh = mask.reshape(nv, N, nv * Nup).max(axis=1)
+    id2_hh, id1_hh = np.nonzero(rows_hh)
+    d4 = d.reshape(nv, N, nv, Nup)
+    closest_dist = d4.min(axis=1)
+    idx_closest = d4.argmin(axis=1)
+    return closest_dist, idx_closest, (id1, id2), (id1_hh, id2_hh), (ids0, ids1, ids2)
+
+
+def all_exact_stokes_sl_target(Xsrc, sa_src, f, tarX, excl=None, offset=0):
+    """Far field of all other vesicles with near-pair exclusion.
+
+    Restates allExactStokesSLTarget_compare2 (biem_support.py:124-228):
+    target column t excludes source vesicle offset+t; ``excl`` = (ids0, ids1,
+    ids2) zeroes the whole contribution of source vesicle indices[t][ids0] to
+    target point ids1 of column ids2.
+    """
+    Ns, nv = Xsrc.shape[0] // 2, Xsrc.shape[1]
+    Nt, nt = tarX.shape[0] // 2, tarX.shape[1]
+    idx = other_indices(nv)[offset:offset + nt]
+    den = f * np.tile(sa_src, (2, 1)) * 2 * np.pi / Ns
+    out = np.zeros((2 * Nt, nt))
+    keep = np.ones((nv - 1, Nt, nt), dtype=bool)
+    if excl is not None and len(excl[0]):
+        keep[excl[0], excl[1], excl[2]] = False
+    for t in range(nt):
+        src = idx[t]
+        xs = Xsrc[:Ns, src]                       # (Ns, nv-1)
+        ys = Xsrc[Ns:, src]
+        dx_ = den[:Ns, src]
+        dy_ = den[Ns:, src]
+        xt = tarX[:Nt, t]
+        yt = tarX[Nt:, t]
+        dx = xt[None, None, :] - xs[:, :, None]   # (Ns, nv-1, Nt)
+        dy = yt[None, None, :] - ys[:, :, None]
+        r2 = dx ** 2 + dy ** 2
+        coeff = (dx * dx_[:, :, None] + dy * dy_[:, :, None]) / r2
+        lg = 0.5 * np.log(r2)
+        tx = coeff * dx - lg * dx_[:, :, None]
+        ty = coeff * dy - lg * dy_[:, :, None]
+        kp = keep[:, :, t][None]
+        out[:Nt, t] = np.sum(np.where(kp, tx, 0.0), axis=(0, 1))
+        out[Nt:, t] = np.sum(np.where(kp, ty, 0.0), axis=(0, 1))
+    return out / (4 * np.pi)
+
+
+def compare1_exclusions(Xsrc, tarX, length=1.0, offset=0):
+    """Exclusion ids computed by allExactStokesSLTarget_compare1 (biem_support.py:56-75)."""
+    Ns, nv = Xsrc.shape[0] // 2, Xsrc.shape[1]
+    Nt, nt = tarX.shape[0] // 2, tarX.shape[1]
+    idx = other_indices(nv)[offset:offset + nt]
+    flag = np.zeros((nv - 1, Nt, nt), dtype=bool)
+    for t in range(nt):
+        src = idx[t]
+        dx = tarX[:Nt, t][None, None, :] - Xsrc[:Ns, src][:, :, None]
+        dy = tarX[Nt:, t][None, None, :] - Xsrc[Ns:, src][:, :, None]
+        flag[:, :, t] = ((dx ** 2 + dy ** 2) < (length / Nt) ** 2).max(axis=0)
+    j, i, t = np.nonzero(flag)
+    return j, i, t + offset
+
+
+def exact_stokes_sl_points(Xsrc, sa_src, f, Xtar, K1):
+    """Single layer of source vesicles K1 at arbitrary targets (biem_support.py:334-389,
+    evaluated per target column as intended)."""
+    Ns = Xsrc.shape[0] // 2
+    Nt, nc = Xtar.shape[0] // 2, Xtar.shape[1]
+    den = f * np.tile(sa_src, (2, 1)) * 2 * np.pi / Ns
+    xs = Xsrc[:Ns, K1].reshape(-1)
+    ys = Xsrc[Ns:, K1].reshape(-1)
+    dxs = den[:Ns, K1].reshape(-1)
+    dys = den[Ns:, K1].reshape(-1)
+    out = np.zeros((2 * Nt, nc))
+    for k in range(nc):
+        dx = Xtar[:Nt, k][None, :] - xs[:, None]
+        dy = Xtar[Nt:, k][None, :] - ys[:, None]
+        r2 = dx ** 2 + dy ** 2
+        lg = 0.5 * np.log(r2)
+        coeff = (dx * dxs[:, None] + dy * dys[:, None]) / r2
+        out[:Nt, k] = np.sum(coeff * dx - lg * dxs[:, None], axis=0)
+        out[Nt:, k] = np.sum(coeff * dy - lg * dys[:, None], axis=0)
+    return out / (4 * np.pi)
+
+
+def near_sing_int_hh(X, f, vself, near, tab: PotenTables):
+    """nearSingInt_hh restated (poten.py:466-600).
+
+    Far field over upsampled sources with the ``(ids0,ids1,ids2)`` exclusions,
+    plus, for every near entry of the hedgehog list, the gather it reduces to:
+    nearField[J, k2] += vself[(idx_closest - 3) % N, k1] (x and y rows).
+    Returns (LP, nearField).
+    """
+    N, nv = X.shape[0] // 2, X.shape[1]
+    if nv == 1:
+        return np.zeros_like(X), np.zeros_like(X)
+    Nup = tab.Nup
+    Xup = interpft_vec(X, Nup)
+    fup = interpft_vec(f, Nup)
+    sa_up, _, _ = diff_prop(Xup)
+    far = all_exact_stokes_sl_target(Xup, sa_up, fup, X, near[4])
+    nearf = np.zeros((2 * N, nv))
+    entries = hh_entries(near, N, nv)
+    p = 4
+    for k1, k2, J, ic in entries:
+        pn0 = (ic - p + 1) % N
+        nearf[J, k2] += vself[pn0, k1]
+        nearf[J + N, k2] += vself[pn0 + N, k1]
+    return far + nearf, nearf
+
+
+def hh_entries(near, N, nv):
+    """(k1, k2, J, idx_closest) tuples visited by nearSingInt_hh (poten.py:527-597)."""
+    id1, id2 = near[3]
+    idx_closest = near[1]
+    out = []
+    for k1 in range(nv):
+        for k2 in range(nv):
+            if k2 == k1:
+                continue
+            sel = (N * k2 <= id1) & (id1 < N * (k2 + 1)) & (id2 == k1)
+            J = id1[sel] % N
+            for j in J:
+                out.append((k1, k2, int(j), int(idx_closest[k1, k2, j])))
+    return out
+
+
+# --------------------------------------------------------------------------
+# MATLAB-faithful near-singular integration (matlab/poten_py.m:495-692,
+# matlab/capsules_py.m:194-643)
+# --------------------------------------------------------------------------
+
+
+def lagrange_eval(coef, t):
+    """filter(1,[1 -t],coef)(end): Horner evaluation, coefficients high→low."""
+    v = 0.0
+    for c in coef:
+        v = v * t + c
+    return v
+
+
+def closest_point(X, k, xt, yt, icp, interp=LAGRANGE_INTERP):
+    """One Newton step from theta=1/2 on the 7-point local interpolant
+    (capsules_py.m:581-643).  Returns (dist, nx, ny, theta)."""
+    N = X.shape[0] // 2
+    order = interp.shape[0]
+    p = (order + 1 + 1) // 2  # ceil((order+1)/2)
+    # MATLAB's 1-based band icp-p+1..icp-p+order, written 0-based.
+    pn = np.mod(np.arange(icp - p + 1, icp - p + 1 + order), N)
+    px = interp @ X[pn, k]
+    py = interp @ X[pn + N, k]
+    pw = np.arange(order - 1, 0, -1)
+    Dpx = px[:-1] * pw
+    Dpy = py[:-1] * pw
+    pw2 = np.arange(order - 2, 0, -1)
+    D2px = Dpx[:-1] * pw2
+    D2py = Dpy[:-1] * pw2
+    th = 0.5
+    zx, zy = lagrange_eval(px, th), lagrange_eval(py, th)
+    Dzx, Dzy = lagrange_eval(Dpx, th), lagrange_eval(Dpy, th)
+    D2zx, D2zy = lagrange_eval(D2px, th), lagrange_eval(D2py, th)
+    num = (zx - xt) * Dzx + (zy - yt) * Dzy
+    den = (zx - xt) * D2zx + (zy - yt) * D2zy + Dzx ** 2 + Dzy ** 2
+    th = th - num / den
+    nx, ny = lagrange_eval(px, th), lagrange_eval(py, th)
+    return math.sqrt((nx - xt) ** 2 + (ny - yt) ** 2), nx, ny, th
+
+
+@dataclass
+class NearEntry:
+    k1: int      # source vesicle
+    k2: int      # target vesicle
+    j: int       # target point on k2
+    icp: int     # closest grid point on k1
+    dist: float
+    nx: float
+    ny: float
+    theta: float
+
+
+def get_zone(X, h=None, interp=LAGRANGE_INTERP):
+    """Near zone of every vesicle w.r.t. every other (capsules_py.m:194-467,
+    brute force over the candidate set that the bin search guarantees)."""
+    N, nv = X.shape[0] // 2, X.shape[1]
+    if h is None:
+        _, _, L = geom_prop(X)
+        h = float(np.min(L)) / N
+    entries = []
+    for k in range(nv):
+        for k2 in range(nv):
+            if k2 == k:
+                continue
+            for ipt in range(N):
+                d2 = (X[ipt, k2] - X[:N, k]) ** 2 + (X[ipt + N, k2] - X[N:, k]) ** 2
+                loc = int(np.argmin(d2))
+                d0 = math.sqrt(d2[loc])
+                if d0 < 2 * h:
+                    dist, nx, ny, th = closest_point(X, k, X[ipt, k2], X[ipt + N, k2], loc, interp)
+                    if dist < h:
+                        entries.append(NearEntry(k, k2, ipt, loc, dist, nx, ny, th))
+    return entries, h
+
+
+def near_sing_int_matlab(X, f, vself, entries, h, tab: PotenTables):
+    """nearSingInt (poten_py.m:495-692) with explicit subtraction of the
+    trapezoid contribution and Horner evaluation at dscaled."""
+    N, nv = X.shape[0] // 2, X.shape[1]
+    if nv == 1:
+        return np.zeros_like(X)
+    Nup = tab.Nup
+    Xup = interpft_vec(X, Nup)
+    fup = interpft_vec(f, Nup)
+    sa_up, _, _ = diff_prop(Xup)
+    far = all_exact_stokes_sl_target(Xup, sa_up, fup, X, None)
+    nearf = np.zeros((2 * N, nv))
+    interp = tab.interp
+    order = interp.shape[0]
+    p = (order + 2) // 2
+    beta = 1.1
+    for e in entries:
+        pn = np.mod(np.arange(e.icp - p + 1, e.icp - p + 1 + order), N)
+        velx = lagrange_eval(interp @ vself[pn, e.k1], e.theta)
+        vely = lagrange_eval(interp @ vself[pn + N, e.k1], e.theta)
+        tx, ty = X[e.j, e.k2], X[e.j + N, e.k2]
+        pot = exact_stokes_sl_points(Xup, sa_up, fup, np.array([[tx], [ty]]), [e.k1])
+        nearf[e.j, e.k2] -= pot[0, 0]
+        nearf[e.j + N, e.k2] -= pot[1, 0]
+        nx = (tx - e.nx) / e.dist
+        ny = (ty - e.ny) / e.dist
+        s = beta * h * np.arange(1, order)
+        XL = np.concatenate([e.nx + s * nx, e.ny + s * ny])[:, None]
+        lag = exact_stokes_sl_points(Xup, sa_up, fup, XL, [e.k1]).reshape(-1)
+        Px = interp @ np.concatenate([[velx], lag[:order - 1]])
+        Py = interp @ np.concatenate([[vely], lag[order - 1:]])
+        ds = e.dist / (beta * h * (order - 1))
+        nearf[e.j, e.k2] += lagrange_eval(Px, ds)
+        nearf[e.j + N, e.k2] += lagrange_eval(Py, ds)
+    return far + nearf
+
+
+# --------------------------------------------------------------------------
+# Background flow (mytorch/tstep_biem.py:849-952)
+# --------------------------------------------------------------------------
+
+
+def bg_flow(X, kind, speed=1.0, chan_width=1.0, vortex_size=1.0):
+    N = X.shape[0] // 2
+    x, y = X[:N], X[N:]
+    if kind == 'relaxation':
+        v = np.zeros_like(X)
+    elif kind == 'extensional':
+        v = np.vstack((-x, y))
+    elif kind == 'parabolic':
+        v = np.vstack((1 - (y / chan_width) ** 2, np.zeros_like(y)))
+    elif kind == 'taylorGreen':
+        s = np.pi / vortex_size
+        v = vortex_size * np.vstack((np.sin(x * s) * np.cos(y * s), -np.cos(x * s) * np.sin(y * s)))
+    elif kind == 'vortex':
+        cw = chan_width
+        v = np.vstack((np.sin(x / cw * np.pi) * np.cos(y / cw * np.pi),
+                       -np.cos(x / cw * np.pi) * np.sin(y / cw * np.pi)))
+    elif kind == 'shear':
+        v = np.vstack((y, np.zeros_like(y)))
+    else:
+        raise ValueError("Unknown or missing flow type in bg_flow.")
+    return v * speed
+
+
+# --------------------------------------------------------------------------
+# The implicit step (mytorch/tstep_biem.py:181-428, 430-610, 653-711)
+# --------------------------------------------------------------------------
+
+
+@dataclass
+class StepParams:
+    dt: float
+    kappa: float = 1.0
+    gmres_tol: float = 1e-10
+    gmres_maxiter: int = 1000
+    far_field: str = 'shear'
+    speed: float = 1.0
+    chan_width: float = 2.5
+    vortex_size: float = 2.5
+    near: str = 'py_hh'          # 'py_hh' (mytorch) or 'matlab'
+    use_preco: bool = True
+
+
+@dataclass
+class StepResult:
+    X: np.ndarray
+    sigma: np.ndarray
+    iters: int
+    iflag: bool
+    info: int
+
+
+def time_step(X, sigma, prm: StepParams, tab: PotenTables | None = None) -> StepResult:
+    """One implicit BIEM step (tstep_biem.py:181-428)."""
+    N, nv = X.shape[0] // 2, X.shape[1]
+    tab = tab or PotenTables(N)
+    ves = Capsule(X, prm.kappa)
+    G = stokes_sl_matrix(X, tab)
+    alpha = 1.0
+    if prm.near == 'py_hh':
+        near = naive_near_zone_info(X, interpft_vec(X, tab.Nup))
+    else:
+        entries, h = get_zone(X)
+    rhs1 = X + prm.dt * bg_flow(X, prm.far_field, prm.speed, prm.chan_width, prm.vortex_size) / alpha
+    rhs2 = ves.surface_div(X)
+    rhs = np.concatenate([rhs1, rhs2], axis=0).T.reshape(-1)
+
+    lu = None
+    if prm.use_preco:
+        Ben, Ten, Div = ves.compute_derivs()
+        lu = []
+        for k in range(nv):
+            M = np.zeros((3 * N, 3 * N))
+            GB = G[:, :, k] @ Ben[:, :, k]
+            GT = G[:, :, k] @ Ten[:, :, k]
+            M[:2 * N, :2 * N] = np.eye(2 * N) + prm.dt * prm.kappa * GB
+            M[:2 * N, 2 * N:] = -prm.dt * GT / alpha
+            M[2 * N:, :2 * N] = Div[:, :, k]
+            lu.append(sla.lu_factor(M))
+
+    counter = {'n': 0}
+
+    def matvec(v):
+        counter['n'] += 1
+        vr = np.asarray(v, dtype=np.float64).reshape(nv, 3, N)
+        Xm = vr[:, :2, :].reshape(nv, 2 * N).T
+        sig = vr[:, 2, :].T
+        f = ves.trac_jump(Xm, sig)
+        Gf = exact_stokes_sl_diag(G, f)
+        if prm.near == 'py_hh':
+            Fslp, _ = near_sing_int_hh(X, f, Gf, near, tab)
+        else:
+            Fslp = near_sing_int_matlab(X, f, Gf, entries, h, tab)
+        valPos = Xm - prm.dt * Gf / alpha - prm.dt * Fslp / alpha
+        valTen = ves.surface_div(Xm)
+        out = np.concatenate([valPos.reshape(2, N, nv), valTen.reshape(1, N, nv)], axis=0).reshape(3 * N, nv)
+        return out.T.reshape(-1)
+
+    def psolve(z):
+        zr = np.asarray(z, dtype=np.float64).reshape(nv, 3 * N)
+        return np.concatenate([sla.lu_solve(lu[k], zr[k]) for k in range(nv)])
+
+    n = 3 * N * nv
+    A = spla.LinearOperator((n, n), matvec=matvec)
+    x0 = np.concatenate([X, sigma], axis=0).T.reshape(-1)
+    if prm.use_preco:
+        Mop = spla.LinearOperator((n, n), matvec=psolve)
+        xs, info = spla.gmres(A, rhs, rtol=prm.gmres_tol, maxiter=prm.gmres_maxiter, M=Mop, x0=x0)
+    else:
+        xs, info = spla.gmres(A, rhs, rtol=prm.gmres_tol, maxiter=prm.gmres_maxiter, x0=x0)
+    xr = xs.reshape(nv, 3, N)
+    Xn = xr[:, :2, :].reshape(nv, 2 * N).T.copy()
+    sn = xr[:, 2, :].T.copy()
+    return StepResult(Xn, sn, counter['n'], info != 0, int(info))
+
+
+# --------------------------------------------------------------------------
+# Synthetic suspensions (seeded generators for the benchmark configurations)
+# --------------------------------------------------------------------------
+
+
+def ellipse_axes(reduced_area: float, area: float = np.pi):
+    """Semi-axes (a >= b) of the ellipse with the given reduced area and area."""
+    # reduced area of an ellipse with axes a, b: 4*pi*pi*a*b / L^2, L by Ramanujan-free quadrature
+    def ra(ratio):
+        t = np.arange(4096) * 2 * np.pi / 4096
+        L = np.sum(np.sqrt((ratio * np.sin(t)) ** 2 + np.cos(t) ** 2)) * 2 * np.pi / 4096
+        return 4 * np.pi * np.pi * ratio / L ** 2
+    lo, hi = 1.0, 20.0
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        if ra(mid) > reduced_area:
+            lo = mid
+        else:
+            hi = mid
+    ratio = 0.5 * (lo + hi)
+    b = math.sqrt(area / (np.pi * ratio))
+    return ratio * b, b

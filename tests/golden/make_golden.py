@@ -1,0 +1,212 @@
+"""Record golden fixtures from the Ves2Dpy reference (``mytorch/``).
+
+Run in the development container (the reference tree must be present):
+
+    python tests/golden/make_golden.py
+
+Each fixture is produced in a fresh subprocess because the FP64 promotion of
+``ref_shim.load(promote=True)`` rebinds torch dtypes process-wide.  Inputs
+come from the package's seeded generators, so the fixture files are
+reproducible.  The files are small ``.npz`` archives committed next to this
+script; tests read them without needing the reference.
+"""
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, HERE)
+sys.path.insert(0, ROOT)
+
+
+def _np(t):
+    return t.detach().cpu().numpy()
+
+
+def small_cluster(nv=6, N=16, seed=3, gap=0.02):
+    """Closely packed small suspension so that near pairs (< 1/N) exist."""
+    from ves2dpy_gb300.suspension import vesicle_shape
+    rng = np.random.default_rng(seed)
+    X = np.zeros((2 * N, nv))
+    # two rows of vesicles with small gaps, scaled to length ~1 so 1/N matters
+    for k in range(nv):
+        x, y = vesicle_shape(N, rng, 0.8, area=0.06)
+        X[:N, k] = x + (k % 3) * 0.32
+        X[N:, k] = y + (k // 3) * 0.30
+    return X
+
+
+def patch_exact_stokes_sl(R):
+    """Evaluate exactStokesSL_ per target column (the reference raises a shape
+    error at mytorch/biem_support.py:382 for multi-column targets)."""
+    torch = R.torch
+
+    def fixed(vesicle, f, Xtar=None, K1=None):
+        Ntar, ncol = Xtar.shape[0] // 2, Xtar.shape[1]
+        out = torch.zeros((2 * Ntar, ncol), dtype=torch.float64)
+        den = f * torch.tile(vesicle.sa, (2, 1)) * 2 * torch.pi / vesicle.N
+        xs = vesicle.X[:vesicle.N, K1].reshape(-1)
+        ys = vesicle.X[vesicle.N:, K1].reshape(-1)
+        dxs = den[:vesicle.N, K1].reshape(-1)
+        dys = den[vesicle.N:, K1].reshape(-1)
+        for k in range(ncol):
+            dx = Xtar[:Ntar, k][None, :] - xs[:, None]
+            dy = Xtar[Ntar:, k][None, :] - ys[:, None]
+            r2 = dx ** 2 + dy ** 2
+            c = (dx * dxs[:, None] + dy * dys[:, None]) / r2
+            lg = 0.5 * torch.log(r2)
+            out[:Ntar, k] = torch.sum(c * dx - lg * dxs[:, None], dim=0)
+            out[Ntar:, k] = torch.sum(c * dy - lg * dys[:, None], dim=0)
+        return out / (4 * torch.pi)
+
+    R.poten.exactStokesSL_ = fixed
+
+
+def make_prams(R, N, nv, dt, speed, tol=1e-10, kind='shear'):
+    torch = R.torch
+    prams = dict(N=N, nv=nv, dt=dt, T=10 * dt, kappa=1.0, viscCont=torch.ones(nv), gmresTol=tol,
+                 gmresMaxIter=200, areaLenTol=1e-2, repStrength=900, minDist=0.4, farFieldSpeed=speed,
+                 chanWidth=2.5, vortexSize=2.5)
+    options = dict(farField=kind, repulsion=False, correctShape=False, reparameterization=False,
+                   usePreco=True, matFreeWalls=False, confined=False)
+    return prams, options
+
+
+def job_far(promote):
+    import ref_shim
+    R = ref_shim.load(promote=promote)
+    torch = R.torch
+    X = small_cluster()
+    N, nv = X.shape[0] // 2, X.shape[1]
+    rng = np.random.default_rng(11)
+    f = rng.normal(size=(2 * N, nv))
+    Xt = torch.tensor(X)
+    ft = torch.tensor(f)
+    op = R.poten.Poten(N)
+    Xup = R.filter.interpft_vec(Xt, op.Nup)
+    fup = R.filter.interpft_vec(ft, op.Nup)
+    vesUp = R.capsules.capsules(Xup, None, None, 1.0, 1.0)
+    near = R.biem_support.naiveNearZoneInfo(Xt, Xup)
+    far1, ids1 = R.biem_support.allExactStokesSLTarget_compare1(Xup, vesUp.sa, fup, Xt)
+    far2 = R.biem_support.allExactStokesSLTarget_compare2(Xup, vesUp.sa, fup, Xt, *near[4])
+    far_noexcl = R.biem_support.allExactStokesSLTarget_compare2(
+        Xup, vesUp.sa, fup, Xt, torch.zeros(0, dtype=torch.long), torch.zeros(0, dtype=torch.long),
+        torch.zeros(0, dtype=torch.long))
+    # Poten.exactStokesSL: one target column, sources = all vesicles but 0
+    ves = R.capsules.capsules(Xt, None, None, 1.0, torch.ones(nv))
+    sl = R.poten.Poten.exactStokesSL(op, ves, ft, Xt[:, :1], list(range(1, nv)))
+    return dict(X=X, f=f, Xup=_np(Xup), fup=_np(fup), sa_up=_np(vesUp.sa),
+                closest_dist=_np(near[0]), idx_closest=_np(near[1]),
+                id1=_np(near[2][0]), id2=_np(near[2][1]), id1_hh=_np(near[3][0]), id2_hh=_np(near[3][1]),
+                ids0=_np(near[4][0]), ids1=_np(near[4][1]), ids2=_np(near[4][2]),
+                far1=_np(far1), c1_ids0=_np(ids1[0]), c1_ids1=_np(ids1[1]), c1_ids2=_np(ids1[2]),
+                far2=_np(far2), far_noexcl=_np(far_noexcl), exact_sl_col0=_np(sl))
+
+
+def job_capsules(promote):
+    import ref_shim
+    from ves2dpy_gb300.suspension import vesicle_shape
+    R = ref_shim.load(promote=promote)
+    torch = R.torch
+    out = {}
+    for N in (16, 32):
+        rng = np.random.default_rng(100 + N)
+        nv = 4
+        X = np.zeros((2 * N, nv))
+        for k in range(nv):
+            x, y = vesicle_shape(N, rng, 0.65 + 0.08 * k)
+            X[:N, k] = x + 3 * k
+            X[N:, k] = y - k
+        sig = rng.normal(size=(N, nv))
+        f = rng.normal(size=(2 * N, nv))
+        dtype = torch.float64 if promote else torch.float32
+        Xt = torch.tensor(X, dtype=dtype)
+        ves = R.capsules.capsules(Xt, None, None, 1.0, torch.ones(nv))
+        Ben, Ten, Div = ves.computeDerivs()
+        oc = R.curve.Curve()
+        ra, area, length = oc.geomProp(Xt)
+        op = R.poten.Poten(N)
+        G = op.stokesSLmatrix(ves)
+        out.update({
+            f'X{N}': X, f'sig{N}': sig, f'f{N}': f,
+            f'sa{N}': _np(ves.sa), f'xt{N}': _np(ves.xt), f'cur{N}': _np(ves.cur),
+            f'trac{N}': _np(ves.tracJump(Xt, torch.tensor(sig, dtype=dtype))),
+            f'sdiv{N}': _np(ves.surfaceDiv(torch.tensor(f, dtype=dtype))),
+            f'Ben{N}': _np(Ben), f'Ten{N}': _np(Ten), f'Div{N}': _np(Div),
+            f'ra{N}': _np(ra), f'area{N}': _np(area), f'len{N}': _np(length),
+            f'up{N}': _np(R.filter.interpft_vec(Xt, op.Nup)),
+            f'G{N}': _np(G), f'qw{N}': _np(op.qw[:, 0]), f'qp{N}': _np(op.qp),
+            f'Rlp{N}': _np(op.Restrict_LP), f'Plp{N}': _np(op.Prolong_LP),
+        })
+    return out
+
+
+def job_step(promote, which):
+    import ref_shim
+    from ves2dpy_gb300.suspension import config1_suspension
+    R = ref_shim.load(promote=promote)
+    torch = R.torch
+    if which == 'c1':
+        X = config1_suspension(32, 0)
+        dt, speed, nsteps = 1e-4, 2.0, 2 if promote else 1
+    else:
+        patch_exact_stokes_sl(R)
+        X = small_cluster(nv=4, N=16, seed=1)
+        dt, speed, nsteps = 1e-4, 2.0, 1
+    N, nv = X.shape[0] // 2, X.shape[1]
+    dtype = torch.float64 if promote else torch.float32
+    Xt = torch.tensor(X, dtype=dtype)
+    prams, options = make_prams(R, N, nv, dt, speed)
+    tt = R.tstep_biem.TStepBiem(Xt, None, options, prams)
+    sig = torch.zeros(N, nv, dtype=dtype)
+    out = dict(X0=X, dt=dt, speed=speed)
+    if which == 'near':
+        near = R.biem_support.naiveNearZoneInfo(Xt, R.filter.interpft_vec(Xt, tt.op.Nup))
+        out['n_near'] = len(near[4][0])
+        out['n_hh'] = len(near[3][0])
+        rng = np.random.default_rng(7)
+        f = torch.tensor(rng.normal(size=(2 * N, nv)))
+        ves = R.capsules.capsules(Xt, None, None, 1.0, torch.ones(nv))
+        G = tt.op.stokesSLmatrix(ves)
+        SLP = lambda F: tt.op.exactStokesSLdiag(ves, G, F)  # noqa: E731
+        LP, nearF = tt.op.nearSingInt_hh(ves, f, SLP, near, R.biem_support.wrapper_allExactStokesSLTarget_compare2,
+                                        ves, True)
+        out.update(f_near=_np(f), LP_near=_np(LP), nearField=_np(nearF))
+    for s in range(nsteps):
+        Xn, sig, _, _, it, iflag = tt.time_step(Xt, sig, None, None)
+        out[f'X{s + 1}'] = _np(Xn).astype(np.float64)
+        out[f'sig{s + 1}'] = _np(sig).astype(np.float64)
+        out[f'iter{s + 1}'] = int(it)
+        out[f'iflag{s + 1}'] = bool(iflag)
+        Xt = Xn
+    return out
+
+
+JOBS = {
+    'far_fp64': (job_far, True, ()),
+    'capsules_fp64': (job_capsules, True, ()),
+    'capsules_mixed': (job_capsules, False, ()),
+    'step_c1_fp64': (job_step, True, ('c1',)),
+    'step_c1_mixed': (job_step, False, ('c1',)),
+    'step_near_fp64': (job_step, True, ('near',)),
+}
+
+
+def main():
+    if len(sys.argv) > 2 and sys.argv[1] == '--job':
+        name = sys.argv[2]
+        fn, promote, extra = JOBS[name]
+        out = fn(promote, *extra)
+        np.savez_compressed(os.path.join(HERE, f'{name}.npz'), **out)
+        print('wrote', name)
+        return
+    names = sys.argv[1:] or list(JOBS)
+    for name in names:
+        subprocess.run([sys.executable, os.path.abspath(__file__), '--job', name], check=True)
+
+
+if __name__ == '__main__':
+    main()

@@ -1,0 +1,244 @@
+/*
+ * ves2d_gb300.h — C ABI of the GB300 (sm_103a) vesicle-suspension kernels.
+ *
+ * Every function returns an int status (VES_OK == 0).  All array arguments are
+ * caller-owned DEVICE pointers (float64 unless stated) on the device that was
+ * current when the context was created; ``stream`` is a cudaStream_t passed as
+ * void* (NULL = legacy default stream).  No entry point allocates device memory
+ * in a hot call: scratch is passed in as ``ws``/``ws_bytes`` and its size is
+ * given by the matching *_workspace() query.  Kernels never trap; device-side
+ * failures are reported through the returned status.
+ *
+ * Device layout ("vesicle-major", the transpose of the reference's X[2N, nv]):
+ *   X, f, velocities   [nv][2][n]  x-row then y-row of each vesicle
+ *   sigma (tension)    [nv][n]
+ *   G (single layer)   [nv][2N][2N] row-major
+ *   GMRES unknowns     [nv][3][N]  (x, y, sigma) — the reference's flattening
+ *                      torch.cat([X, sigma]).T.reshape(-1)
+ *
+ * Reference interfaces replaced (paths relative to the Ves2Dpy project):
+ *   see the comment above each declaration.
+ */
+#ifndef VES2D_GB300_H
+#define VES2D_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define VES_API __attribute__((visibility("default")))
+#else
+#define VES_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------- */
+#define VES_OK 0
+#define VES_ERR_SHAPE 1            /* bad sizes / unsupported N                  */
+#define VES_ERR_NONFINITE 2        /* NaN/Inf (poten.py:77-78 "NaN or Inf")      */
+#define VES_ERR_NEARLIST_OVERFLOW 3/* near-zone capacity exceeded               */
+#define VES_ERR_GMRES_MAXIT 4      /* GMRES did not reach tolerance (iflag)      */
+#define VES_ERR_CUDA 5             /* CUDA runtime error                          */
+#define VES_ERR_ARG 6              /* invalid argument (NULL, bad enum, ...)      */
+#define VES_ERR_TIMEOUT 7          /* a bounded device-side wait gave up          */
+#define VES_ERR_SINGULAR 8         /* zero pivot in a per-vesicle factorisation   */
+#define VES_ERR_WORKSPACE 9        /* workspace too small                         */
+
+/* arithmetic of the all-pairs Stokeslet sum */
+#define VES_PREC_FP64 0            /* FP64 throughout                              */
+#define VES_PREC_FP32C 1           /* FP32 pair terms, per-vesicle-pair centre      */
+                                   /* shift, compensated accumulation              */
+
+/* near-singular schemes */
+#define VES_NEAR_NONE 0            /* plain upsampled trapezoid rule, no exclusion */
+#define VES_NEAR_PY_HH 1           /* mytorch/poten.py:466-600 + biem_support.py:520-613 */
+#define VES_NEAR_MATLAB 2          /* matlab/poten_py.m:495-692 + capsules_py.m:194-643   */
+
+/* background flows (mytorch/tstep_biem.py:849-952) */
+#define VES_FLOW_RELAXATION 0
+#define VES_FLOW_EXTENSIONAL 1
+#define VES_FLOW_PARABOLIC 2
+#define VES_FLOW_TAYLOR_GREEN 3
+#define VES_FLOW_SHEAR 4
+#define VES_FLOW_VORTEX 5
+
+typedef struct ves_ctx ves_ctx;
+
+/* ---- context (immutable per-N quadrature tables; poten.py:15-37) ---------- */
+/* Replaces Poten.__init__ (mytorch/poten.py:15-37): builds, on the current
+ * device, the Alpert weights (poten.py:899-974), Fourier restriction and
+ * prolongation (fft1.py:209-231), spectral derivative and Lagrange tables. */
+VES_API int ves_ctx_create(int N, ves_ctx** out);
+VES_API int ves_ctx_destroy(ves_ctx* ctx);
+/* N, Nup = N*ceil(sqrt(N)) (poten.py:24), number of Alpert nodes */
+VES_API int ves_ctx_info(const ves_ctx* ctx, int* N, int* Nup, int* nquad);
+/* Text of the last error recorded on this thread (never NULL). */
+VES_API const char* ves_last_error(void);
+
+/* ---- curve geometry (curve_batch_compile.py, capsules.py) ------------------ */
+/* Curve.diffProp (curve_batch_compile.py:400-423) on the N grid (grid=0) or the
+ * upsampled Nup grid (grid=1, X then holds Nup points per vesicle).
+ * Outputs sa[nv][n], tang[nv][2][n], cur[nv][n]; any output may be NULL. */
+VES_API int ves_diff_prop(ves_ctx* ctx, int grid, int nv, const double* X, double* sa, double* tang,
+                  double* cur, void* stream);
+/* Curve.geomProp (curve_batch_compile.py:455-473): reduced area, area, length [nv]. */
+VES_API int ves_geom_prop(ves_ctx* ctx, int nv, const double* X, double* reduced_area, double* area,
+                  double* length, void* stream);
+/* interpft_vec (filter.py:192-194) from N to Nup points: in[nv][ncomp][N] ->
+ * out[nv][ncomp][Nup]. */
+VES_API int ves_upsample(ves_ctx* ctx, int nv, int ncomp, const double* in, double* out, void* stream);
+/* capsules.tracJump (capsules.py:54-80): f = -kappa d^4X/ds^4 + d/ds(sigma X_s).
+ * X, sigma may be read with per-vesicle strides (GMRES packing): vesicle k's
+ * positions start at X + k*x_stride, its tension at sigma + k*s_stride. */
+VES_API int ves_trac_jump(ves_ctx* ctx, int nv, double kappa, const double* isa, const double* tang,
+                  const double* X, long long x_stride, const double* sigma, long long s_stride,
+                  double* f, void* stream);
+/* capsules.surfaceDiv (capsules.py:82-89): out[nv][N] = d f/ds . X_s. */
+VES_API int ves_surface_div(ves_ctx* ctx, int nv, const double* isa, const double* tang, const double* f,
+                    long long f_stride, double* out, long long out_stride, void* stream);
+/* capsules.computeDerivs (capsules.py:91-206): Ben[nv][2N][2N], Ten[nv][2N][N],
+ * Div[nv][N][2N] (real parts of the complex products, as in the reference). */
+VES_API int ves_compute_derivs(ves_ctx* ctx, int nv, const double* isa, const double* tang, double* Ben,
+                       double* Ten, double* Div, void* ws, size_t ws_bytes, void* stream);
+VES_API size_t ves_compute_derivs_workspace(ves_ctx* ctx, int nv);
+/* TStepBiem.bg_flow (tstep_biem.py:849-952): v[nv][2][N] = speed * u(X). */
+VES_API int ves_bg_flow(ves_ctx* ctx, int nv, int flow, double speed, double chan_width,
+                double vortex_size, const double* X, double* v, void* stream);
+
+/* ---- single-layer self interaction (poten.py:40-99, 213-224) -------------- */
+/* Poten.stokesSLmatrix: Alpert log-singular quadrature on the Nup grid,
+ * restricted to N (G = R*Gup*P).  precision: VES_PREC_FP64, or VES_PREC_FP32C
+ * (kernel values and the R*Gup*P products in FP32, FP64 weights and output). */
+VES_API int ves_stokes_sl_matrix(ves_ctx* ctx, int nv, const double* X, int precision, double* G,
+                         void* ws, size_t ws_bytes, void* stream);
+VES_API size_t ves_stokes_sl_matrix_workspace(ves_ctx* ctx, int nv, int precision);
+/* Poten.exactStokesSLdiag: out[k] = G[k] @ f[k], G[nv][m][m]. */
+VES_API int ves_sl_diag(int nv, int m, const double* G, const double* f, double* out, void* stream);
+
+/* ---- near zone ------------------------------------------------------------- */
+/* Near-pair lists.  Every target vesicle t owns up to ``maxc`` candidate source
+ * vesicles (bounding boxes closer than the threshold), in ascending order:
+ *   cand_count[nv], cand_src[nv][maxc],
+ *   excl_mask[nv][maxc][ceil(N/32)]   bit i: target point i of t is near source s
+ *                                     (far-field exclusion; biem_support.py:72,
+ *                                      the (ids0, ids1, ids2) of :610-613)
+ *   hh_mask  [nv][maxc][Nup/32]       bit u: upsampled point u of s is near a
+ *                                     point of t (the (id1_hh, id2_hh) list)
+ * MATLAB scheme entries (capsules_py.m:194-467): up to ``max_entries`` records
+ *   ent_tsj[max][3] int (target vesicle, source vesicle, target point),
+ *   ent_icp[max] int, ent_geo[max][4] double (dist, nearest x, nearest y, theta),
+ *   *n_entries (device int). */
+typedef struct ves_near_lists {
+  int maxc;
+  int* cand_count;
+  int* cand_src;
+  uint32_t* excl_mask;
+  uint32_t* hh_mask;
+  int max_entries;
+  int* n_entries;
+  int* ent_tsj;
+  int* ent_icp;
+  double* ent_geo;
+} ves_near_lists;
+
+/* naiveNearZoneInfo (biem_support.py:520-613): threshold 1/N by default
+ * (thresh <= 0), Euclidean distance between coarse targets and upsampled
+ * sources of every other vesicle. Xup may be NULL (computed into ws). */
+VES_API int ves_near_zone_py(ves_ctx* ctx, int nv, const double* X, const double* Xup, double thresh,
+                     ves_near_lists* nl, void* ws, size_t ws_bytes, void* stream);
+/* capsules_py.m getZone (relate==1) with closestPnt (:581-643): near if the
+ * Newton closest point on the 7-point local interpolant is closer than h
+ * (h <= 0: min vesicle length / N). */
+VES_API int ves_near_zone_matlab(ves_ctx* ctx, int nv, const double* X, double h, ves_near_lists* nl,
+                         void* ws, size_t ws_bytes, void* stream);
+VES_API size_t ves_near_zone_workspace(ves_ctx* ctx, int nv);
+
+/* ---- layer potentials between vesicles ------------------------------------ */
+/* All-pairs Stokeslet sum, allExactStokesSLTarget_compare1/2
+ * (biem_support.py:7-272, poten.py:280-336):
+ *   u(x) = 1/(4 pi) sum_src [ -1/2 log|r|^2 den + (r.den) r/|r|^2 ],
+ *   den = f * sa * 2 pi / ns,
+ * sources Xsrc[nsrc][2][ns], den[nsrc][2][ns]; targets Xtar[nt][2][ntp].
+ * self_idx[nt] (or NULL): source vesicle skipped for target column t.
+ * nl (or NULL): candidate lists whose excl_mask removes (target point, source
+ * vesicle) pairs (requires nt == nsrc, ntp == N of ctx).  Result written to
+ * out[nt][2][ntp].  precision: VES_PREC_FP64 or VES_PREC_FP32C. */
+VES_API int ves_farfield(ves_ctx* ctx, int precision, int nsrc, int ns, const double* Xsrc,
+                 const double* den, int nt, int ntp, const double* Xtar, const int* self_idx,
+                 const ves_near_lists* nl, double* out, void* ws, size_t ws_bytes, void* stream);
+VES_API size_t ves_farfield_workspace(ves_ctx* ctx, int precision, int nsrc, int ns, int nt, int ntp);
+/* den[nv][2][ns] = f * sa * 2*pi/ns  (biem_support.py:39) */
+VES_API int ves_density(int nv, int ns, const double* f, const double* sa, double* den, void* stream);
+
+/* nearSingInt_hh (poten.py:466-600) / nearSingInt (poten_py.m:495-692):
+ * LP[nv][2][N] = far field of f over Nup-upsampled sources with the near
+ * pairs removed, plus the near correction built from vself = G f.
+ * scheme: VES_NEAR_PY_HH or VES_NEAR_MATLAB (lists from the matching
+ * ves_near_zone_*), VES_NEAR_NONE (nl ignored).  near_only (or NULL)
+ * receives the correction alone (the reference's second return value). */
+VES_API int ves_near_sing_int(ves_ctx* ctx, int scheme, int precision, int nv, const double* X,
+                      const double* sa_up, const double* Xup, const double* f,
+                      const double* vself, const ves_near_lists* nl, double h, double* LP,
+                      double* near_only, void* ws, size_t ws_bytes, void* stream);
+VES_API size_t ves_near_sing_int_workspace(ves_ctx* ctx, int precision, int nv);
+
+/* ---- the implicit BIEM step (tstep_biem.py:181-428) ------------------------ */
+typedef struct ves_step_params {
+  double dt;
+  double kappa;
+  double gmres_tol;      /* relative tolerance (scipy rtol) */
+  int gmres_maxiter;     /* outer restart cycles (scipy maxiter) */
+  int gmres_restart;     /* 20 = scipy default */
+  int use_preco;         /* block-diagonal LU preconditioner (tstep_biem.py:653-711) */
+  int flow;              /* VES_FLOW_* */
+  double speed, chan_width, vortex_size;
+  int near_scheme;       /* VES_NEAR_* */
+  int farfield_precision;/* VES_PREC_* for the all-pairs sum */
+  int sl_precision;      /* VES_PREC_* for the Alpert matrix build */
+  int maxc;              /* candidate capacity per vesicle (0 = default 64) */
+  int max_entries;       /* MATLAB near entries capacity (0 = default) */
+} ves_step_params;
+
+typedef struct ves_step_result {
+  int matvecs;           /* number of time_matvec calls (the reference's iter) */
+  int inner_iters;       /* GMRES inner iterations */
+  int info;              /* 0 converged; maxiter (scipy's code) if the restart
+                            cycles ran out; -1 if the true residual stopped
+                            decreasing (3 cycles without halving) above the
+                            tolerance, i.e. the arithmetic's noise floor */
+  double resid;          /* final true residual norm / ||b|| */
+  int n_near_pairs;      /* (target point, source vesicle) pairs excluded */
+  int n_near_entries;    /* near-correction entries applied */
+} ves_step_result;
+
+/* TStepBiem.time_step: X[nv][2][N], sigma[nv][N] -> Xout, sigma_out (may alias
+ * the inputs).  Unconfined, viscosity contrast 1, no repulsion (the only
+ * branches the benchmark configurations use). */
+VES_API int ves_biem_step(ves_ctx* ctx, const ves_step_params* prm, int nv, const double* X,
+                  const double* sigma, double* Xout, double* sigma_out, ves_step_result* res,
+                  void* ws, size_t ws_bytes, void* stream);
+VES_API size_t ves_biem_step_workspace(ves_ctx* ctx, const ves_step_params* prm, int nv);
+
+/* ---- measurement utilities (no counterpart in the reference) -------------- */
+typedef struct ves_stats {
+  long long kernel_launches;  /* kernels launched through this library (all contexts) */
+  long long farfield_launches;/* all-pairs kernel launches timed on this context        */
+  double farfield_ms;         /* their summed CUDA-event duration                       */
+  double farfield_pairs;      /* (target point, source point) pairs they evaluated      */
+} ves_stats;
+/* Enable/disable CUDA-event timing of the all-pairs kernel on ``ctx`` (events
+ * are recorded on the launching stream around each launch; off by default). */
+VES_API int ves_ctx_set_timing(ves_ctx* ctx, int on);
+/* Read (and with reset != 0 clear) the counters; synchronises pending events. */
+VES_API int ves_ctx_stats(ves_ctx* ctx, ves_stats* out, int reset);
+/* Measured MUFU throughput of this GPU: lg2.approx + rcp.approx operations
+ * per second over all SMs (a ~0.1 s probe on ``stream``). */
+VES_API int ves_probe_sfu_peak(double* ops_per_second, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VES2D_GB300_H */

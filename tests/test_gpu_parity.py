@@ -1,0 +1,187 @@
+"""GPU parity of the C-ABI kernels against the reference golden fixtures and
+the FP64 oracle.
+
+Tolerances (relative, max-norm): FP64 paths 1e-10; FP32-compensated far field
+1e-5; the mixed-precision Alpert matrix 1e-5.
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import ves2d_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10
+FP32_TOL = 1e-5
+
+
+def dev():
+    return torch.device("cuda:0")
+
+
+def T(a):
+    return torch.tensor(np.asarray(a), dtype=torch.float64, device=dev())
+
+
+def rel(a, b):
+    a = a.detach().cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+@pytest.mark.parametrize("N", [16, 32])
+def test_capsule_operators(golden, N):
+    from ves2dpy_gb300.capsules import capsules
+    from ves2dpy_gb300.curve import Curve
+    g = golden("capsules_fp64")
+    X, sig, f = g[f"X{N}"], g[f"sig{N}"], g[f"f{N}"]
+    ves = capsules(T(X), None, None, 1.0, 1.0)
+    assert rel(ves.sa, g[f"sa{N}"]) < FP64_TOL
+    assert rel(ves.xt, g[f"xt{N}"]) < FP64_TOL
+    assert rel(ves.cur, g[f"cur{N}"]) < FP64_TOL
+    assert rel(ves.tracJump(T(X), T(sig)), g[f"trac{N}"]) < FP64_TOL
+    assert rel(ves.surfaceDiv(T(f)), g[f"sdiv{N}"]) < FP64_TOL
+    Ben, Ten, Div = ves.computeDerivs()
+    assert rel(Ben, g[f"Ben{N}"]) < FP64_TOL
+    assert rel(Ten, g[f"Ten{N}"]) < FP64_TOL
+    assert rel(Div, g[f"Div{N}"]) < FP64_TOL
+    ra, area, length = Curve().geomProp(T(X))
+    assert rel(area, g[f"area{N}"]) < FP64_TOL and rel(length, g[f"len{N}"]) < FP64_TOL
+
+
+@pytest.mark.parametrize("N", [16, 32])
+def test_upsample(golden, N):
+    from ves2dpy_gb300.filter import interpft_vec
+    g = golden("capsules_fp64")
+    tab = O.PotenTables(N)
+    assert rel(interpft_vec(T(g[f"X{N}"]), tab.Nup), g[f"up{N}"]) < FP64_TOL
+
+
+@pytest.mark.parametrize("N", [16, 32])
+def test_alpert_matrix(golden, N):
+    from ves2dpy_gb300.capsules import capsules
+    from ves2dpy_gb300.poten import Poten
+    g = golden("capsules_fp64")
+    ves = capsules(T(g[f"X{N}"]), None, None, 1.0, 1.0)
+    op = Poten(N)
+    assert rel(op.stokesSLmatrix(ves, "fp64"), g[f"G{N}"]) < FP64_TOL
+    assert rel(op.stokesSLmatrix(ves, "fp32c"), g[f"G{N}"]) < FP32_TOL
+
+
+def test_near_zone_ids(golden):
+    from ves2dpy_gb300.biem_support import naiveNearZoneInfo
+    g = golden("far_fp64")
+    near = naiveNearZoneInfo(T(g["X"]), T(g["Xup"]))
+    ids = near[4]
+    for got, key in zip(ids, ["ids0", "ids1", "ids2"]):
+        np.testing.assert_array_equal(got, g[key])
+    id1, id2 = near[2]
+    np.testing.assert_array_equal(id1, g["id1"])
+    np.testing.assert_array_equal(id2, g["id2"])
+    h1, h2 = near[3]
+    np.testing.assert_array_equal(h1, g["id1_hh"])
+    np.testing.assert_array_equal(h2, g["id2_hh"])
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", FP64_TOL), ("fp32c", FP32_TOL)])
+def test_far_field_compare(golden, prec, tol):
+    from ves2dpy_gb300 import biem_support as B
+    g = golden("far_fp64")
+    far2 = B.allExactStokesSLTarget_compare2(T(g["Xup"]), T(g["sa_up"]), T(g["fup"]), T(g["X"]), g["ids0"],
+                                             g["ids1"], g["ids2"], precision=prec)
+    assert rel(far2, g["far2"]) < tol
+    far0 = B.allExactStokesSLTarget_compare2(T(g["Xup"]), T(g["sa_up"]), T(g["fup"]), T(g["X"]), [], [], [],
+                                             precision=prec)
+    assert rel(far0, g["far_noexcl"]) < tol
+    far1, ids = B.allExactStokesSLTarget_compare1(T(g["Xup"]), T(g["sa_up"]), T(g["fup"]), T(g["X"]),
+                                                  precision=prec)
+    assert rel(far1, g["far1"]) < tol
+    for got, key in zip(ids, ["c1_ids0", "c1_ids1", "c1_ids2"]):
+        np.testing.assert_array_equal(got, g[key])
+
+
+def test_exact_stokes_sl_column(golden):
+    from ves2dpy_gb300.capsules import capsules
+    from ves2dpy_gb300.poten import Poten
+    g = golden("far_fp64")
+    X = T(g["X"])
+    ves = capsules(X, None, None, 1.0, 1.0)
+    nv = X.shape[1]
+    sl = Poten(X.shape[0] // 2).exactStokesSL(ves, T(g["f"]), X[:, :1], list(range(1, nv)))
+    assert rel(sl, g["exact_sl_col0"]) < FP64_TOL
+    with pytest.raises(TypeError):
+        Poten(X.shape[0] // 2).exactStokesSL(ves, T(g["f"]), X[:, :2], [1])
+
+
+def test_near_sing_int_hh(golden):
+    from ves2dpy_gb300.biem_support import naiveNearZoneInfo
+    from ves2dpy_gb300.capsules import capsules
+    from ves2dpy_gb300.poten import Poten
+    g = golden("step_near_fp64")
+    X = T(g["X0"])
+    N = X.shape[0] // 2
+    ves = capsules(X, None, None, 1.0, 1.0)
+    op = Poten(N)
+    G = op.stokesSLmatrix(ves, "fp64")
+    near = naiveNearZoneInfo(X)
+    LP, nearF = op.nearSingInt_hh(ves, T(g["f_near"]), lambda F: op.exactStokesSLdiag(ves, G, F), near, None, ves,
+                                  True)
+    assert rel(nearF, g["nearField"]) < FP64_TOL
+    assert rel(LP, g["LP_near"]) < FP64_TOL
+
+
+def _step(X, dt, speed, near="py_hh", ff="fp64", sl="fp64", sig=None):
+    from ves2dpy_gb300.tstep_biem import TStepBiem
+    N, nv = X.shape[0] // 2, X.shape[1]
+    prams = dict(dt=dt, kappa=1.0, gmresTol=1e-10, gmresMaxIter=200, farFieldSpeed=speed, viscCont=[1.0] * nv)
+    options = dict(farField="shear", usePreco=True, repulsion=False)
+    tt = TStepBiem(T(X), None, options, prams, near=near, farfield_precision=ff, sl_precision=sl)
+    sig = torch.zeros(N, nv, dtype=torch.float64, device=dev()) if sig is None else T(sig)
+    return tt.time_step(T(X), sig)
+
+
+def test_time_step_config1_fp64(golden):
+    g = golden("step_c1_fp64")
+    X, sig = g["X0"], None
+    for s in (1, 2):
+        Xn, sn, _, _, it, iflag = _step(X, float(g["dt"]), float(g["speed"]), sig=sig)
+        assert not iflag
+        assert it == int(g[f"iter{s}"])
+        assert rel(Xn, g[f"X{s}"]) < FP64_TOL
+        assert rel(sn, g[f"sig{s}"]) < 1e-8
+        X, sig = Xn.cpu().numpy(), sn.cpu().numpy()
+
+
+def test_time_step_near_fp64(golden):
+    g = golden("step_near_fp64")
+    Xn, sn, _, _, it, iflag = _step(g["X0"], float(g["dt"]), float(g["speed"]))
+    assert not iflag and it == int(g["iter1"])
+    assert rel(Xn, g["X1"]) < FP64_TOL
+    assert rel(sn, g["sig1"]) < 1e-8
+
+
+def test_time_step_config1_mixed(golden):
+    """FP32C far field and Alpert matrix against the FP64 reference step."""
+    g = golden("step_c1_fp64")
+    Xn, sn, _, _, it, iflag = _step(g["X0"], float(g["dt"]), float(g["speed"]), ff="fp32c", sl="fp32c")
+    assert rel(Xn, g["X1"]) < FP32_TOL
+
+
+def test_time_step_matlab_near_vs_oracle():
+    """MATLAB near-singular scheme against its CPU FP64 restatement."""
+    import sys
+    sys.path.insert(0, "tests/golden")
+    from ves2dpy_gb300.suspension import vesicle_shape
+    rng = np.random.default_rng(1)
+    N, nv = 16, 4
+    X = np.zeros((2 * N, nv))
+    for k in range(nv):
+        x, y = vesicle_shape(N, rng, 0.8, area=0.06)
+        X[:N, k] = x + (k % 3) * 0.32
+        X[N:, k] = y + (k // 3) * 0.30
+    prm = O.StepParams(dt=1e-4, speed=2.0, near="matlab")
+    ref = O.time_step(X, np.zeros((N, nv)), prm, O.PotenTables(N))
+    Xn, sn, _, _, it, iflag = _step(X, 1e-4, 2.0, near="matlab")
+    assert not iflag
+    assert abs(it - ref.iters) <= 1
+    assert rel(Xn, ref.X) < 1e-9

@@ -1,0 +1,129 @@
+// Internal declarations shared by the ves2d translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/ves2d_gb300.h"
+#include "ves_common.cuh"
+
+// Per-N constant tables, resident on one device (created by ves_ctx_create).
+struct ves_ctx {
+  int N, Nup, m, nquad, device;
+  int nwords_N;   // ceil(N/32)
+  int nwords_up;  // ceil(Nup/32)
+  void* d_buf;    // single allocation holding every table below
+  // FP64 tables
+  double* d1N;     // [N]    first-derivative circulant on the N grid (Nyquist zeroed)
+  double* d1Nup;   // [Nup]  same on the Nup grid
+  double* pc;      // [Nup]  N->Nup prolongation circulant: P[u][i] = pc[(u - m i) mod Nup]
+  double* pcd;     // [Nup]  its derivative (d/dtheta of the interpolant)
+  double* qw;      // [nquad] Alpert weights (already / 4pi)
+  double* cq;      // [14][Nup] coarse cardinal at the 14 off-grid Alpert nodes
+  double* adense;  // [14][Nup] Nup-grid trig interpolation rows of the 14 off-grid nodes
+  double* Rm;      // [N][Nup] restriction
+  double* Pm;      // [Nup][N] prolongation
+  double* lag;     // [7][7]  Lagrange interpolation matrix (poten.py:977-990)
+  // FP32 copies used by the mixed-precision Alpert build
+  float* Rm32;
+  float* Pm32;
+  float* adense32;
+  float* qw32;
+  VesDeviceStatus* status;  // device status word (reset per API call)
+  VesDeviceStatus* h_status;// pinned host mirror
+  double* h_scal;            // pinned host scalars (GMRES read-back), 256 doubles
+  // optional timing of the all-pairs kernel
+  int timing;
+  int n_ev;                  // recorded event pairs not yet accumulated
+  cudaEvent_t ev[2 * 256];
+  double ev_pairs[256];
+  long long ff_launches;
+  double ff_ms, ff_pairs;
+};
+
+// launch accounting (every kernel launch site calls ves_count_launch)
+void ves_count_launch(int n = 1);
+// all-pairs kernel timing hooks (no-ops unless timing is on)
+void ves_ff_timing_begin(ves_ctx* c, cudaStream_t s);
+void ves_ff_timing_end(ves_ctx* c, cudaStream_t s, double pairs);
+
+// status plumbing -----------------------------------------------------------
+int ves_reset_status(ves_ctx* ctx, cudaStream_t s);
+int ves_check_status(ves_ctx* ctx, cudaStream_t s, const char* stage);  // syncs the stream
+int ves_launch_check(const char* what);                                 // cudaGetLastError
+
+// workspace carving ------------------------------------------------------------
+struct WsCarver {
+  char* base;
+  size_t cap, off;
+  bool sizing;  // true: only count bytes
+  WsCarver(void* b, size_t c) : base((char*)b), cap(c), off(0), sizing(b == nullptr) {}
+  template <typename T>
+  T* take(size_t count) {
+    off = (off + 255) & ~(size_t)255;
+    T* p = sizing ? nullptr : (T*)(base + off);
+    off += count * sizeof(T);
+    return p;
+  }
+  bool ok() const { return sizing || off <= cap; }
+};
+
+// launchers (implemented in the .cu files) ------------------------------------
+// spectral / geometry
+void launch_upsample(const ves_ctx* c, int nv, int ncomp, const double* in, long long in_stride,
+                     double* out, cudaStream_t s);
+void launch_upsample_deriv(const ves_ctx* c, int nv, const double* X, double* Xup, double* dXup,
+                           double* sa_up, cudaStream_t s);
+void launch_diff_prop(const ves_ctx* c, int grid, int nv, const double* X, double* sa, double* isa,
+                      double* tang, double* cur, cudaStream_t s);
+void launch_geom_prop(const ves_ctx* c, int nv, const double* X, double* ra, double* area,
+                      double* length, cudaStream_t s);
+void launch_trac_jump(const ves_ctx* c, int nv, double kappa, const double* isa, const double* tang,
+                      const double* X, long long xs, const double* sig, long long ss, double* f,
+                      cudaStream_t s);
+void launch_surface_div(const ves_ctx* c, int nv, const double* isa, const double* tang,
+                        const double* f, long long fs, double* out, long long os, cudaStream_t s);
+void launch_bg_flow(int nv, int N, int flow, double speed, double cw, double vs, const double* X,
+                    double* v, cudaStream_t s);
+void launch_density(int nv, int ns, const double* f, const double* sa, double* den, cudaStream_t s);
+int derivs_and_precond(ves_ctx* c, int nv, const double* isa, const double* tang, const double* G,
+                       double dt, double kappa, double* Ben, double* Ten, double* Div, double* M,
+                       WsCarver& ws, cudaStream_t s);
+
+// dense per-vesicle algebra
+void launch_bgemm_f64(int batch, int M, int N, int K, double alpha, const double* A, int lda,
+                      long long sA, const double* B, int ldb, long long sB, double beta, double* C,
+                      int ldc, long long sC, cudaStream_t s);
+void launch_bgemm_f32(int batch, int M, int N, int K, float alpha, const float* A, int lda,
+                      long long sA, const float* B, int ldb, long long sB, float beta, float* C,
+                      int ldc, long long sC, cudaStream_t s);
+void launch_bgemv_f64(int nv, int m, int n, const double* A, const double* x, long long xs,
+                      double* y, long long ys, cudaStream_t s);
+int launch_lu_factor(ves_ctx* c, int nv, int n, double* A, int* piv, cudaStream_t s);
+void launch_lu_solve(int nv, int n, const double* LU, const int* piv, const double* b, double* x,
+                     cudaStream_t s);
+
+// Alpert
+int alpert_sl_matrix(ves_ctx* c, int nv, const double* X, int precision, double* G, WsCarver& ws,
+                     cudaStream_t s);
+
+// far field
+int farfield_run(ves_ctx* c, int precision, int nsrc, int ns, const double* Xsrc, const double* den,
+                 int nt, int ntp, const double* Xtar, const int* self_idx, const ves_near_lists* nl,
+                 double* out, WsCarver& ws, cudaStream_t s);
+
+// near zone / near-singular corrections
+int near_zone_py(ves_ctx* c, int nv, const double* X, const double* Xup, double thresh,
+                 const ves_near_lists* nl, WsCarver& ws, cudaStream_t s);
+int near_zone_matlab(ves_ctx* c, int nv, const double* X, double h, const ves_near_lists* nl,
+                     WsCarver& ws, cudaStream_t s);
+int near_sing_int_run(ves_ctx* c, int scheme, int precision, int nv, const double* X,
+                      const double* sa_up, const double* Xup, const double* f, const double* vself,
+                      const ves_near_lists* nl, double h, double* LP, double* near_only, WsCarver& ws,
+                      cudaStream_t s);
+
+// vector kernels (GMRES)
+void launch_dot_partials(long long n, const double* a, const double* b, double* partials,
+                         cudaStream_t s);
+int dot_partial_blocks();

@@ -1,0 +1,535 @@
+// The implicit BIEM time step (TStepBiem.time_step, mytorch/tstep_biem.py:181-428)
+// with its GMRES matvec (time_matvec, :430-610) and block-diagonal LU
+// preconditioner (preconditionerBD, :653-711).
+//
+// GMRES restates scipy.sparse.linalg.gmres (the solver the reference calls at
+// tstep_biem.py:381): left preconditioning, restart 20, modified Gram-Schmidt,
+// LAPACK lartg Givens rotations and SciPy's inner/outer tolerance control.
+// Every vector operation runs on the device; the host keeps the (restart+1)
+// x restart Hessenberg matrix, whose current column (at most 22 numbers) is
+// read back once per inner iteration to decide convergence.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "ves_internal.h"
+
+namespace {
+
+__global__ void finalize_dot_kernel(const double* __restrict__ partials, int np, double* __restrict__ out,
+                                    int take_sqrt) {
+  __shared__ double red[512];
+  red[threadIdx.x] = threadIdx.x < np ? partials[threadIdx.x] : 0.0;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = take_sqrt ? sqrt(red[0]) : red[0];
+}
+
+// w -= h * v with h = sum(partials) (fixed-order), block 0 stores h
+__global__ void __launch_bounds__(512) mgs_axpy_kernel(long long n, const double* __restrict__ partials, int np,
+                                                       double* __restrict__ w, const double* __restrict__ v,
+                                                       double* __restrict__ hout) {
+  __shared__ double red[512];
+  red[threadIdx.x] = threadIdx.x < np ? partials[threadIdx.x] : 0.0;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  const double h = red[0];
+  if (blockIdx.x == 0 && threadIdx.x == 0) *hout = h;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    w[i] -= h * v[i];
+}
+
+// dst = src * (1/scal) unless skip(scal, ref): the "v *= 1/tmp" of SciPy
+__global__ void scale_inv_kernel(long long n, double* __restrict__ dst, const double* __restrict__ src,
+                                 const double* __restrict__ scal, const double* __restrict__ ref, double eps) {
+  const double h1 = *scal;
+  const bool brk = ref ? (h1 <= eps * (*ref)) : false;
+  const double inv = 1.0 / h1;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dst[i] = brk ? src[i] : src[i] * inv;
+}
+
+__global__ void sub_kernel(long long n, double* __restrict__ r, const double* __restrict__ b,
+                           const double* __restrict__ a) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    r[i] = b[i] - a[i];
+}
+
+// x += sum_k y[k] V[k]  (accumulated in k order, then added)
+__global__ void update_x_kernel(long long n, int cnt, const double* __restrict__ y, const double* __restrict__ V,
+                                double* __restrict__ x) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double t = 0.0;
+    for (int k = 0; k < cnt; ++k) t = fma(y[k], V[(long long)k * n + i], t);
+    x[i] += t;
+  }
+}
+
+// pack [X + dt*vinf ; surfaceDiv(X)] and [X ; sigma]
+__global__ void pack_kernel(int nv, int N, const double* __restrict__ A2, const double* __restrict__ B1,
+                            double* __restrict__ out) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)nv * 3 * N) return;
+  const long long k = idx / (3 * N), r = idx % (3 * N);
+  out[idx] = (r < 2 * N) ? A2[k * 2 * N + r] : B1[k * N + (r - 2 * N)];
+}
+
+__global__ void rhs_pos_kernel(long long n, double dt, const double* __restrict__ X, const double* __restrict__ v,
+                               double* __restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = X[i] + dt * v[i];
+}
+
+__global__ void unpack_kernel(int nv, int N, const double* __restrict__ x, double* __restrict__ X,
+                              double* __restrict__ sig) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)nv * 3 * N) return;
+  const long long k = idx / (3 * N), r = idx % (3 * N);
+  if (r < 2 * N)
+    X[k * 2 * N + r] = x[idx];
+  else
+    sig[k * N + (r - 2 * N)] = x[idx];
+}
+
+// valPos = ((-(dt*Gf)) - dt*LP) + Xm  (tstep_biem.py:541-576, alpha = 1)
+__global__ void combine_pos_kernel(int nv, int N, double dt, const double* __restrict__ v,
+                                   const double* __restrict__ Gf, const double* __restrict__ LP,
+                                   double* __restrict__ out) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)nv * 2 * N) return;
+  const long long k = idx / (2 * N), r = idx % (2 * N);
+  double val = -(dt * Gf[idx]);
+  val -= dt * LP[idx];
+  val += v[k * 3 * N + r];
+  out[k * 3 * N + r] = val;
+}
+
+inline unsigned vec_grid(long long n) {
+  long long g = (n + 511) / 512;
+  if (g > 4096) g = 4096;
+  if (g < 1) g = 1;
+  return (unsigned)g;
+}
+
+// LAPACK dlartg (3.10+): c >= 0, r carries the sign of f.
+void lartg(double f, double g, double& c, double& s, double& r) {
+  if (g == 0.0) {
+    c = 1.0;
+    s = 0.0;
+    r = f;
+  } else if (f == 0.0) {
+    c = 0.0;
+    s = (g > 0) ? 1.0 : -1.0;
+    r = fabs(g);
+  } else {
+    const double d = sqrt(f * f + g * g);
+    c = fabs(f) / d;
+    r = (f > 0) ? d : -d;
+    s = g / r;
+  }
+}
+
+struct StepState {
+  ves_ctx* c;
+  const ves_step_params* prm;
+  int nv, N, Nup;
+  long long n;
+  cudaStream_t s;
+  const double* X;  // positions at the start of the step [nv][2][N]
+  // geometry of the step
+  double *sa, *isa, *tang, *Xup, *sa_up, *G, *LU;
+  int* piv;
+  ves_near_lists nl;
+  double h;
+  // matvec temporaries
+  double *f, *Gf, *LP;
+  char* scratch;
+  size_t scratch_bytes;
+  int matvecs;
+};
+
+// out = A v (time_matvec, tstep_biem.py:430-610), v and out in [nv][3][N]
+int matvec(StepState& S, const double* v, double* out) {
+  ves_ctx* c = S.c;
+  const int nv = S.nv, N = S.N;
+  S.matvecs++;
+  launch_trac_jump(c, nv, S.prm->kappa, S.isa, S.tang, v, 3LL * N, v + 2 * N, 3LL * N, S.f, S.s);
+  launch_bgemv_f64(nv, 2 * N, 2 * N, S.G, S.f, 2LL * N, S.Gf, 2LL * N, S.s);
+  WsCarver sub(S.scratch, S.scratch_bytes);
+  int rc = near_sing_int_run(c, S.prm->near_scheme, S.prm->farfield_precision, nv, S.X, S.sa_up, S.Xup, S.f, S.Gf,
+                             &S.nl, S.h, S.LP, nullptr, sub, S.s);
+  if (rc) return rc;
+  ves_count_launch();
+  combine_pos_kernel<<<ceil_div((long long)nv * 2 * N, 256), 256, 0, S.s>>>(nv, N, S.prm->dt, v, S.Gf, S.LP, out);
+  launch_surface_div(c, nv, S.isa, S.tang, v, 3LL * N, out + 2 * N, 3LL * N, S.s);
+  return ves_launch_check("matvec");
+}
+
+int psolve(StepState& S, const double* z, double* out) {
+  if (!S.prm->use_preco) {
+    return ves_cuda_status(cudaMemcpyAsync(out, z, S.n * sizeof(double), cudaMemcpyDeviceToDevice, S.s), "psolve copy");
+  }
+  launch_lu_solve(S.nv, 3 * S.N, S.LU, S.piv, z, out, S.s);
+  return ves_launch_check("psolve");
+}
+
+struct GmresBufs {
+  double *V, *w, *r, *b, *x, *t, *partials, *dsc, *hsc;  // hsc: pinned host scalars
+  double* ydev;
+};
+
+int device_norm(StepState& S, GmresBufs& B, const double* a, double* dst) {
+  launch_dot_partials(S.n, a, a, B.partials, S.s);
+  ves_count_launch();
+  finalize_dot_kernel<<<1, 512, 0, S.s>>>(B.partials, dot_partial_blocks(), dst, 1);
+  return ves_launch_check("norm");
+}
+
+int read_scalars(StepState& S, GmresBufs& B, const double* src, int count) {
+  int rc = ves_cuda_status(cudaMemcpyAsync(B.hsc, src, count * sizeof(double), cudaMemcpyDeviceToHost, S.s), "read");
+  if (rc) return rc;
+  return ves_cuda_status(cudaStreamSynchronize(S.s), "read sync");
+}
+
+// scipy.sparse.linalg.gmres (scipy/sparse/linalg/_isolve/iterative.py), device vectors
+int gmres(StepState& S, GmresBufs& B, ves_step_result* res) {
+  const long long n = S.n;
+  const int restart = std::min<long long>(S.prm->gmres_restart > 0 ? S.prm->gmres_restart : 20, n);
+  const int maxiter = S.prm->gmres_maxiter > 0 ? S.prm->gmres_maxiter : (int)std::min<long long>(n * 10, 1 << 30);
+  const double eps = 2.220446049250313e-16;
+  const unsigned g = vec_grid(n);
+  // dsc layout: [0..restart+1] current h column, [restart+2] h0, [restart+3] scratch norm
+  double* hcol = B.dsc;
+  double* h0 = B.dsc + restart + 2;
+  double* nrm = B.dsc + restart + 3;
+  int rc;
+  if ((rc = device_norm(S, B, B.b, nrm))) return rc;
+  if ((rc = read_scalars(S, B, nrm, 1))) return rc;
+  const double bnrm2 = B.hsc[0];
+  const double atol = std::max(0.0, S.prm->gmres_tol * bnrm2);
+  res->matvecs = 0;
+  res->inner_iters = 0;
+  if (bnrm2 == 0.0) {
+    rc = ves_cuda_status(cudaMemcpyAsync(B.x, B.b, n * sizeof(double), cudaMemcpyDeviceToDevice, S.s), "x=b");
+    res->info = 0;
+    res->resid = 0;
+    return rc;
+  }
+  // Mb_nrm2 = ||psolve(b)||
+  if ((rc = psolve(S, B.b, B.t))) return rc;
+  if ((rc = device_norm(S, B, B.t, nrm))) return rc;
+  if ((rc = read_scalars(S, B, nrm, 1))) return rc;
+  const double Mb_nrm2 = B.hsc[0];
+  double ptol_max_factor = 1.0;
+  double ptol = Mb_nrm2 * std::min(ptol_max_factor, atol / bnrm2);
+  double presid = 0.0;
+  std::vector<double> h((size_t)restart * (restart + 1), 0.0), giv((size_t)restart * 2, 0.0), Sv(restart + 1, 0.0),
+      y(restart + 1, 0.0);
+  auto H = [&](int col, int k) -> double& { return h[(size_t)col * (restart + 1) + k]; };
+  int inner_iter = 0;
+  double rnorm = 0.0;
+  std::vector<double> rhist;  // true residual after each outer cycle
+  bool stagnated = false;
+  for (int iteration = 0; iteration < maxiter; ++iteration) {
+    if (iteration == 0) {
+      // r = b - A x (the initial guess [X; sigma] is nonzero in practice; an
+      // all-zero guess gives r = b either way)
+      if ((rc = matvec(S, B.x, B.t))) return rc;
+      ves_count_launch();
+      sub_kernel<<<g, 512, 0, S.s>>>(n, B.r, B.b, B.t);
+      if ((rc = device_norm(S, B, B.r, nrm))) return rc;
+      if ((rc = read_scalars(S, B, nrm, 1))) return rc;
+      if (B.hsc[0] < atol) {
+        rnorm = B.hsc[0];
+        break;
+      }
+    }
+    double* v0 = B.V;
+    if ((rc = psolve(S, B.r, v0))) return rc;
+    if ((rc = device_norm(S, B, v0, nrm))) return rc;
+    ves_count_launch();
+    scale_inv_kernel<<<g, 512, 0, S.s>>>(n, v0, v0, nrm, nullptr, eps);
+    if ((rc = read_scalars(S, B, nrm, 1))) return rc;
+    std::fill(Sv.begin(), Sv.end(), 0.0);
+    Sv[0] = B.hsc[0];
+    bool breakdown = false;
+    int col = 0;
+    for (col = 0; col < restart; ++col) {
+      double* vc = B.V + (long long)col * n;
+      double* vn = B.V + (long long)(col + 1) * n;
+      if ((rc = matvec(S, vc, B.t))) return rc;
+      if ((rc = psolve(S, B.t, B.w))) return rc;
+      if ((rc = device_norm(S, B, B.w, h0))) return rc;
+      for (int k = 0; k <= col; ++k) {
+        launch_dot_partials(n, B.V + (long long)k * n, B.w, B.partials, S.s);
+        ves_count_launch();
+        mgs_axpy_kernel<<<g, 512, 0, S.s>>>(n, B.partials, dot_partial_blocks(), B.w, B.V + (long long)k * n, hcol + k);
+      }
+      if ((rc = device_norm(S, B, B.w, hcol + col + 1))) return rc;
+      ves_count_launch();
+      scale_inv_kernel<<<g, 512, 0, S.s>>>(n, vn, B.w, hcol + col + 1, h0, eps);
+      if ((rc = ves_launch_check("mgs"))) return rc;
+      if ((rc = read_scalars(S, B, B.dsc, restart + 3))) return rc;
+      for (int k = 0; k <= col + 1; ++k) H(col, k) = B.hsc[k];
+      const double h0v = B.hsc[restart + 2];
+      const double h1 = H(col, col + 1);
+      if (h1 <= eps * h0v) {
+        H(col, col + 1) = 0.0;
+        breakdown = true;
+      }
+      for (int k = 0; k < col; ++k) {
+        const double cg = giv[2 * k], sg = giv[2 * k + 1];
+        const double n0 = H(col, k), n1 = H(col, k + 1);
+        H(col, k) = cg * n0 + sg * n1;
+        H(col, k + 1) = -sg * n0 + cg * n1;
+      }
+      double cg, sg, mag;
+      lartg(H(col, col), H(col, col + 1), cg, sg, mag);
+      giv[2 * col] = cg;
+      giv[2 * col + 1] = sg;
+      H(col, col) = mag;
+      H(col, col + 1) = 0.0;
+      const double tmp = -sg * Sv[col];
+      Sv[col] = cg * Sv[col];
+      Sv[col + 1] = tmp;
+      presid = fabs(tmp);
+      inner_iter++;
+      if (presid <= ptol || breakdown) break;
+    }
+    if (col == restart) col = restart - 1;
+    if (H(col, col) == 0.0) Sv[col] = 0.0;
+    for (int k = 0; k <= col; ++k) y[k] = Sv[k];
+    for (int k = col; k > 0; --k) {
+      if (y[k] != 0.0) {
+        y[k] /= H(k, k);
+        const double tmp = y[k];
+        for (int j = 0; j < k; ++j) y[j] -= tmp * H(k, j);
+      }
+    }
+    if (y[0] != 0.0) y[0] /= H(0, 0);
+    if ((rc = ves_cuda_status(cudaMemcpyAsync(B.ydev, y.data(), (col + 1) * sizeof(double), cudaMemcpyHostToDevice,
+                                              S.s),
+                              "y upload")))
+      return rc;
+    ves_count_launch();
+    update_x_kernel<<<g, 512, 0, S.s>>>(n, col + 1, B.ydev, B.V, B.x);
+    if ((rc = matvec(S, B.x, B.t))) return rc;
+    ves_count_launch();
+    sub_kernel<<<g, 512, 0, S.s>>>(n, B.r, B.b, B.t);
+    if ((rc = device_norm(S, B, B.r, nrm))) return rc;
+    if ((rc = read_scalars(S, B, nrm, 1))) return rc;
+    rnorm = B.hsc[0];
+    if (rnorm <= atol) break;
+    if (breakdown) break;
+    // Stagnation at the arithmetic's noise floor (e.g. an FP32 all-pairs sum
+    // against a 1e-10 tolerance): stop once three outer cycles have not
+    // halved the true residual, instead of running to maxiter.
+    rhist.push_back(rnorm);
+    if (rhist.size() >= 4 && rnorm > 0.5 * rhist[rhist.size() - 4]) {
+      stagnated = true;
+      break;
+    }
+    if (presid <= ptol)
+      ptol_max_factor = std::max(eps, 0.25 * ptol_max_factor);
+    else
+      ptol_max_factor = std::min(1.0, 1.5 * ptol_max_factor);
+    ptol = presid * std::min(ptol_max_factor, atol / rnorm);
+  }
+  res->inner_iters = inner_iter;
+  res->info = (rnorm <= atol) ? 0 : (stagnated ? -1 : maxiter);
+  res->resid = rnorm / bnrm2;
+  return VES_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+static int biem_step_impl(ves_ctx* c, const ves_step_params* prm, int nv, const double* X, const double* sigma,
+                          double* Xout, double* sigma_out, ves_step_result* res, WsCarver& ws, cudaStream_t s) {
+  const int N = c->N, Nup = c->Nup;
+  const long long n = 3LL * N * nv;
+  const int restart = (int)std::min<long long>(prm->gmres_restart > 0 ? prm->gmres_restart : 20, n > 0 ? n : 1);
+  const int maxc = prm->maxc > 0 ? prm->maxc : 64;
+  const int maxe = prm->max_entries > 0 ? prm->max_entries : std::max(1024, nv * N);
+  StepState S;
+  memset(&S, 0, sizeof(S));
+  S.c = c;
+  S.prm = prm;
+  S.nv = nv;
+  S.N = N;
+  S.Nup = Nup;
+  S.n = n;
+  S.s = s;
+  S.X = X;
+  S.sa = ws.take<double>((size_t)nv * N);
+  S.isa = ws.take<double>((size_t)nv * N);
+  S.tang = ws.take<double>((size_t)nv * 2 * N);
+  S.Xup = ws.take<double>((size_t)nv * 2 * Nup);
+  S.sa_up = ws.take<double>((size_t)nv * Nup);
+  S.G = ws.take<double>((size_t)nv * 4 * N * N);
+  S.LU = ws.take<double>((size_t)nv * 9 * N * N);
+  S.piv = ws.take<int>((size_t)nv * 3 * N);
+  S.f = ws.take<double>((size_t)nv * 2 * N);
+  S.Gf = ws.take<double>((size_t)nv * 2 * N);
+  S.LP = ws.take<double>((size_t)nv * 2 * N);
+  S.nl.maxc = maxc;
+  S.nl.cand_count = ws.take<int>(nv);
+  S.nl.cand_src = ws.take<int>((size_t)nv * maxc);
+  S.nl.excl_mask = ws.take<uint32_t>((size_t)nv * maxc * c->nwords_N);
+  S.nl.hh_mask = ws.take<uint32_t>((size_t)nv * maxc * c->nwords_up);
+  S.nl.max_entries = maxe;
+  S.nl.n_entries = ws.take<int>(1);
+  S.nl.ent_tsj = ws.take<int>((size_t)maxe * 3);
+  S.nl.ent_icp = ws.take<int>((size_t)maxe);
+  S.nl.ent_geo = ws.take<double>((size_t)maxe * 4);
+  GmresBufs B;
+  B.V = ws.take<double>((size_t)(restart + 1) * n);
+  B.w = ws.take<double>(n);
+  B.r = ws.take<double>(n);
+  B.b = ws.take<double>(n);
+  B.x = ws.take<double>(n);
+  B.t = ws.take<double>(n);
+  B.partials = ws.take<double>(dot_partial_blocks());
+  B.dsc = ws.take<double>(restart + 8);
+  B.ydev = ws.take<double>(restart + 2);
+  double* vinf = ws.take<double>((size_t)nv * 2 * N);
+  double* rhs2 = ws.take<double>((size_t)nv * N);
+  // one scratch region shared by the sub-stages
+  size_t scratch = 0;
+  {
+    WsCarver w(nullptr, 0);
+    alpert_sl_matrix(c, nv, nullptr, prm->sl_precision, nullptr, w, s);
+    scratch = std::max(scratch, w.off);
+  }
+  {
+    WsCarver w(nullptr, 0);
+    derivs_and_precond(c, nv, nullptr, nullptr, nullptr, 0, 0, nullptr, nullptr, nullptr, (double*)1, w, s);
+    w.take<double>((size_t)nv * 4 * N * N);  // Ben
+    w.take<double>((size_t)nv * 2 * N * N);  // Ten
+    w.take<double>((size_t)nv * 2 * N * N);  // Div
+    scratch = std::max(scratch, w.off);
+  }
+  {
+    WsCarver w(nullptr, 0);
+    if (prm->near_scheme == VES_NEAR_MATLAB)
+      near_zone_matlab(c, nv, nullptr, 0, nullptr, w, s);
+    else
+      near_zone_py(c, nv, nullptr, (const double*)1, 0, nullptr, w, s);
+    scratch = std::max(scratch, w.off);
+  }
+  {
+    WsCarver w(nullptr, 0);
+    near_sing_int_run(c, prm->near_scheme, prm->farfield_precision, nv, nullptr, nullptr, nullptr, nullptr, nullptr,
+                      nullptr, 0, nullptr, nullptr, w, s);
+    scratch = std::max(scratch, w.off);
+  }
+  S.scratch = ws.take<char>(scratch + 1024);
+  S.scratch_bytes = scratch + 1024;
+  if (ws.sizing) return VES_OK;
+  if (!ws.ok()) {
+    ves_record_error(VES_ERR_WORKSPACE, "biem_step: workspace too small (%zu needed)", ws.off);
+    return VES_ERR_WORKSPACE;
+  }
+  if (!prm || !X || !sigma || !Xout || !sigma_out || nv <= 0) {
+    ves_record_error(VES_ERR_ARG, "biem_step: bad arguments");
+    return VES_ERR_ARG;
+  }
+  if (prm->near_scheme != VES_NEAR_NONE && prm->near_scheme != VES_NEAR_PY_HH && prm->near_scheme != VES_NEAR_MATLAB) {
+    ves_record_error(VES_ERR_ARG, "biem_step: bad near scheme");
+    return VES_ERR_ARG;
+  }
+  int rc = ves_reset_status(c, s);
+  if (rc) return rc;
+  if (restart + 8 > 256) {
+    ves_record_error(VES_ERR_ARG, "biem_step: restart %d too large", restart);
+    return VES_ERR_ARG;
+  }
+  B.hsc = c->h_scal;
+  // geometry (capsules(X), poten.stokesSLmatrix, near zone)
+  launch_diff_prop(c, 0, nv, X, S.sa, S.isa, S.tang, nullptr, s);
+  launch_upsample_deriv(c, nv, X, S.Xup, nullptr, S.sa_up, s);
+  {
+    WsCarver sub(S.scratch, S.scratch_bytes);
+    if ((rc = alpert_sl_matrix(c, nv, X, prm->sl_precision, S.G, sub, s))) goto done;
+  }
+  S.h = 0.0;
+  if (prm->near_scheme == VES_NEAR_MATLAB) {
+    WsCarver sub(S.scratch, S.scratch_bytes);
+    if ((rc = near_zone_matlab(c, nv, X, 0.0, &S.nl, sub, s))) goto done;
+    // h = min length / N (capsules.py:46-47)
+    double* len = (double*)S.scratch;
+    launch_geom_prop(c, nv, X, nullptr, nullptr, len, s);
+    std::vector<double> hl(nv);
+    if ((rc = ves_cuda_status(cudaMemcpyAsync(hl.data(), len, nv * sizeof(double), cudaMemcpyDeviceToHost, s), "len")))
+      goto done;
+    if ((rc = ves_cuda_status(cudaStreamSynchronize(s), "len sync"))) goto done;
+    S.h = *std::min_element(hl.begin(), hl.end()) / N;
+  } else if (prm->near_scheme == VES_NEAR_PY_HH) {
+    WsCarver sub(S.scratch, S.scratch_bytes);
+    if ((rc = near_zone_py(c, nv, X, S.Xup, 0.0, &S.nl, sub, s))) goto done;
+  }
+  // right-hand side [X + dt*vinf; surfaceDiv(X)]
+  launch_bg_flow(nv, N, prm->flow, prm->speed, prm->chan_width, prm->vortex_size, X, vinf, s);
+  ves_count_launch();
+  rhs_pos_kernel<<<ceil_div((long long)nv * 2 * N, 256), 256, 0, s>>>((long long)nv * 2 * N, prm->dt, X, vinf, vinf);
+  launch_surface_div(c, nv, S.isa, S.tang, X, 2LL * N, rhs2, N, s);
+  ves_count_launch();
+  pack_kernel<<<ceil_div(n, 256), 256, 0, s>>>(nv, N, vinf, rhs2, B.b);
+  ves_count_launch();
+  pack_kernel<<<ceil_div(n, 256), 256, 0, s>>>(nv, N, X, sigma, B.x);
+  // preconditioner
+  if (prm->use_preco) {
+    WsCarver sub(S.scratch, S.scratch_bytes);
+    double* Ben = nullptr;
+    double* Ten = sub.take<double>((size_t)nv * 2 * N * N);
+    double* Div = sub.take<double>((size_t)nv * 2 * N * N);
+    if ((rc = derivs_and_precond(c, nv, S.isa, S.tang, S.G, prm->dt, prm->kappa, Ben, Ten, Div, S.LU, sub, s)))
+      goto done;
+    if ((rc = launch_lu_factor(c, nv, 3 * N, S.LU, S.piv, s))) goto done;
+  }
+  if ((rc = ves_check_status(c, s, "biem_step setup"))) goto done;
+  S.matvecs = 0;
+  rc = gmres(S, B, res);
+  if (rc) goto done;
+  res->matvecs = S.matvecs;
+  ves_count_launch();
+  unpack_kernel<<<ceil_div(n, 256), 256, 0, s>>>(nv, N, B.x, Xout, sigma_out);
+  {
+    int nn = 0;
+    if (prm->near_scheme == VES_NEAR_MATLAB)
+      cudaMemcpyAsync(&nn, S.nl.n_entries, sizeof(int), cudaMemcpyDeviceToHost, s);
+    res->n_near_entries = nn;
+  }
+  rc = ves_check_status(c, s, "biem_step");
+  if (!rc && res->info != 0) {
+    ves_record_error(VES_ERR_GMRES_MAXIT, "biem_step: GMRES reached maxiter (resid %.3e)", res->resid);
+    rc = VES_ERR_GMRES_MAXIT;
+  }
+done:
+  return rc;
+}
+
+extern "C" size_t ves_biem_step_workspace(ves_ctx* c, const ves_step_params* prm, int nv) {
+  if (!c || !prm) return 0;
+  WsCarver w(nullptr, 0);
+  ves_step_result r;
+  biem_step_impl(c, prm, nv, nullptr, nullptr, nullptr, nullptr, &r, w, 0);
+  return w.off + 256;
+}
+
+extern "C" int ves_biem_step(ves_ctx* c, const ves_step_params* prm, int nv, const double* X, const double* sigma,
+                             double* Xout, double* sigma_out, ves_step_result* res, void* ws, size_t ws_bytes,
+                             void* stream) {
+  if (!c || !prm || !res || !ws) return VES_ERR_ARG;
+  memset(res, 0, sizeof(*res));
+  WsCarver w(ws, ws_bytes);
+  return biem_step_impl(c, prm, nv, X, sigma, Xout, sigma_out, res, w, (cudaStream_t)stream);
+}

@@ -1,0 +1,134 @@
+"""Implicit BIEM time stepper on one GPU (reference: mytorch/tstep_biem.py).
+
+``TStepBiem(X, Xwalls, options, prams)`` and ``time_step(X, sigma, eta, RS)``
+keep the reference signatures and return values; the whole step (geometry,
+Alpert matrix, near lists, block preconditioner, GMRES with its matvecs) runs
+in one call to ``ves_biem_step`` of the C library.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _native as nat
+from .layout import as_device_f64, from_vm, to_vm
+
+
+class TStepBiem:
+    """tstep_biem.py:25-153.
+
+    Extra keyword options select the device arithmetic:
+    ``near`` ("py_hh" = the reference's nearSingInt_hh, "matlab" = the MATLAB
+    near-singular scheme, "none"), ``farfield_precision`` and ``sl_precision``
+    ("fp64" or "fp32c").
+    """
+
+    def __init__(self, X, Xwalls, options, prams, near: str = "py_hh", farfield_precision: str = "fp32c",
+                 sl_precision: str = "fp32c", device=None):
+        if Xwalls is not None:
+            raise NotImplementedError("confined flows (walls) are not supported by the device stepper")
+        if options.get("repulsion", False):
+            raise NotImplementedError("repulsion is not supported by the device stepper")
+        visc = torch.as_tensor(prams.get("viscCont", 1.0), dtype=torch.float64)
+        if torch.any(visc != 1):
+            raise NotImplementedError("viscosity contrast != 1 is not supported by the device stepper")
+        X = as_device_f64(X, device)
+        self.device = X.device
+        self.N = X.shape[0] // 2
+        self.nv = X.shape[1]
+        self.Xwalls = None
+        self.dt = float(prams["dt"])
+        self.kappa = float(prams["kappa"])
+        self.viscCont = prams.get("viscCont")
+        self.gmresTol = float(prams["gmresTol"])
+        self.gmresMaxIter = int(prams["gmresMaxIter"])
+        self.farFieldSpeed = float(prams.get("farFieldSpeed", 1.0))
+        self.chanWidth = float(prams.get("chanWidth", 1.0))
+        self.vortexSize = float(prams.get("vortexSize", 1.0))
+        self.options = dict(options)
+        self.usePreco = bool(options.get("usePreco", True))
+        self.confined = False
+        self.near = near
+        self.farfield_precision = farfield_precision
+        self.sl_precision = sl_precision
+        from .poten import Poten
+        from .curve import Curve
+        self.op = Poten(self.N, self.device)
+        _, self.area, self.length = Curve().geomProp(X)
+        self._ctx = nat.context(self.N, self.device)
+        self.last = None
+
+    def params(self) -> nat.StepParams:
+        p = nat.StepParams()
+        p.dt = self.dt
+        p.kappa = self.kappa
+        p.gmres_tol = self.gmresTol
+        p.gmres_maxiter = self.gmresMaxIter
+        p.gmres_restart = 20
+        p.use_preco = 1 if self.usePreco else 0
+        flow = self.options.get("farField", "shear")
+        if flow not in nat.FLOW:
+            raise ValueError("Unknown or missing flow type in bg_flow.")
+        p.flow = nat.FLOW[flow]
+        p.speed = self.farFieldSpeed
+        p.chan_width = self.chanWidth
+        p.vortex_size = self.vortexSize
+        p.near_scheme = nat.NEAR[self.near]
+        p.farfield_precision = nat.PREC[self.farfield_precision]
+        p.sl_precision = nat.PREC[self.sl_precision]
+        p.maxc = 64
+        p.max_entries = 0
+        return p
+
+    def workspace_bytes(self) -> int:
+        p = self.params()
+        return int(self._ctx.lib.ves_biem_step_workspace(self._ctx.handle, ctypes.byref(p), self.nv))
+
+    def step_device(self, Xv, sigv, Xout=None, sigout=None, ws=None):
+        """One step on device-layout tensors Xv[nv][2N], sigv[nv][N] (float64,
+        contiguous); returns (Xout, sigout, result)."""
+        p = self.params()
+        ctx = self._ctx
+        nbytes = ctx.lib.ves_biem_step_workspace(ctx.handle, ctypes.byref(p), self.nv)
+        if ws is None:
+            ws = ctx.workspace(nbytes)
+        Xout = torch.empty_like(Xv) if Xout is None else Xout
+        sigout = torch.empty_like(sigv) if sigout is None else sigout
+        res = nat.StepResult()
+        rc = ctx.lib.ves_biem_step(ctx.handle, ctypes.byref(p), self.nv, Xv.data_ptr(), sigv.data_ptr(),
+                                   Xout.data_ptr(), sigout.data_ptr(), ctypes.byref(res), ws.data_ptr(), ws.numel(),
+                                   nat.stream_ptr(self.device))
+        if rc not in (nat.VES_OK, nat.VES_ERR_GMRES_MAXIT):
+            nat.check(rc, "time_step")
+        self.last = res
+        return Xout, sigout, res
+
+    def time_step(self, Xstore, sigStore, etaStore=None, RSstore=None):
+        """tstep_biem.py:181-428 -> (X, sigma, eta, RS, iter, iflag).
+
+        ``iter`` follows the reference's count of time_matvec calls, which
+        includes the one call scipy's LinearOperator makes on a zero vector to
+        infer its dtype (tstep_biem.py:366); the device solver makes no such
+        call, so ``iter = matvecs + 1``.  ``self.last.matvecs`` holds the
+        number of operator applications actually performed."""
+        X = as_device_f64(Xstore, self.device)
+        sig = as_device_f64(sigStore, self.device)
+        Xv, sv = to_vm(X), to_vm(sig)
+        Xo, so, res = self.step_device(Xv, sv)
+        return from_vm(Xo), from_vm(so), None, None, res.matvecs + 1, res.info != 0
+
+    def bg_flow(self, X, Xwalls=None, *args, **kwargs):
+        """tstep_biem.py:849-952 for the unconfined flows."""
+        X = as_device_f64(X, self.device)
+        kind = next((a for a in args if a in nat.FLOW), self.options.get("farField", "shear"))
+        if kind not in nat.FLOW:
+            raise ValueError("Unknown or missing flow type in bg_flow.")
+        speed = float(kwargs.get("Speed", 1.0))
+        Xv = to_vm(X)
+        out = torch.empty_like(Xv)
+        ctx = self._ctx
+        nat.check(ctx.lib.ves_bg_flow(ctx.handle, self.nv if X.shape[1] == self.nv else X.shape[1], nat.FLOW[kind],
+                                      speed, float(kwargs.get("chanWidth", 1.0)), float(kwargs.get("vortexSize", 1.0)),
+                                      Xv.data_ptr(), out.data_ptr(), nat.stream_ptr(self.device)), "bg_flow")
+        return from_vm(out)

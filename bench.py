@@ -167,9 +167,7 @@ def run_gb300(a, rank, world):
     sv = torch.zeros(nv, N, dtype=torch.float64, device=dev)
     Xo, so = torch.empty_like(Xv), torch.empty_like(sv)
 
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
+    from ves2dpy_gb300.replicas import barrier
 
     mv = []
     for _ in range(a.warmup):
@@ -196,13 +194,9 @@ def run_gb300(a, rank, world):
     st = ctx.stats(reset=True)
     ctx.set_timing(False)
     launches = st.kernel_launches - l0
-    t_max = ms
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(t.item())
+    from ves2dpy_gb300.replicas import aggregate
+    t_max, value = aggregate(ms, float(nv * a.steps), dev)
     ms_per_step = t_max / a.steps
-    value = world * nv * a.steps / (t_max * 1e-3)
 
     # end to end through the public API with pinned host buffers
     Xh = torch.from_numpy(X0).pin_memory()
@@ -257,6 +251,8 @@ def run_gb300(a, rank, world):
             "roofline": {"bound": "sfu", "kernel": "ff_main_kernel<float> (all-pairs Stokeslet sum)",
                          "achieved": mufu_rate / 1e9, "peak": sfu_peak / 1e9, "unit": "Gop/s (MUFU lg2+rcp)",
                          "frac": mufu_rate / sfu_peak if sfu_peak else None, "traffic": None,
+                         "traffic_note": "compute-bound; ncu measured 6.7 MB DRAM per launch at nv=256 "
+                                         "(sources L2-resident), see profiles/ff_main_kernel_nv256_N128_full.md",
                          "pairs_per_launch": ff_pairs, "ms_per_launch": ff_ms,
                          "gpairs_per_s": ff_pairs / (ff_ms * 1e-3) / 1e9 if ff_ms > 0 else None,
                          "peak_source": "measured by ves_probe_sfu_peak on this GPU",

@@ -222,6 +222,24 @@ VES_API int ves_biem_step(ves_ctx* ctx, const ves_step_params* prm, int nv, cons
                   void* ws, size_t ws_bytes, void* stream);
 VES_API size_t ves_biem_step_workspace(ves_ctx* ctx, const ves_step_params* prm, int nv);
 
+/* ---- all-pairs sum without allocation (no counterpart in the reference) ---- */
+/* The sum of ves_farfield (no near-pair lists) for callers that cannot allocate
+ * device memory when they call: applications whose GPU memory is entirely
+ * reserved by their own pool allocator, and hosts that call in from a runtime
+ * or callback where a cudaMalloc would synchronise the device or is not
+ * permitted.  The call takes its scratch from one fixed device array of
+ * VES_STATIC_SCRATCH_BYTES bytes that belongs to the library image (held on
+ * every GPU that loads the library until the process exits), so it performs
+ * no allocation and needs no ves_ctx.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture.  Sizes whose scratch exceeds the array return
+ * VES_ERR_WORKSPACE.  All calls share the one array: calls that overlap on the
+ * GPU race and must be serialised by the caller.  Synchronises ``stream``. */
+#define VES_STATIC_SCRATCH_BYTES (64u << 20)
+VES_API int ves_farfield_static_scratch(int precision, int nsrc, int ns, const double* Xsrc, const double* den,
+                                        int nt, int ntp, const double* Xtar, const int* self_idx, double* out,
+                                        void* stream);
+
 /* ---- measurement utilities (no counterpart in the reference) -------------- */
 typedef struct ves_stats {
   long long kernel_launches;  /* kernels launched through this library (all contexts) */

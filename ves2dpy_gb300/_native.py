@@ -138,6 +138,7 @@ SIGNATURES = {
     "ves_biem_step": (_I, [_P, ctypes.POINTER(StepParams), _I, _P, _P, _P, _P, ctypes.POINTER(StepResult), _P,
                            _SZ, _P]),
     "ves_biem_step_workspace": (_SZ, [_P, ctypes.POINTER(StepParams), _I]),
+    "ves_farfield_static_scratch": (_I, [_I, _I, _I, _P, _P, _I, _I, _P, _P, _P, _P]),
     "ves_ctx_set_timing": (_I, [_P, _I]),
     "ves_ctx_stats": (_I, [_P, ctypes.POINTER(Stats), _I]),
     "ves_probe_sfu_peak": (_I, [ctypes.POINTER(ctypes.c_double), _P]),

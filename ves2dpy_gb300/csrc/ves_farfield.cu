@@ -365,7 +365,7 @@ FFPlan ff_plan(int nsrc, int ns, long long total_pts) {
 }
 
 template <typename Real>
-int ff_run(ves_ctx* c, int nsrc, int ns, const double* Xsrc, const double* den, int nt, int ntp,
+int ff_run(const FFEnv& env, int nsrc, int ns, const double* Xsrc, const double* den, int nt, int ntp,
            const double* Xtar, const int* self_idx, const ves_near_lists* nl, double* out, WsCarver& ws,
            cudaStream_t s) {
   typedef typename FFT<Real>::Rec Rec;
@@ -387,7 +387,7 @@ int ff_run(ves_ctx* c, int nsrc, int ns, const double* Xsrc, const double* den, 
   }
   if (total_pts == 0) return VES_OK;
   if (nsrc == 0) return ves_cuda_status(cudaMemsetAsync(out, 0, (size_t)total_pts * 2 * sizeof(double), s), "ff zero");
-  if (nl && ntp != c->N) {
+  if (nl && ntp != env.N) {
     ves_record_error(VES_ERR_SHAPE, "farfield: near lists need N target points per column");
     return VES_ERR_SHAPE;
   }
@@ -413,12 +413,12 @@ int ff_run(ves_ctx* c, int nsrc, int ns, const double* Xsrc, const double* den, 
   a.cand_src = nl ? nl->cand_src : nullptr;
   a.excl_mask = nl ? nl->excl_mask : nullptr;
   a.maxc = nl ? nl->maxc : 0;
-  a.nwords = c->nwords_N;
+  a.nwords = (env.N + 31) / 32;
   a.sv_per_stage = pl.sv_per_stage;
   a.src_per_split = pl.src_per_split;
   a.nsplit = pl.nsplit;
   a.partial = partial;
-  a.st = c->status;
+  a.st = env.status;
   if (pl.smem > 32 * 1024) {  // dynamic + static shared memory must fit the opt-in limit
     cudaError_t e = cudaFuncSetAttribute(ff_main_kernel<Real>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)pl.smem);
@@ -426,9 +426,9 @@ int ff_run(ves_ctx* c, int nsrc, int ns, const double* Xsrc, const double* den, 
   }
   dim3 grid(pl.tgt_blocks, pl.nsplit);
   ves_count_launch();
-  ves_ff_timing_begin(c, s);
+  if (env.timing) ves_ff_timing_begin(env.timing, s);
   ff_main_kernel<Real><<<grid, FF_WARPS * 32, pl.smem, s>>>(a);
-  ves_ff_timing_end(c, s, (double)total_pts * ns * (double)nsrc);
+  if (env.timing) ves_ff_timing_end(env.timing, s, (double)total_pts * ns * (double)nsrc);
   ves_count_launch();
   ff_reduce_kernel<<<ceil_div(total_pts, 256), 256, 0, s>>>(total_pts, ntp, pl.nsplit, partial, out);
   return ves_launch_check("farfield");
@@ -436,13 +436,26 @@ int ff_run(ves_ctx* c, int nsrc, int ns, const double* Xsrc, const double* den, 
 
 }  // namespace
 
+int farfield_run_env(const FFEnv& env, int precision, int nsrc, int ns, const double* Xsrc, const double* den,
+                     int nt, int ntp, const double* Xtar, const int* self_idx, const ves_near_lists* nl,
+                     double* out, WsCarver& ws, cudaStream_t s) {
+  if (precision == VES_PREC_FP64)
+    return ff_run<double>(env, nsrc, ns, Xsrc, den, nt, ntp, Xtar, self_idx, nl, out, ws, s);
+  if (precision == VES_PREC_FP32C)
+    return ff_run<float>(env, nsrc, ns, Xsrc, den, nt, ntp, Xtar, self_idx, nl, out, ws, s);
+  ves_record_error(VES_ERR_ARG, "farfield: bad precision %d", precision);
+  return VES_ERR_ARG;
+}
+
 int farfield_run(ves_ctx* c, int precision, int nsrc, int ns, const double* Xsrc, const double* den, int nt,
                  int ntp, const double* Xtar, const int* self_idx, const ves_near_lists* nl, double* out,
                  WsCarver& ws, cudaStream_t s) {
-  if (precision == VES_PREC_FP64)
-    return ff_run<double>(c, nsrc, ns, Xsrc, den, nt, ntp, Xtar, self_idx, nl, out, ws, s);
-  if (precision == VES_PREC_FP32C)
-    return ff_run<float>(c, nsrc, ns, Xsrc, den, nt, ntp, Xtar, self_idx, nl, out, ws, s);
+  FFEnv env;
+  env.status = c ? c->status : nullptr;
+  env.N = c ? c->N : ntp;
+  env.timing = c;
+  if (precision == VES_PREC_FP64 || precision == VES_PREC_FP32C)
+    return farfield_run_env(env, precision, nsrc, ns, Xsrc, den, nt, ntp, Xtar, self_idx, nl, out, ws, s);
   ves_record_error(VES_ERR_ARG, "farfield: bad precision %d", precision);
   return VES_ERR_ARG;
 }

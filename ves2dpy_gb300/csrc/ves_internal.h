@@ -109,6 +109,17 @@ int alpert_sl_matrix(ves_ctx* c, int nv, const double* X, int precision, double*
                      cudaStream_t s);
 
 // far field
+// Execution environment of the all-pairs driver: the device status word, the
+// number of target points per column the near-list masks are laid out for,
+// and the context whose timing hooks record the launch (may be null).
+struct FFEnv {
+  VesDeviceStatus* status;
+  int N;
+  ves_ctx* timing;
+};
+int farfield_run_env(const FFEnv& env, int precision, int nsrc, int ns, const double* Xsrc, const double* den,
+                     int nt, int ntp, const double* Xtar, const int* self_idx, const ves_near_lists* nl,
+                     double* out, WsCarver& ws, cudaStream_t s);
 int farfield_run(ves_ctx* c, int precision, int nsrc, int ns, const double* Xsrc, const double* den,
                  int nt, int ntp, const double* Xtar, const int* self_idx, const ves_near_lists* nl,
                  double* out, WsCarver& ws, cudaStream_t s);

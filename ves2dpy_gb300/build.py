@@ -44,6 +44,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     headers = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
     headers.append(os.path.join(ROOT, "include", "ves2d_gb300.h"))
     cc = nvcc()
+    extra = os.environ.get("VES2D_NVCC_EXTRA", "").split()
     jobs = []
     objs = []
     for src in SOURCES:
@@ -51,7 +52,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         obj = os.path.join(BUILD, src.replace(".cu", ".o"))
         objs.append(obj)
         if force or _needs(obj, [sp] + headers):
-            cmd = [cc, *ARCH, *FLAGS, "-I", os.path.join(ROOT, "include"), "-c", sp, "-o", obj]
+            cmd = [cc, *ARCH, *FLAGS, *extra, "-I", os.path.join(ROOT, "include"), "-c", sp, "-o", obj]
             jobs.append(cmd)
 
     def run(cmd):

@@ -29,6 +29,12 @@
 
 namespace {
 
+#ifndef VES_FF_PAIRED_RCP
+#define VES_FF_PAIRED_RCP 0
+#endif
+#ifndef VES_FF_MINB
+#define VES_FF_MINB 2  // resident CTAs per SM requested from the register allocator
+#endif
 constexpr int FF_WARPS = 8;
 constexpr int FF_TPL = 4;  // target slots per lane
 constexpr int FF_PTS_PER_WARP = 32 * FF_TPL;
@@ -181,7 +187,7 @@ __global__ void __launch_bounds__(256) ff_prep_kernel(int n, const double* __res
 
 // --------------------------------------------------------------------------
 template <typename Real>
-__global__ void __launch_bounds__(FF_WARPS * 32) ff_main_kernel(FFArgs<Real> p) {
+__global__ void __launch_bounds__(FF_WARPS * 32, VES_FF_MINB) ff_main_kernel(FFArgs<Real> p) {
   typedef typename FFT<Real>::Rec Rec;
   typedef typename FFT<Real>::Pair Pair;
   extern __shared__ __align__(128) unsigned char ff_smem[];
@@ -256,20 +262,52 @@ __global__ void __launch_bounds__(FF_WARPS * 32) ff_main_kernel(FFArgs<Real> p) 
         acx[q] = acy[q] = alx[q] = aly[q] = Real(0);
       }
       const Rec* Sv = S + v * p.ns;
+      if (sizeof(Real) == 4 && VES_FF_PAIRED_RCP) {
+        // One MUFU reciprocal per two target slots: 1/a = b * rcp(a*b).  The
+        // 1e-20 inside the FMA keeps a*b normal when a slot coincides with a
+        // source (its own vesicle, whose result is discarded) and is below one
+        // ulp of every separated pair's |r|^2.
 #pragma unroll 2
-      for (int j = 0; j < p.ns; ++j) {
-        const Rec r = Sv[j];
+        for (int j = 0; j < p.ns; ++j) {
+          const Rec r = Sv[j];
 #pragma unroll
-        for (int q = 0; q < FF_TPL; ++q) {
-          const Real dx = tx[q] - r.x, dy = ty[q] - r.y;
-          const Real r2 = fma(dx, dx, dy * dy);
-          const Real inv = FFT<Real>::rcp(r2);
-          const Real lg = FFT<Real>::lg2(r2 * irc2[q]);
-          const Real cc = fma(dx, r.z, dy * r.w) * inv;
-          acx[q] = fma(cc, dx, acx[q]);
-          acy[q] = fma(cc, dy, acy[q]);
-          alx[q] = fma(lg, r.z, alx[q]);
-          aly[q] = fma(lg, r.w, aly[q]);
+          for (int q = 0; q < FF_TPL; q += 2) {
+            const Real dx0 = tx[q] - r.x, dy0 = ty[q] - r.y;
+            const Real dx1 = tx[q + 1] - r.x, dy1 = ty[q + 1] - r.y;
+            const Real r20 = fma(dx0, dx0, fma(dy0, dy0, Real(1e-20)));
+            const Real r21 = fma(dx1, dx1, fma(dy1, dy1, Real(1e-20)));
+            const Real ip = FFT<Real>::rcp(r20 * r21);
+            const Real inv0 = r21 * ip, inv1 = r20 * ip;
+            const Real lg0 = FFT<Real>::lg2(r20 * irc2[q]);
+            const Real lg1 = FFT<Real>::lg2(r21 * irc2[q + 1]);
+            const Real cc0 = fma(dx0, r.z, dy0 * r.w) * inv0;
+            const Real cc1 = fma(dx1, r.z, dy1 * r.w) * inv1;
+            acx[q] = fma(cc0, dx0, acx[q]);
+            acy[q] = fma(cc0, dy0, acy[q]);
+            alx[q] = fma(lg0, r.z, alx[q]);
+            aly[q] = fma(lg0, r.w, aly[q]);
+            acx[q + 1] = fma(cc1, dx1, acx[q + 1]);
+            acy[q + 1] = fma(cc1, dy1, acy[q + 1]);
+            alx[q + 1] = fma(lg1, r.z, alx[q + 1]);
+            aly[q + 1] = fma(lg1, r.w, aly[q + 1]);
+          }
+        }
+      } else {
+#pragma unroll 2
+        for (int j = 0; j < p.ns; ++j) {
+          const Rec r = Sv[j];
+#pragma unroll
+          for (int q = 0; q < FF_TPL; ++q) {
+            const Real dx = tx[q] - r.x, dy = ty[q] - r.y;
+            const Real r2 = fma(dx, dx, dy * dy);
+            const Real inv = FFT<Real>::rcp(r2);
+            const Real lg = FFT<Real>::lg2(r2 * irc2[q]);
+            const Real cc = fma(dx, r.z, dy * r.w) * inv;
+            acx[q] = fma(cc, dx, acx[q]);
+            acy[q] = fma(cc, dy, acy[q]);
+            alx[q] = fma(lg, r.z, alx[q]);
+            aly[q] = fma(lg, r.w, aly[q]);
+          }
         }
       }
 #pragma unroll

@@ -222,6 +222,31 @@ VES_API int ves_biem_step(ves_ctx* ctx, const ves_step_params* prm, int nv, cons
                   void* ws, size_t ws_bytes, void* stream);
 VES_API size_t ves_biem_step_workspace(ves_ctx* ctx, const ves_step_params* prm, int nv);
 
+/* ---- post-step shape conditioning (curve_batch_compile.py) ---------------- */
+/* One redistributeArcLength pass (curve_batch_compile.py:905-972, with
+ * my_arcLengthParameter :1039-1092 and the driver's Fourier modes
+ * driver_confined.py:240): Xout[nv][2][N] (may alias X); flags[nv] device
+ * ints (1 = already equispaced within 1e-5, left unchanged); *all_good (host,
+ * may be NULL: no synchronisation) = all flags set. */
+VES_API int ves_redistribute_arclength(ves_ctx* ctx, int nv, const double* X, double* Xout, int* flags,
+                                       int* all_good, void* stream);
+/* alignCenterAngle (curve_batch_compile.py:842-901): rigid motion of X onto
+ * the physical centre and inclination angle of Xorg. */
+VES_API int ves_align_center_angle(ves_ctx* ctx, int nv, const double* Xorg, const double* X, double* Xout,
+                                   void* stream);
+/* getPhysicalCenter (:84-100) -> center[nv][2]; getIncAngle (:105-194) -> angle[nv]
+ * (either may be NULL). */
+VES_API int ves_center_angle(ves_ctx* ctx, int nv, const double* X, double* center, double* angle,
+                             void* stream);
+/* correctAreaAndLengthAugLag (curve_batch_compile.py:590-710): vesicles whose
+ * area or length is off by more than 1e-2 are moved to the nearest shape
+ * with area0/length0 (augmented Lagrangian, Adam, 100 x 20 iterations at
+ * most).  *outer_iters (host, may be NULL) = augmented-Lagrangian updates. */
+VES_API int ves_correct_area_length(ves_ctx* ctx, int nv, const double* X, const double* area0,
+                                    const double* length0, double* Xout, int* outer_iters, void* ws,
+                                    size_t ws_bytes, void* stream);
+VES_API size_t ves_correct_area_length_workspace(ves_ctx* ctx, int nv);
+
 /* ---- all-pairs sum without allocation (no counterpart in the reference) ---- */
 /* The sum of ves_farfield (no near-pair lists) for callers that cannot allocate
  * device memory when they call: applications whose GPU memory is entirely

@@ -714,3 +714,169 @@ def ellipse_axes(reduced_area: float, area: float = np.pi):
     ratio = 0.5 * (lo + hi)
     b = math.sqrt(area / (np.pi * ratio))
     return ratio * b, b
+
+
+# --------------------------------------------------------------------------
+# Post-step conditioning (mytorch/curve_batch_compile.py:84-100, 105-194,
+# 590-710, 842-901, 905-972, 1039-1092)
+# --------------------------------------------------------------------------
+
+
+def physical_center(X):
+    """getPhysicalCenter (curve_batch_compile.py:84-100)."""
+    x, y = get_xy(X)
+    Dx, Dy = get_dxy(X)
+    A = np.sum(x * Dy - y * Dx, axis=0)
+    return np.vstack([np.sum(x ** 2 * Dy, axis=0) / A, -np.sum(y ** 2 * Dx, axis=0) / A])
+
+
+def inc_angle(X):
+    """getIncAngle (curve_batch_compile.py:105-194): angle in [0, pi] of the
+    principal axis of the smallest |eigenvalue| of the moment tensor."""
+    N, nv = X.shape[0] // 2, X.shape[1]
+    c = physical_center(X)
+    xc, yc = X[:N] - c[0], X[N:] - c[1]
+    Xc = np.vstack([xc, yc])
+    Dx, Dy = get_dxy(Xc)
+    jac = np.sqrt(Dx ** 2 + Dy ** 2)
+    nx, ny = Dy / jac, -Dx / jac
+    rdn = xc * nx + yc * ny
+    rho2 = xc ** 2 + yc ** 2
+    J11 = np.sum(rdn * (rho2 - xc ** 2) * jac, axis=0)
+    J12 = np.sum(rdn * (-xc * yc) * jac, axis=0)
+    J22 = np.sum(rdn * (rho2 - yc ** 2) * jac, axis=0)
+    out = np.zeros(nv)
+    for k in range(nv):
+        w, V = np.linalg.eig(np.array([[J11[k], J12[k]], [J12[k], J22[k]]]))
+        i = int(np.argmin(np.abs(w)))
+        v = np.real(V[:, i])
+        if v[1] < 0:
+            v = -v
+        out[k] = math.atan2(v[1], v[0])
+    return out
+
+
+def align_center_angle(Xorg, X):
+    """alignCenterAngle (curve_batch_compile.py:842-901)."""
+    N = X.shape[0] // 2
+    c0, c1 = physical_center(Xorg), physical_center(X)
+    a0, a1 = inc_angle(Xorg), inc_angle(X)
+    a2 = np.where(a1 > np.pi, a1 - np.pi, a1 + np.pi)
+    pick = np.abs(a0 - a2) < np.abs(a0 - a1)
+    a1 = np.where(pick, a2, a1)
+    th = -a1 + a0
+    xp, yp = X[:N] - c1[0], X[N:] - c1[1]
+    return np.vstack([xp * np.cos(th) - yp * np.sin(th) + c0[0], xp * np.sin(th) + yp * np.cos(th) + c0[1]])
+
+
+def arc_length_parameter(X):
+    """my_arcLengthParameter (curve_batch_compile.py:1039-1092): (N, nv) theta."""
+    N, nv = X.shape[0] // 2, X.shape[1]
+    Nup = 6 * N
+    t = np.arange(Nup) * 2 * np.pi / Nup
+    Xu = interpft_vec(X, Nup)
+    length = np.sum(np.sqrt(sum(d ** 2 for d in get_dxy(X))), axis=0) * 2 * np.pi / N
+    Dx, Dy = get_dxy(Xu)
+    arc = np.sqrt(Dx ** 2 + Dy ** 2)
+    arch = np.fft.fft(arc.T, axis=1)
+    k = np.concatenate([[np.inf], np.arange(1, Nup // 2), [np.inf], np.arange(-Nup // 2 + 1, 0)])
+    modes = -1j / k
+    al = np.real(np.fft.ifft(modes * arch, axis=1) - np.sum(modes * arch, axis=1, keepdims=True) / Nup
+                 + arch[:, 0:1] * t / Nup)
+    theta = np.zeros((nv, N))
+    target = np.arange(1, N)[None, :] * length[:, None] / N
+    for v in range(nv):
+        idx = np.searchsorted(al[v], target[v], side="left")
+        theta[v, 1:] = t[idx - 1] + (target[v] - al[v, idx - 1]) * (2 * np.pi)
+    return theta.T
+
+
+def redistribute_arc_length(X):
+    """redistributeArcLength (curve_batch_compile.py:905-972) with the
+    driver's modes [0..N/2-1, -N/2..-1] (driver_confined.py:240)."""
+    N = X.shape[0] // 2
+    X = X.copy()
+    jac = np.sqrt(sum(d ** 2 for d in get_dxy(X)))
+    mean = jac.mean(axis=0)
+    redo = np.abs(jac - mean).max(axis=0) > 1e-5 * mean
+    if not redo.any():
+        return X, True
+    ids = np.nonzero(redo)[0]
+    theta = arc_length_parameter(X[:, ids])
+    z = X[:N, ids] + 1j * X[N:, ids]
+    zh = np.fft.fft(z, axis=0) / N
+    m = np.concatenate([np.arange(0, N // 2), np.arange(-N // 2, 0)])
+    zz = np.einsum('mj,mnj->nj', zh, np.exp(1j * m[:, None, None] * theta))
+    X[:N, ids] = zz.real
+    X[N:, ids] = zz.imag
+    return X, False
+
+
+def correct_area_length(X, area0, length0, tol_c=1e-2, tol_f=1e-2, maxiter=100, inner=20, lr=3e-5):
+    """correctAreaAndLengthAugLag (curve_batch_compile.py:590-710): augmented
+    Lagrangian with torch-style Adam (fresh optimiser per outer iteration)."""
+    N = X.shape[0] // 2
+    _, a, l = geom_prop(X)
+    eA, eL = np.abs((a - area0) / area0), np.abs((l - length0) / length0)
+    if eA.max() < tol_c and eL.max() < tol_c:
+        return X.copy()
+    mask = (eA > tol_c) | (eL > tol_c)
+    X0 = X[:, mask].copy()
+    a0, l0 = area0[mask], length0[mask]
+    nv = X0.shape[1]
+    z = X0.copy()
+    lam = np.zeros(2 * nv)
+    mu = 0.1
+    d = np.array([deriv_stencil(N)])[0]
+    D = d[(np.arange(N)[:, None] - np.arange(N)[None, :]) % N]
+    nX = np.linalg.norm(X0, axis=0)
+
+    def forward(z):
+        _, a, l = geom_prop(z)
+        f = np.mean(np.linalg.norm(z - X0, axis=0) / nX)
+        return a, l, f
+
+    def grad(z, a, l):
+        x, y = z[:N], z[N:]
+        Dx, Dy = D @ x, D @ y
+        jac = np.sqrt(Dx ** 2 + Dy ** 2)
+        gA = np.vstack([(2 * np.pi / N) * Dy, -(2 * np.pi / N) * Dx])
+        gL = np.vstack([-(2 * np.pi / N) * (D @ (Dx / jac)), -(2 * np.pi / N) * (D @ (Dy / jac))])
+        r = z - X0
+        nr = np.linalg.norm(r, axis=0)
+        gF = np.where(nr > 0, r / np.where(nr > 0, nr, 1) / nX, 0.0) / nv
+        ca = -lam[:nv] / a0 / nv + (a - a0) / a0 ** 2 / (mu * nv)
+        cl = -lam[nv:] / l0 / nv + (l - l0) / l0 ** 2 / (mu * nv)
+        return gF + ca * gA + cl * gL
+
+    it = 0
+    while it < maxiter:
+        m1 = np.zeros_like(z)
+        m2 = np.zeros_like(z)
+        done = False
+        for step in range(1, inner + 1):
+            a, l, f = forward(z)
+            if f < tol_f and np.max(np.abs(a - a0) / a0) < tol_c and np.max(np.abs(l - l0) / l0) < tol_c:
+                done = True
+                break
+            g = grad(z, a, l)
+            m1 = 0.9 * m1 + 0.1 * g
+            m2 = 0.999 * m2 + 0.001 * g * g
+            bc1 = 1 - 0.9 ** step
+            bc2 = 1 - 0.999 ** step
+            z = z - (lr / bc1) * m1 / (np.sqrt(m2) / math.sqrt(bc2) + 1e-8)
+        if done:
+            break
+        lam = lam - (1 / mu) * np.concatenate([(a - a0) / a0, (l - l0) / l0])
+        mu *= 0.8
+        it += 1
+    out = X.copy()
+    out[:, mask] = z
+    return out
+
+
+def deriv_stencil(n):
+    """First-derivative circulant column (Nyquist mode zeroed)."""
+    r = np.arange(n)
+    k = np.arange(1, n // 2)
+    return -(2.0 / n) * (k[None, :] * np.sin(2 * np.pi * np.outer(r, k) / n)).sum(axis=1)

@@ -185,7 +185,53 @@ def job_step(promote, which):
     return out
 
 
+def job_post(promote):
+    """Post-step conditioning (curve_batch_compile.py:590-972) on perturbed shapes."""
+    import ref_shim
+    from ves2dpy_gb300.suspension import vesicle_shape
+    R = ref_shim.load(promote=promote)
+    torch = R.torch
+    dtype = torch.float64 if promote else torch.float32
+    oc = R.curve.Curve()
+    out = {}
+    for tag, N, area in (("unit", 32, 0.06), ("big", 32, float(np.pi))):
+        rng = np.random.default_rng(21 if tag == "unit" else 22)
+        nv = 4
+        X = np.zeros((2 * N, nv))
+        for k in range(nv):
+            # non-equispaced parametrisation: theta -> theta + 0.15 sin(theta)
+            x, y = vesicle_shape(N, rng, 0.65 + 0.05 * k, area=area)
+            th = np.arange(N) * 2 * np.pi / N
+            z = np.fft.fft(x + 1j * y) / N
+            m = np.concatenate([np.arange(0, N // 2), np.arange(-N // 2, 0)])
+            tw = th + 0.15 * np.sin(th + k)
+            zz = (z[None, :] * np.exp(1j * np.outer(tw, m))).sum(1)
+            X[:N, k] = zz.real + 2.0 * k
+            X[N:, k] = zz.imag - 1.0 * k
+        modes = torch.concatenate((torch.arange(0, N // 2), torch.arange(-N // 2, 0)))
+        Xt = torch.tensor(X, dtype=dtype)
+        X1, good = oc.redistributeArcLength(Xt.clone(), modes)
+        X5 = Xt.clone()
+        for _ in range(5):
+            X5, _ = oc.redistributeArcLength(X5, modes)
+        Xal = oc.alignCenterAngle(Xt, X5)
+        ctr = oc.getPhysicalCenter(Xt)
+        ia = oc.getIncAngle(Xt)
+        _, a0, l0 = oc.geomProp(Xt)
+        # a shape whose area and length are off by a few percent
+        Xpert = Xt.clone()
+        Xpert[:, 1] = Xpert[:, 1] * 1.03
+        Xpert[:N, 2] = Xpert[:N, 2] * 1.02
+        Xc = oc.correctAreaAndLengthAugLag(Xpert.clone(), a0, l0)
+        out.update({f"X_{tag}": X, f"redist1_{tag}": _np(X1), f"redist5_{tag}": _np(X5), f"align_{tag}": _np(Xal),
+                    f"center_{tag}": _np(ctr), f"incangle_{tag}": _np(ia), f"pert_{tag}": _np(Xpert),
+                    f"corrected_{tag}": _np(Xc), f"a0_{tag}": _np(a0), f"l0_{tag}": _np(l0)})
+    return out
+
+
 JOBS = {
+    'post_fp64': (job_post, True, ()),
+    'post_mixed': (job_post, False, ()),
     'far_fp64': (job_far, True, ()),
     'capsules_fp64': (job_capsules, True, ()),
     'capsules_mixed': (job_capsules, False, ()),

@@ -185,3 +185,28 @@ def test_time_step_matlab_near_vs_oracle():
     assert not iflag
     assert abs(it - ref.iters) <= 1
     assert rel(Xn, ref.X) < 1e-9
+
+
+@pytest.mark.parametrize("tag", ["unit", "big"])
+def test_post_step_conditioning(golden, tag):
+    from ves2dpy_gb300.curve import Curve
+    g = golden("post_fp64")
+    X = g[f"X_{tag}"]
+    N = X.shape[0] // 2
+    oc = Curve()
+    assert rel(oc.getPhysicalCenter(T(X)), g[f"center_{tag}"]) < FP64_TOL
+    assert np.max(np.abs(oc.getIncAngle(T(X)).cpu().numpy() - g[f"incangle_{tag}"])) < FP64_TOL
+    modes = torch.cat((torch.arange(0, N // 2), torch.arange(-N // 2, 0)))
+    X1, good = oc.redistributeArcLength(T(X), modes)
+    assert not good
+    X5 = T(X)
+    for _ in range(5):
+        X5, _ = oc.redistributeArcLength(X5, modes)
+    # unit-length curves are what the reference's 2*pi slope assumes; on longer
+    # curves each pass amplifies round-off (1e-16 -> 1e-6 after five), so 1e-5 is asked
+    tol = FP64_TOL if tag == "unit" else 1e-5
+    assert rel(X1, g[f"redist1_{tag}"]) < tol
+    assert rel(X5, g[f"redist5_{tag}"]) < tol
+    assert rel(oc.alignCenterAngle(T(X), T(g[f"redist5_{tag}"])), g[f"align_{tag}"]) < FP64_TOL
+    Xc = oc.correctAreaAndLengthAugLag(T(g[f"pert_{tag}"]), T(g[f"a0_{tag}"]), T(g[f"l0_{tag}"]))
+    assert rel(Xc, g[f"corrected_{tag}"]) < 1e-9

@@ -123,3 +123,21 @@ def test_time_step_vs_mixed_reference(golden):
     prm = O.StepParams(dt=float(g["dt"]), speed=float(g["speed"]))
     res = O.time_step(X, np.zeros((N, nv)), prm, O.PotenTables(N))
     assert rel(res.X, g["X1"]) < 1e-6
+
+
+@pytest.mark.parametrize("tag", ["unit", "big"])
+def test_post_step_conditioning(golden, tag):
+    g = golden("post_fp64")
+    X = g[f"X_{tag}"]
+    assert rel(O.physical_center(X), g[f"center_{tag}"]) < 1e-12
+    assert np.max(np.abs(O.inc_angle(X) - g[f"incangle_{tag}"])) < 1e-12
+    X1, _ = O.redistribute_arc_length(X)
+    X5 = X.copy()
+    for _ in range(5):
+        X5, _ = O.redistribute_arc_length(X5)
+    tol = 1e-10 if tag == "unit" else 1e-6
+    assert rel(X1, g[f"redist1_{tag}"]) < tol
+    assert rel(X5, g[f"redist5_{tag}"]) < tol
+    assert rel(O.align_center_angle(X, g[f"redist5_{tag}"]), g[f"align_{tag}"]) < 1e-10
+    Xc = O.correct_area_length(g[f"pert_{tag}"], g[f"a0_{tag}"], g[f"l0_{tag}"])
+    assert rel(Xc, g[f"corrected_{tag}"]) < 1e-9

@@ -138,6 +138,11 @@ SIGNATURES = {
     "ves_biem_step": (_I, [_P, ctypes.POINTER(StepParams), _I, _P, _P, _P, _P, ctypes.POINTER(StepResult), _P,
                            _SZ, _P]),
     "ves_biem_step_workspace": (_SZ, [_P, ctypes.POINTER(StepParams), _I]),
+    "ves_redistribute_arclength": (_I, [_P, _I, _P, _P, _P, ctypes.POINTER(_I), _P]),
+    "ves_align_center_angle": (_I, [_P, _I, _P, _P, _P, _P]),
+    "ves_center_angle": (_I, [_P, _I, _P, _P, _P, _P]),
+    "ves_correct_area_length": (_I, [_P, _I, _P, _P, _P, _P, ctypes.POINTER(_I), _P, _SZ, _P]),
+    "ves_correct_area_length_workspace": (_SZ, [_P, _I]),
     "ves_farfield_static_scratch": (_I, [_I, _I, _I, _P, _P, _I, _I, _P, _P, _P, _P]),
     "ves_ctx_set_timing": (_I, [_P, _I]),
     "ves_ctx_stats": (_I, [_P, ctypes.POINTER(Stats), _I]),

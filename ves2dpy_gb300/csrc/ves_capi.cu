@@ -184,3 +184,51 @@ extern "C" int ves_near_sing_int(ves_ctx* c, int scheme, int precision, int nv, 
   if (rc) return rc;
   return finish(c, s, "ves_near_sing_int");
 }
+
+extern "C" int ves_redistribute_arclength(ves_ctx* c, int nv, const double* X, double* Xout, int* flags,
+                                          int* all_good, void* stream) {
+  VES_REQUIRE(c && X && Xout && flags && nv >= 0, "ves_redistribute_arclength: bad arguments");
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = post_redistribute(c, nv, X, Xout, flags, s);
+  if (rc || !all_good) return rc;
+  *all_good = 1;
+  if (nv == 0) return VES_OK;
+  int* h = (int*)c->h_scal;  // pinned scratch, nv ints at most 512 at a time
+  for (int k0 = 0; k0 < nv; k0 += 512) {
+    const int n = nv - k0 < 512 ? nv - k0 : 512;
+    rc = ves_cuda_status(cudaMemcpyAsync(h, flags + k0, n * sizeof(int), cudaMemcpyDeviceToHost, s), "flags");
+    if (!rc) rc = ves_cuda_status(cudaStreamSynchronize(s), "flags sync");
+    if (rc) return rc;
+    for (int i = 0; i < n; ++i)
+      if (!h[i]) *all_good = 0;
+  }
+  return VES_OK;
+}
+
+extern "C" int ves_align_center_angle(ves_ctx* c, int nv, const double* Xorg, const double* X, double* Xout,
+                                      void* stream) {
+  VES_REQUIRE(c && Xorg && X && Xout && nv >= 0, "ves_align_center_angle: bad arguments");
+  launch_align_center_angle(c, nv, Xorg, X, Xout, nullptr, nullptr, (cudaStream_t)stream);
+  return ves_launch_check("ves_align_center_angle");
+}
+
+extern "C" int ves_center_angle(ves_ctx* c, int nv, const double* X, double* center, double* angle, void* stream) {
+  VES_REQUIRE(c && X && nv >= 0, "ves_center_angle: bad arguments");
+  launch_align_center_angle(c, nv, nullptr, X, nullptr, center, angle, (cudaStream_t)stream);
+  return ves_launch_check("ves_center_angle");
+}
+
+extern "C" size_t ves_correct_area_length_workspace(ves_ctx* c, int nv) {
+  if (!c) return 0;
+  WsCarver w(nullptr, 0);
+  post_correct_area_length(c, nv, nullptr, nullptr, nullptr, nullptr, nullptr, w, 0);
+  return w.off + 256;
+}
+
+extern "C" int ves_correct_area_length(ves_ctx* c, int nv, const double* X, const double* area0,
+                                       const double* length0, double* Xout, int* outer_iters, void* ws,
+                                       size_t ws_bytes, void* stream) {
+  VES_REQUIRE(c && X && area0 && length0 && Xout && ws && nv >= 0, "ves_correct_area_length: bad arguments");
+  WsCarver w(ws, ws_bytes);
+  return post_correct_area_length(c, nv, X, area0, length0, Xout, outer_iters, w, (cudaStream_t)stream);
+}

@@ -25,6 +25,10 @@ struct ves_ctx {
   double* Rm;      // [N][Nup] restriction
   double* Pm;      // [Nup][N] prolongation
   double* lag;     // [7][7]  Lagrange interpolation matrix (poten.py:977-990)
+  double* c6;      // [6N]  N->6N prolongation circulant (arc-length reparametrisation grid)
+  double* c6d;     // [6N]  its derivative
+  double* cos6;    // [6N]  cos(2 pi r / 6N)
+  double* sin6;    // [6N]  sin(2 pi r / 6N)
   // FP32 copies used by the mixed-precision Alpert build
   float* Rm32;
   float* Pm32;
@@ -133,6 +137,13 @@ int near_sing_int_run(ves_ctx* c, int scheme, int precision, int nv, const doubl
                       const double* sa_up, const double* Xup, const double* f, const double* vself,
                       const ves_near_lists* nl, double h, double* LP, double* near_only, WsCarver& ws,
                       cudaStream_t s);
+
+// post-step conditioning
+int post_redistribute(ves_ctx* c, int nv, const double* X, double* Xout, int* flags, cudaStream_t s);
+void launch_align_center_angle(ves_ctx* c, int nv, const double* Xorg, const double* X, double* Xout,
+                               double* center, double* angle, cudaStream_t s);
+int post_correct_area_length(ves_ctx* c, int nv, const double* X, const double* area0, const double* length0,
+                             double* Xout, int* outer_iters, WsCarver& ws, cudaStream_t s);
 
 // vector kernels (GMRES)
 void launch_dot_partials(long long n, const double* a, const double* b, double* partials,

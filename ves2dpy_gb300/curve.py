@@ -1,6 +1,8 @@
 """Curve calculus on the device (reference: mytorch/curve_batch_compile.py)."""
 from __future__ import annotations
 
+import ctypes
+
 import torch
 
 from . import _native as nat
@@ -42,3 +44,79 @@ class Curve:
         nat.check(ctx.lib.ves_geom_prop(ctx.handle, nv, Xv.data_ptr(), out[0].data_ptr(), out[1].data_ptr(),
                                         out[2].data_ptr(), nat.stream_ptr(X.device)), "geomProp")
         return out[0], out[1], out[2]
+
+    # -- post-step conditioning -------------------------------------------------
+    def getPhysicalCenter(self, X):
+        """Physical centre (2, nv) (curve_batch_compile.py:84-100)."""
+        c, _ = self._center_angle(X)
+        return c
+
+    def getIncAngle(self, X):
+        """Inclination angle in [0, pi] (curve_batch_compile.py:105-194)."""
+        _, a = self._center_angle(X)
+        return a
+
+    def _center_angle(self, X):
+        X = as_device_f64(X)
+        N, nv = X.shape[0] // 2, X.shape[1]
+        ctx = nat.context(N, X.device)
+        Xv = to_vm(X)
+        c = torch.empty(nv, 2, dtype=torch.float64, device=X.device)
+        a = torch.empty(nv, dtype=torch.float64, device=X.device)
+        nat.check(ctx.lib.ves_center_angle(ctx.handle, nv, Xv.data_ptr(), c.data_ptr(), a.data_ptr(),
+                                           nat.stream_ptr(X.device)), "center_angle")
+        return c.t().contiguous(), a
+
+    def alignCenterAngle(self, Xorg, X):
+        """Rigid motion of X onto the centre and angle of Xorg (curve_batch_compile.py:842-901)."""
+        X = as_device_f64(X)
+        N, nv = X.shape[0] // 2, X.shape[1]
+        ctx = nat.context(N, X.device)
+        Xo, Xv = to_vm(as_device_f64(Xorg)), to_vm(X)
+        out = torch.empty_like(Xv)
+        nat.check(ctx.lib.ves_align_center_angle(ctx.handle, nv, Xo.data_ptr(), Xv.data_ptr(), out.data_ptr(),
+                                                 nat.stream_ptr(X.device)), "alignCenterAngle")
+        return from_vm(out)
+
+    def redistributeArcLength(self, X, modes=None):
+        """One equi-arclength pass (curve_batch_compile.py:905-972).  Like the
+        reference, ``X`` is updated in place when it is a float64 CUDA tensor;
+        returns (X, allGood)."""
+        Xd = as_device_f64(X)
+        N, nv = Xd.shape[0] // 2, Xd.shape[1]
+        if modes is not None:
+            m = torch.as_tensor(modes).cpu()
+            ref = torch.cat((torch.arange(0, N // 2), torch.arange(-N // 2, 0)))
+            if m.numel() != N or not torch.equal(m.to(ref.dtype), ref):
+                raise ValueError("redistributeArcLength: modes must be [0..N/2-1, -N/2..-1]")
+        ctx = nat.context(N, Xd.device)
+        Xv = to_vm(Xd)
+        out = torch.empty_like(Xv)
+        flags = torch.empty(nv, dtype=torch.int32, device=Xd.device)
+        good = ctypes.c_int(0)
+        nat.check(ctx.lib.ves_redistribute_arclength(ctx.handle, nv, Xv.data_ptr(), out.data_ptr(),
+                                                     flags.data_ptr(), ctypes.byref(good),
+                                                     nat.stream_ptr(Xd.device)), "redistributeArcLength")
+        res = from_vm(out)
+        if X is Xd:
+            X.copy_(res)
+            res = X
+        return res, bool(good.value)
+
+    def correctAreaAndLengthAugLag(self, X, area0, length0):
+        """Nearest shape with the original area and length, for vesicles off by
+        more than 1e-2 (curve_batch_compile.py:590-710)."""
+        X = as_device_f64(X)
+        N, nv = X.shape[0] // 2, X.shape[1]
+        ctx = nat.context(N, X.device)
+        Xv = to_vm(X)
+        a0 = as_device_f64(area0, X.device).contiguous()
+        l0 = as_device_f64(length0, X.device).contiguous()
+        out = torch.empty_like(Xv)
+        ws = ctx.workspace(ctx.lib.ves_correct_area_length_workspace(ctx.handle, nv))
+        it = ctypes.c_int(0)
+        nat.check(ctx.lib.ves_correct_area_length(ctx.handle, nv, Xv.data_ptr(), a0.data_ptr(), l0.data_ptr(),
+                                                  out.data_ptr(), ctypes.byref(it), ws.data_ptr(), ws.numel(),
+                                                  nat.stream_ptr(X.device)), "correctAreaAndLengthAugLag")
+        self.last_auglag_iters = it.value
+        return from_vm(out)

@@ -798,7 +798,11 @@ def redistribute_arc_length(X):
     X = X.copy()
     jac = np.sqrt(sum(d ** 2 for d in get_dxy(X)))
     mean = jac.mean(axis=0)
-    redo = np.abs(jac - mean).max(axis=0) > 1e-5 * mean
+    # torch.linalg.norm(jac - mean, ord=inf) of the (N, nv) matrix is the
+    # matrix infinity norm (largest row sum over all vesicles), one scalar
+    # that every vesicle's threshold is compared with (:953)
+    spread = np.abs(jac - mean).sum(axis=1).max()
+    redo = spread > 1e-5 * mean
     if not redo.any():
         return X, True
     ids = np.nonzero(redo)[0]

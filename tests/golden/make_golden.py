@@ -229,7 +229,156 @@ def job_post(promote):
     return out
 
 
+def mlarm_suspension(nv=4, N=128, seed=17):
+    """Four unit-length vesicles (reduced area 0.65), one pair closer than 1/N."""
+    import math
+    from ves2dpy_gb300.suspension import random_suspension
+    return random_suspension(nv, N, 0.35, min_gap=0.003, area=0.65 / (4 * math.pi), seed=seed)
+
+
+def _mlarm_instance(R, precision, root, dt=1e-5, speed=2.0):
+    """The reference MLARM with seeded synthetic networks saved as TorchScript
+    files where its constructor looks for them (``../trained/torch_script_models``
+    relative to the working directory)."""
+    torch = R.torch
+    from ves2dpy_gb300.mlarm_weights import NETS, NET_ARGS, MODEL_FILES, synthetic_state_dict, synthetic_norms
+    mdir = os.path.join(root, "trained", "torch_script_models")
+    os.makedirs(mdir, exist_ok=True)
+    os.makedirs(os.path.join(root, "run"), exist_ok=True)
+    for name in NETS:
+        m = getattr(R.nets, name)(*NET_ARGS[name])
+        sd = synthetic_state_dict(name, 0)
+        m.load_state_dict({k: torch.from_numpy(v) for k, v in sd.items()}, strict=False)
+        m.eval()
+        torch.jit.script(m).save(os.path.join(mdir, MODEL_FILES[name]))
+    nrm = synthetic_norms(0)
+
+    def T(a):
+        return torch.from_numpy(np.asarray(a, dtype=np.float64))
+
+    def vinf(X):  # shear, entry_driver_manyfreeSpaceVesicle_N128.py:53
+        N = X.shape[0] // 2
+        return speed * torch.vstack((X[N:], torch.zeros_like(X[:N])))
+
+    cwd = os.getcwd()
+    os.chdir(os.path.join(root, "run"))
+    try:
+        oc = R.curve.Curve()
+        m = R.wrapper.MLARM_manyfree_py(
+            dt, vinf, oc, False, 1e2, -1,
+            T(nrm["adv_in"]), T(nrm["adv_out"]), T(nrm["relax_in"]), T(nrm["relax_out"]),
+            T(nrm["near_in"]), T(nrm["near_out"]), T(nrm["selften_in"]), T(nrm["selften_out"]),
+            T(nrm["advten_in"]), T(nrm["advten_out"]), device=torch.device("cpu"), logger=None)
+    finally:
+        os.chdir(cwd)
+    if precision == "fp64":
+        for net in (m.relaxNetwork, m.mergedAdvNetwork, m.nearNetwork, m.tenSelfNetwork, m.tenAdvNetwork):
+            net.model.double()
+    return m, oc
+
+
+def job_mlarm(precision):
+    """Two MLARM steps (time_step_many_noinfo, N128:986-1206) with stage outputs of the first."""
+    import tempfile
+    import ref_shim
+    R = ref_shim.load_mlarm(precision)
+    torch = R.torch
+    root = tempfile.mkdtemp(prefix="mlarm_golden_")
+    m, oc = _mlarm_instance(R, precision, root)
+    X0 = mlarm_suspension()
+    N, nv = X0.shape[0] // 2, X0.shape[1]
+    X = torch.from_numpy(X0.copy())
+    # entry_driver_manyfreeSpaceVesicle_N128.py:157-167: reference area and
+    # length first, then up to 10 redistribution passes
+    area0, len0 = oc.geomProp(X)[1:]
+    m.area0, m.len0 = area0, len0
+    modes = torch.concatenate((torch.arange(0, N // 2), torch.arange(-N // 2, 0)))
+    for _ in range(10):
+        X, flag = oc.redistributeArcLength(X, modes)
+        if flag:
+            break
+    Xinit = X.clone()
+    rec = {}
+
+    def wrap(cls, name):
+        f = getattr(cls, name)
+
+        def g(self, *a, **k):
+            r = f(self, *a, **k)
+            # copies: redistributeArcLength later updates some results in place
+            rec.setdefault(name, []).append(_clone(r))
+            return r
+        setattr(cls, name, g)
+
+    def _clone(r):
+        if isinstance(r, torch.Tensor):
+            return r.clone()
+        if isinstance(r, (tuple, list)):
+            return type(r)(_clone(x) for x in r)
+        return r
+
+    for nm in ("standardizationStep", "translateVinfwTorch", "relaxWTorchNet", "invTenMatOnVback",
+               "invTenMatOnSelfBend", "computeStokesInteractions_noinfo"):
+        wrap(type(m), nm)
+    for nm in ("alignCenterAngle", "correctAreaAndLengthAugLag"):
+        wrap(type(oc), nm)
+    ten = torch.zeros((N, nv), dtype=torch.float64)  # entry :121
+    out = {"X0": X0, "Xinit": _np(Xinit), "area0": _np(area0), "len0": _np(len0)}
+    for step in range(2):
+        with torch.no_grad():
+            X, ten = m.time_step_many_noinfo(X, ten, 3)
+        out[f"X{step + 1}"] = _np(X)
+        out[f"ten{step + 1}"] = _np(ten)
+        if step == 0:
+            Xs, sv = rec["standardizationStep"][0]
+            out["stand_X"] = _np(Xs)
+            for k, v in zip(("scaling", "rotate", "rotCenter", "trans", "sortIdx"), sv):
+                out["stand_" + k] = _np(v)
+            Xs2, sv2 = rec["standardizationStep"][1]
+            out["relax_stand_X"] = _np(Xs2)
+            f1, _, ids = rec["computeStokesInteractions_noinfo"][0]
+            out["far1"] = _np(f1)
+            for i in range(3):
+                out[f"near_ids{i}"] = _np(ids[i])
+            out["far2"] = _np(rec["computeStokesInteractions_noinfo"][1][0])
+            out["vback_solve"] = _np(rec["invTenMatOnVback"][0])
+            out["selfbend_solve"] = _np(rec["invTenMatOnSelfBend"][0])
+            out["Xadv"] = _np(rec["translateVinfwTorch"][0])
+            out["Xrelax"] = _np(rec["relaxWTorchNet"][0])
+            out["Xalign"] = _np(rec["alignCenterAngle"][0])
+            out["Xcorr"] = _np(rec["correctAreaAndLengthAugLag"][0])
+    return out
+
+
+def job_nets(precision):
+    """Each network's output (FP64 reference modules) on seeded inputs, one vesicle.
+
+    The merged networks are independent per channel group, so only groups
+    0-3 and the last two are stored."""
+    import ref_shim
+    from ves2dpy_gb300.mlarm_weights import NETS, NET_ARGS, synthetic_state_dict, net_test_input
+    R = ref_shim.load_mlarm(precision)
+    torch = R.torch
+    out = {}
+    for name, spec in NETS.items():
+        m = getattr(R.nets, name)(*NET_ARGS[name])
+        m.load_state_dict({k: torch.from_numpy(v) for k, v in synthetic_state_dict(name, 0).items()}, strict=False)
+        m.eval()
+        m.double()
+        x = torch.from_numpy(net_test_input(name))
+        with torch.no_grad():
+            y = m(x).numpy()
+        co = spec.cout
+        groups = [0, 1, 2, 3, spec.rep - 2, spec.rep - 1] if spec.rep > 6 else list(range(spec.rep))
+        out[name + "_groups"] = np.asarray(groups)
+        out[name] = np.stack([y[:, g * co:(g + 1) * co] for g in groups], axis=1)  # (nv, groups, cout, L)
+    return out
+
+
 JOBS = {
+    'mlarm_fp64': (job_mlarm, 'fp64', ()),
+    'mlarm_mixed': (job_mlarm, 'mixed', ()),
+    'nets_fp64': (job_nets, 'fp64', ()),
     'post_fp64': (job_post, True, ()),
     'post_mixed': (job_post, False, ()),
     'far_fp64': (job_far, True, ()),

@@ -96,3 +96,82 @@ def load(promote: bool = True, variant: str = "mytorch"):
         tstep_biem=tstep_biem, torch=torch,
     )
     return ns
+
+
+def load_mlarm(precision: str = "fp64"):
+    """Import the reference MLARM N=128 wrapper (``newtorch/``) for golden runs.
+
+    Import order follows the reference driver
+    (``newtorch/entry_driver_manyfreeSpaceVesicle_N128.py:1-20``): the
+    ``newtorch`` modules come first, ``newtorch/tools`` provides ``filter``,
+    the project root provides ``model_zoo``, and ``fft1`` (absent from
+    ``newtorch``) comes from ``mytorch``.  ``torch.compile`` is replaced by
+    the identity, so the ``@torch.compile(backend='cudagraphs')`` methods
+    (``wrapper_MLARM_batch_compile_N128.py:4140,4154``) run eagerly on CPU.
+
+    As written, the reference step cannot run with stock PyTorch in either
+    dtype: with float64 shapes ``redistributeArcLength`` writes a complex64
+    result into the float64 ``X`` (``curve_batch_compile.py:962-970``,
+    "Index put requires the source and destination dtypes match"), and with
+    float32 shapes ``buildVelocityInNear`` multiplies ``.double()`` network
+    outputs with a float32 force (``wrapper_MLARM_batch_compile_N128.py:1831``,
+    "expected scalar type Float but found Double").  Two minimal patches make
+    it run:
+
+    * ``precision="mixed"``: ``Tensor.cfloat`` returns complex128, so the
+      geometry runs in FP64 and the networks in the reference's FP32
+      (``.float()`` casts in ``model_zoo/get_network_torch.py``) -- the
+      combination the driver sets up (float64 initial shapes,
+      ``entry_driver_manyfreeSpaceVesicle_N128.py:4,100``);
+    * ``precision="fp64"``: the whole reference, networks included (the
+      caller converts the loaded models with ``.double()``), runs in FP64
+      through the same rebinding ``load(promote=True)`` uses.
+    """
+    import torch
+
+    torch.set_default_device("cpu")
+    _install_cupy_stub()
+    if precision == "fp64":
+        _promote_torch_to_fp64()
+    elif precision == "mixed":
+        torch.Tensor.cfloat = torch.Tensor.cdouble
+    else:
+        raise ValueError(precision)
+
+    def _identity_compile(fn=None, **_kw):
+        if fn is None:
+            return lambda f: f
+        return fn
+
+    torch.compile = _identity_compile
+    # model_zoo/Net_ves_factor.py:3 and Net_ves_merge_nocoords_nearFourier.py:3
+    # import torchsummary (a printing helper they never call).
+    ts = types.ModuleType("torchsummary")
+    ts.summary = lambda *a, **k: None
+    sys.modules.setdefault("torchsummary", ts)
+    for sub in ("mytorch", "", "newtorch/tools", "newtorch"):
+        p = os.path.join(REF_ROOT, sub) if sub else REF_ROOT
+        if p in sys.path:
+            sys.path.remove(p)
+        sys.path.insert(0, p)
+    import wrapper_MLARM_batch_compile_N128 as wrapper
+    import curve_batch_compile
+    import capsules
+    import biem_support
+    import filter as ref_filter
+    import poten
+    from model_zoo import (Net_ves_factor, Net_ves_merge_adv, Net_ves_selften,
+                           Net_ves_merge_advten, Net_ves_merge_nocoords_nearFourier)
+
+    ns = types.SimpleNamespace(
+        wrapper=wrapper, curve=curve_batch_compile, capsules=capsules,
+        biem_support=biem_support, filter=ref_filter, poten=poten, torch=torch,
+        nets=types.SimpleNamespace(
+            relax=Net_ves_factor.pdeNet_Ves_factor_periodic,
+            adv=Net_ves_merge_adv.Net_merge_advection,
+            selften=Net_ves_selften.Net_ves_selften,
+            advten=Net_ves_merge_advten.Net_ves_merge_advten,
+            near=Net_ves_merge_nocoords_nearFourier.Net_ves_merge_nocoords_nearFourier,
+        ),
+    )
+    return ns

@@ -225,11 +225,15 @@ VES_API size_t ves_biem_step_workspace(ves_ctx* ctx, const ves_step_params* prm,
 /* ---- post-step shape conditioning (curve_batch_compile.py) ---------------- */
 /* One redistributeArcLength pass (curve_batch_compile.py:905-972, with
  * my_arcLengthParameter :1039-1092 and the driver's Fourier modes
- * driver_confined.py:240): Xout[nv][2][N] (may alias X); flags[nv] device
- * ints (1 = already equispaced within 1e-5, left unchanged); *all_good (host,
- * may be NULL: no synchronisation) = all flags set. */
+ * driver_confined.py:240): Xout[nv][2][N] (may alias X); flags[nv]
+ * device ints (1 = left unchanged); *all_good (host, may be NULL: no
+ * synchronisation) = all flags set.  As in the reference, a vesicle is
+ * re-parametrised when the matrix infinity norm of the jacobian deviations
+ * of the whole suspension (one scalar, :953) exceeds 1e-5 times its own mean
+ * jacobian. */
 VES_API int ves_redistribute_arclength(ves_ctx* ctx, int nv, const double* X, double* Xout, int* flags,
-                                       int* all_good, void* stream);
+                                       int* all_good, void* ws, size_t ws_bytes, void* stream);
+VES_API size_t ves_redistribute_arclength_workspace(ves_ctx* ctx, int nv);
 /* alignCenterAngle (curve_batch_compile.py:842-901): rigid motion of X onto
  * the physical centre and inclination angle of Xorg. */
 VES_API int ves_align_center_angle(ves_ctx* ctx, int nv, const double* Xorg, const double* X, double* Xout,
@@ -246,6 +250,103 @@ VES_API int ves_correct_area_length(ves_ctx* ctx, int nv, const double* X, const
                                     const double* length0, double* Xout, int* outer_iters, void* ws,
                                     size_t ws_bytes, void* stream);
 VES_API size_t ves_correct_area_length_workspace(ves_ctx* ctx, int nv);
+
+/* ---- MLARM surrogate networks (model_zoo/Net_ves_*.py) -------------------- */
+/* A network is a chain of blocks of one template applied to ``groups``
+ * independent channel groups (grouped convolutions, model_zoo/Net_ves_merge_adv.py:6-191):
+ *   A = bn1(relu(conv7,s2,circ pad 3 (x)) ++ relu(conv7,s2,dil 2,circ pad 6 (x)))   2*c1 channels, L/2
+ *   B = bn2(the same pair on A)                                                  2*c2 channels, L/4
+ *   C = bn3(relu(convT10,s2,pad 4 (B)));  D = bn4(relu(convT10,s2,pad 4 (C)))   2*c2 channels, L/2, L
+ *   out = [conv3,zero pad 1 (D) (+ x[0:cmix] if residual)] ++ x[cin-npass:cin]
+ * Activations are [nv][groups*channels][length] in the network's precision. */
+#define VES_NET_FP64 0             /* CUDA cores, FP64 (parity)                     */
+#define VES_NET_FP32 1             /* CUDA cores, FP32 (the reference networks' type) */
+typedef struct ves_net ves_net;
+typedef struct ves_net_block {
+  int cin, c1, c2, cmix, residual, npass;
+} ves_net_block;
+/* ``params`` holds 30 host pointers per block, in the reference's full
+ * (all-groups) parameter layout and this order: conv1_1.{weight,bias},
+ * conv1_2.{..}, conv2_1.{..}, conv2_2.{..}, deconv1.{..}, deconv2.{..},
+ * mix.{..}, then bn1..bn4.{weight,bias,running_mean,running_var}
+ * (eval-mode batch norm, eps 1e-5).  Replaces the TorchScript models loaded
+ * by get_network_torch.py:26-35, 137-142, 217-223, 316-323, 403-415.
+ * Allocates the weights on the current device. */
+VES_API int ves_net_create(int precision, int groups, int length, int nblocks, const ves_net_block* blocks,
+                           const float* const* params, ves_net** out);
+VES_API int ves_net_destroy(ves_net* net);
+VES_API int ves_net_info(const ves_net* net, int* precision, int* groups, int* length, int* cin, int* cout);
+/* Forward pass (model(input), e.g. get_network_torch.py:76): in
+ * [nv][groups*cin][length] -> out [nv][groups*cout][length]. */
+VES_API int ves_net_forward(const ves_net* net, int nv, const void* in, void* out, void* ws, size_t ws_bytes,
+                            void* stream);
+VES_API size_t ves_net_forward_workspace(const ves_net* net, int nv);
+
+/* ---- MLARM step (newtorch/wrapper_MLARM_batch_compile_N128.py) ------------- */
+/* Normalisation constants of the five networks, host FP64, the shapes the
+ * reference constructor takes (entry_driver_manyfreeSpaceVesicle_N128.py:120-155). */
+typedef struct ves_mlarm_norms {
+  const double* adv_in;       /* [127][4] */
+  const double* adv_out;      /* [127][4] */
+  const double* relax_in;     /* [4]      */
+  const double* relax_out;    /* [4]      */
+  const double* near_in;      /* [128][4] */
+  const double* near_out;     /* [128][2][12] */
+  const double* selften_in;   /* [4]      */
+  const double* selften_out;  /* [2]      */
+  const double* advten_in;    /* [127][4] */
+  const double* advten_out;   /* [127][4] */
+} ves_mlarm_norms;
+typedef struct ves_mlarm ves_mlarm;
+/* MLARM_manyfree_py.__init__ (:650-710) for N = 128: binds the context and the
+ * five networks (relax [1 group, 2->2, L 128], adv [127, 2->2, L 256],
+ * near [128, 2->12, L 128], selften [1, 2->1, L 128], advten [127, 2->2,
+ * L 128]; all of one precision) and copies the constants to the device.
+ * ``near`` may be NULL when the step never evaluates it. */
+VES_API int ves_mlarm_create(ves_ctx* ctx, const ves_net* relax, const ves_net* adv, const ves_net* near,
+                             const ves_net* selften, const ves_net* advten, const ves_mlarm_norms* norms,
+                             ves_mlarm** out);
+VES_API int ves_mlarm_destroy(ves_mlarm* m);
+typedef struct ves_mlarm_params {
+  double dt, kappa;
+  int flow;                   /* background flow when vback is NULL (VES_FLOW_*) */
+  double speed, chan_width, vortex_size;
+  int farfield_precision;     /* VES_PREC_* of the two all-pairs sums            */
+  int eval_near_net;          /* 1: evaluate the near-field network as the reference
+                                 does (:1034); its velocities enter the step only
+                                 through the repulsion force, zero here          */
+  int maxc;                   /* near-pair candidate capacity per vesicle (0: 64) */
+} ves_mlarm_params;
+typedef struct ves_mlarm_result {
+  int n_near_pairs;           /* excluded (target point, source vesicle) pairs   */
+  int auglag_iters;           /* augmented-Lagrangian updates of the correction  */
+} ves_mlarm_result;
+/* Optional device buffers receiving stage outputs of the step (NULL = skip):
+ * the standardised shape and its values (:4119-4138), the two far fields
+ * (:2495-2675, before filtering), the two tension solves (:3632-3688), the
+ * advected shape (:3584-3620, before filtering), the relaxed shape (:3622),
+ * and the aligned and corrected shapes (:1160-1179). */
+typedef struct ves_mlarm_trace {
+  double *Xstand, *scaling, *rotate, *rot_center, *trans;  /* [nv][2][N], [nv], [nv], [nv][2], [nv][2] */
+  int* sort_idx;                                           /* [nv][N] */
+  double *far1, *far2, *vback_solve, *selfbend_solve;      /* [nv][2][N] x2, [nv][N] x2 */
+  double *Xadv, *Xrelax, *Xalign, *Xcorr;                  /* [nv][2][N] */
+} ves_mlarm_trace;
+/* time_step_many_noinfo(Xold, tenOld, nlayers=3) (:986-1206) without
+ * repulsion: X[nv][2][N], ten[nv][N] -> Xout, ten_out.  vback[nv][2][N] is
+ * vinf(Xold) (may be NULL: computed from prm->flow).  area0/len0[nv] are the
+ * reference area and length of the correction (:1172). */
+VES_API int ves_mlarm_step(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double* X,
+                           const double* ten, const double* vback, const double* area0, const double* len0,
+                           double* Xout, double* ten_out, ves_mlarm_result* res, const ves_mlarm_trace* trace,
+                           void* ws, size_t ws_bytes, void* stream);
+VES_API size_t ves_mlarm_step_workspace(ves_mlarm* m, const ves_mlarm_params* prm, int nv);
+/* standardizationStep (:4119-4138): five redistribution passes, then the
+ * reference values (:4179-4223) and the standardised shape. */
+VES_API int ves_mlarm_standardize(ves_ctx* ctx, int nv, const double* X, double* Xstand, double* scaling,
+                                  double* rotate, double* rot_center, double* trans, int* sort_idx, void* ws,
+                                  size_t ws_bytes, void* stream);
+VES_API size_t ves_mlarm_standardize_workspace(ves_ctx* ctx, int nv);
 
 /* ---- all-pairs sum without allocation (no counterpart in the reference) ---- */
 /* The sum of ves_farfield (no near-pair lists) for callers that cannot allocate

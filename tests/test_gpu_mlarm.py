@@ -1,0 +1,120 @@
+"""GPU parity of the MLARM path: the network engine and the whole step.
+
+References: ``tests/golden/nets_fp64.npz`` (reference model classes, FP64),
+``mlarm_fp64.npz`` (two reference MLARM steps, everything FP64) and
+``mlarm_mixed.npz`` (FP64 geometry, the reference's FP32 networks).
+Weights and normalisation constants are the seeded synthetic ones.
+"""
+import functools
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+DEV = torch.device("cuda:0")
+
+
+def rel(a, b):
+    a = a.detach().cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+    b = np.asarray(b)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@functools.lru_cache(maxsize=1)
+def _state_dicts():
+    from ves2dpy_gb300.mlarm_weights import NETS, synthetic_state_dict
+    return {n: synthetic_state_dict(n, 0) for n in NETS}
+
+
+@functools.lru_cache(maxsize=2)
+def _mlarm(net_precision, farfield_precision):
+    from ves2dpy_gb300.curve import Curve
+    from ves2dpy_gb300.mlarm import MLARM_manyfree_py
+    from ves2dpy_gb300.mlarm_weights import synthetic_norms
+    nrm = {k: torch.from_numpy(v) for k, v in synthetic_norms(0).items()}
+
+    def vinf(X):
+        N = X.shape[0] // 2
+        return 2.0 * torch.vstack((X[N:], torch.zeros_like(X[:N])))
+
+    return MLARM_manyfree_py(1e-5, vinf, Curve(), False, 1e2, -1,
+                             nrm["adv_in"], nrm["adv_out"], nrm["relax_in"], nrm["relax_out"],
+                             nrm["near_in"], nrm["near_out"], nrm["selften_in"], nrm["selften_out"],
+                             nrm["advten_in"], nrm["advten_out"], DEV, state_dicts=_state_dicts(),
+                             net_precision=net_precision, farfield_precision=farfield_precision)
+
+
+# FP64 engine: summation order only; FP32 engine: the reference networks' own type
+NET_TOL = {"fp64": 1e-12, "fp32": 1e-4}
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("name", ["relax", "adv", "near", "selften", "advten"])
+def test_network_engine_matches_reference(golden, name, precision):
+    from ves2dpy_gb300.mlarm import Network
+    from ves2dpy_gb300.mlarm_weights import NETS, net_test_input
+    g = golden("nets_fp64")
+    spec = NETS[name]
+    net = Network(name, _state_dicts()[name], precision, DEV)
+    y = net(torch.from_numpy(net_test_input(name))).double().cpu().numpy()
+    co = spec.cout
+    ys = np.stack([y[:, k * co:(k + 1) * co] for k in g[name + "_groups"]], axis=1)
+    err = rel(ys, g[name])
+    assert err < NET_TOL[precision], (name, precision, err)
+
+
+def test_network_engine_batch_of_vesicles():
+    """Vesicles are independent: a batch equals its members run alone."""
+    from ves2dpy_gb300.mlarm import Network
+    from ves2dpy_gb300.mlarm_weights import net_test_input
+    net = Network("advten", _state_dicts()["advten"], "fp32", DEV)
+    x = torch.from_numpy(net_test_input("advten", nv=3, seed=11))
+    yb = net(x)
+    for v in range(3):
+        assert torch.equal(net(x[v:v + 1]), yb[v:v + 1])
+
+
+def test_standardization_matches_reference(golden):
+    g = golden("mlarm_fp64")
+    m = _mlarm("fp64", "fp64")
+    Xs, (sc, rot, rc, tr, si) = m.standardizationStep(torch.from_numpy(g["Xinit"]).to(DEV))
+    assert rel(Xs, g["stand_X"]) < 1e-10
+    assert rel(sc, g["stand_scaling"]) < 1e-12
+    assert rel(rot, g["stand_rotate"]) < 1e-10
+    assert rel(rc, g["stand_rotCenter"]) < 1e-10
+    assert rel(tr, g["stand_trans"]) < 1e-10
+    assert np.array_equal(si.cpu().numpy(), g["stand_sortIdx"])
+
+
+def test_mlarm_step_fp64_matches_reference(golden):
+    """FP64 networks and far field: every stage and two steps at 1e-10."""
+    g = golden("mlarm_fp64")
+    m = _mlarm("fp64", "fp64")
+    m.area0 = torch.from_numpy(g["area0"])
+    m.len0 = torch.from_numpy(g["len0"])
+    X0 = torch.from_numpy(g["Xinit"]).to(DEV)
+    t = m.time_step_trace(X0, torch.zeros(128, 4, dtype=torch.float64, device=DEV))
+    assert m.last_result.n_near_pairs == len(g["near_ids0"])
+    for k in ("far1", "far2", "vback_solve", "selfbend_solve", "Xadv", "Xrelax", "Xalign", "Xcorr"):
+        assert rel(t[k], g[k]) < 1e-10, (k, rel(t[k], g[k]))
+    assert rel(t["X"], g["X1"]) < 1e-10
+    assert rel(t["ten"], g["ten1"]) < 1e-10
+    X2, t2 = m.time_step_many_noinfo(t["X"], t["ten"], 3)
+    assert rel(X2, g["X2"]) < 1e-10
+    assert rel(t2, g["ten2"]) < 1e-10
+
+
+def test_mlarm_step_fp32_networks(golden):
+    """FP32 networks and the compensated FP32 far field, against the FP64
+    reference and against the reference with its own FP32 networks."""
+    m = _mlarm("fp32", "fp32c")
+    for fixture, tol_x, tol_t in (("mlarm_fp64", 1e-4, 1e-3), ("mlarm_mixed", 1e-4, 1e-3)):
+        g = golden(fixture)
+        m.area0 = torch.from_numpy(g["area0"])
+        m.len0 = torch.from_numpy(g["len0"])
+        X1, t1 = m.time_step_many_noinfo(torch.from_numpy(g["Xinit"]).to(DEV),
+                                         torch.zeros(128, 4, dtype=torch.float64, device=DEV), 3)
+        assert rel(X1, g["X1"]) < tol_x, (fixture, rel(X1, g["X1"]))
+        assert rel(t1, g["ten1"]) < tol_t, (fixture, rel(t1, g["ten1"]))

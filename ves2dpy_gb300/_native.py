@@ -110,6 +110,41 @@ _LL = ctypes.c_longlong
 _SZ = ctypes.c_size_t
 
 # name: (restype, argtypes)
+class NetBlock(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("cin", "c1", "c2", "cmix", "residual", "npass")]
+
+
+class MlarmNorms(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("adv_in", "adv_out", "relax_in", "relax_out", "near_in", "near_out",
+                                               "selften_in", "selften_out", "advten_in", "advten_out")]
+
+
+class MlarmParams(ctypes.Structure):
+    _fields_ = [
+        ("dt", ctypes.c_double),
+        ("kappa", ctypes.c_double),
+        ("flow", ctypes.c_int),
+        ("speed", ctypes.c_double),
+        ("chan_width", ctypes.c_double),
+        ("vortex_size", ctypes.c_double),
+        ("farfield_precision", ctypes.c_int),
+        ("eval_near_net", ctypes.c_int),
+        ("maxc", ctypes.c_int),
+    ]
+
+
+class MlarmResult(ctypes.Structure):
+    _fields_ = [("n_near_pairs", ctypes.c_int), ("auglag_iters", ctypes.c_int)]
+
+
+class MlarmTrace(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("Xstand", "scaling", "rotate", "rot_center", "trans", "sort_idx",
+                                               "far1", "far2", "vback_solve", "selfbend_solve", "Xadv", "Xrelax",
+                                               "Xalign", "Xcorr")]
+
+
+NET_PREC = {"fp64": 0, "fp32": 1}
+
 SIGNATURES = {
     "ves_ctx_create": (_I, [_I, ctypes.POINTER(_P)]),
     "ves_ctx_destroy": (_I, [_P]),
@@ -138,7 +173,22 @@ SIGNATURES = {
     "ves_biem_step": (_I, [_P, ctypes.POINTER(StepParams), _I, _P, _P, _P, _P, ctypes.POINTER(StepResult), _P,
                            _SZ, _P]),
     "ves_biem_step_workspace": (_SZ, [_P, ctypes.POINTER(StepParams), _I]),
-    "ves_redistribute_arclength": (_I, [_P, _I, _P, _P, _P, ctypes.POINTER(_I), _P]),
+    "ves_redistribute_arclength": (_I, [_P, _I, _P, _P, _P, ctypes.POINTER(_I), _P, _SZ, _P]),
+    "ves_redistribute_arclength_workspace": (_SZ, [_P, _I]),
+    "ves_net_create": (_I, [_I, _I, _I, _I, ctypes.POINTER(NetBlock), ctypes.POINTER(ctypes.c_void_p),
+                            ctypes.POINTER(_P)]),
+    "ves_net_destroy": (_I, [_P]),
+    "ves_net_info": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
+                          ctypes.POINTER(_I)]),
+    "ves_net_forward": (_I, [_P, _I, _P, _P, _P, _SZ, _P]),
+    "ves_net_forward_workspace": (_SZ, [_P, _I]),
+    "ves_mlarm_create": (_I, [_P, _P, _P, _P, _P, _P, ctypes.POINTER(MlarmNorms), ctypes.POINTER(_P)]),
+    "ves_mlarm_destroy": (_I, [_P]),
+    "ves_mlarm_step": (_I, [_P, ctypes.POINTER(MlarmParams), _I, _P, _P, _P, _P, _P, _P, _P,
+                            ctypes.POINTER(MlarmResult), ctypes.POINTER(MlarmTrace), _P, _SZ, _P]),
+    "ves_mlarm_step_workspace": (_SZ, [_P, ctypes.POINTER(MlarmParams), _I]),
+    "ves_mlarm_standardize": (_I, [_P, _I, _P, _P, _P, _P, _P, _P, _P, _P, _SZ, _P]),
+    "ves_mlarm_standardize_workspace": (_SZ, [_P, _I]),
     "ves_align_center_angle": (_I, [_P, _I, _P, _P, _P, _P]),
     "ves_center_angle": (_I, [_P, _I, _P, _P, _P, _P]),
     "ves_correct_area_length": (_I, [_P, _I, _P, _P, _P, _P, ctypes.POINTER(_I), _P, _SZ, _P]),

@@ -185,11 +185,19 @@ extern "C" int ves_near_sing_int(ves_ctx* c, int scheme, int precision, int nv, 
   return finish(c, s, "ves_near_sing_int");
 }
 
+extern "C" size_t ves_redistribute_arclength_workspace(ves_ctx* c, int nv) {
+  if (!c) return 0;
+  WsCarver w(nullptr, 0);
+  post_redistribute(c, nv, nullptr, nullptr, nullptr, w, 0);
+  return w.off + 256;
+}
+
 extern "C" int ves_redistribute_arclength(ves_ctx* c, int nv, const double* X, double* Xout, int* flags,
-                                          int* all_good, void* stream) {
-  VES_REQUIRE(c && X && Xout && flags && nv >= 0, "ves_redistribute_arclength: bad arguments");
+                                          int* all_good, void* ws, size_t ws_bytes, void* stream) {
+  VES_REQUIRE(c && X && Xout && flags && ws && nv >= 0, "ves_redistribute_arclength: bad arguments");
   cudaStream_t s = (cudaStream_t)stream;
-  int rc = post_redistribute(c, nv, X, Xout, flags, s);
+  WsCarver w(ws, ws_bytes);
+  int rc = post_redistribute(c, nv, X, Xout, flags, w, s);
   if (rc || !all_good) return rc;
   *all_good = 1;
   if (nv == 0) return VES_OK;

@@ -139,7 +139,8 @@ int near_sing_int_run(ves_ctx* c, int scheme, int precision, int nv, const doubl
                       cudaStream_t s);
 
 // post-step conditioning
-int post_redistribute(ves_ctx* c, int nv, const double* X, double* Xout, int* flags, cudaStream_t s);
+int post_redistribute(ves_ctx* c, int nv, const double* X, double* Xout, int* flags, WsCarver& ws,
+                      cudaStream_t s);
 void launch_align_center_angle(ves_ctx* c, int nv, const double* Xorg, const double* X, double* Xout,
                                double* center, double* angle, cudaStream_t s);
 int post_correct_area_length(ves_ctx* c, int nv, const double* X, const double* area0, const double* length0,

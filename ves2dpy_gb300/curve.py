@@ -94,9 +94,10 @@ class Curve:
         out = torch.empty_like(Xv)
         flags = torch.empty(nv, dtype=torch.int32, device=Xd.device)
         good = ctypes.c_int(0)
+        ws = ctx.workspace(ctx.lib.ves_redistribute_arclength_workspace(ctx.handle, nv))
         nat.check(ctx.lib.ves_redistribute_arclength(ctx.handle, nv, Xv.data_ptr(), out.data_ptr(),
-                                                     flags.data_ptr(), ctypes.byref(good),
-                                                     nat.stream_ptr(Xd.device)), "redistributeArcLength")
+                                                     flags.data_ptr(), ctypes.byref(good), ws.data_ptr(),
+                                                     ws.numel(), nat.stream_ptr(Xd.device)), "redistributeArcLength")
         res = from_vm(out)
         if X is Xd:
             X.copy_(res)

@@ -261,6 +261,8 @@ VES_API size_t ves_correct_area_length_workspace(ves_ctx* ctx, int nv);
  * Activations are [nv][groups*channels][length] in the network's precision. */
 #define VES_NET_FP64 0             /* CUDA cores, FP64 (parity)                     */
 #define VES_NET_FP32 1             /* CUDA cores, FP32 (the reference networks' type) */
+#define VES_NET_BF16 2             /* tcgen05 tensor cores: BF16 operands, FP32 accumulation,
+                                      FP32 activations between blocks and at the I/O  */
 typedef struct ves_net ves_net;
 typedef struct ves_net_block {
   int cin, c1, c2, cmix, residual, npass;
@@ -277,7 +279,8 @@ VES_API int ves_net_create(int precision, int groups, int length, int nblocks, c
 VES_API int ves_net_destroy(ves_net* net);
 VES_API int ves_net_info(const ves_net* net, int* precision, int* groups, int* length, int* cin, int* cout);
 /* Forward pass (model(input), e.g. get_network_torch.py:76): in
- * [nv][groups*cin][length] -> out [nv][groups*cout][length]. */
+ * [nv][groups*cin][length] -> out [nv][groups*cout][length], FP64 for
+ * VES_NET_FP64 and FP32 otherwise. */
 VES_API int ves_net_forward(const ves_net* net, int nv, const void* in, void* out, void* ws, size_t ws_bytes,
                             void* stream);
 VES_API size_t ves_net_forward_workspace(const ves_net* net, int nv);

@@ -143,7 +143,7 @@ class MlarmTrace(ctypes.Structure):
                                                "Xalign", "Xcorr")]
 
 
-NET_PREC = {"fp64": 0, "fp32": 1}
+NET_PREC = {"fp64": 0, "fp32": 1, "bf16": 2}
 
 SIGNATURES = {
     "ves_ctx_create": (_I, [_I, ctypes.POINTER(_P)]),

@@ -24,7 +24,8 @@
 #include "ves_internal.h"
 
 // engine entry points (ves_nets.cu)
-int net_forward_run(const ves_net* net, int nv, const void* in, void* out, WsCarver& ws, cudaStream_t s);
+int net_forward_run(const ves_net* net, int nv, const void* in, void* out, WsCarver& ws, VesDeviceStatus* st,
+                    cudaStream_t s);
 int net_dims(const ves_net* net, int* groups, int* length, int* cin, int* cout);
 
 namespace {
@@ -640,7 +641,7 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
     for (const ves_net* n : nets) {
       if (!n) continue;
       WsCarver w(nullptr, 0);
-      net_forward_run(n, nv, nullptr, nullptr, w, s);
+      net_forward_run(n, nv, nullptr, nullptr, w, nullptr, s);
       scratch = std::max(scratch, w.off);
     }
     WsCarver w(nullptr, 0);
@@ -709,7 +710,7 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
     prep_modes_kernel<Real><<<ceil_div((long long)nv * kNearModes * 2 * N, 256), 256, 0, s>>>(nv, N, kNearModes, Xs,
                                                                                              m->near_in, nin);
     WsCarver w = sub();
-    if ((rc = net_forward_run(m->near, nv, nin, nout, w, s))) return rc;
+    if ((rc = net_forward_run(m->near, nv, nin, nout, w, c->status, s))) return rc;
   }
   // near pairs (compare1 :429-536): target points of a vesicle closer than 1/N
   // to an upsampled point of another vesicle
@@ -738,13 +739,13 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
                                                                                        m->advten_in, nin);
   {
     WsCarver w = sub();
-    if ((rc = net_forward_run(m->advten, nv, nin, nout, w, s))) return rc;
+    if ((rc = net_forward_run(m->advten, nv, nin, nout, w, c->status, s))) return rc;
   }
   ves_count_launch();
   prep_xy_kernel<Real><<<gb, 256, 0, s>>>(nv, N, Xs, m->selften_in, nin);
   {
     WsCarver w = sub();
-    if ((rc = net_forward_run(m->selften, nv, nin, nout2, w, s))) return rc;
+    if ((rc = net_forward_run(m->selften, nv, nin, nout2, w, c->status, s))) return rc;
   }
   ves_count_launch();
   tension_kernel<Real><<<nv, 128, (size_t)4 * N * sizeof(double), s>>>(
@@ -763,7 +764,7 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
   prep_adv_kernel<Real><<<ceil_div((long long)nv * kModes * 2 * 2 * N, 256), 256, 0, s>>>(nv, N, Xs, m->adv_in, nin);
   {
     WsCarver w = sub();
-    if ((rc = net_forward_run(m->adv, nv, nin, nout, w, s))) return rc;
+    if ((rc = net_forward_run(m->adv, nv, nin, nout, w, c->status, s))) return rc;
   }
   ves_count_launch();
   translate_kernel<Real><<<nv, 128, (size_t)6 * N * sizeof(double), s>>>(N, prm->dt, X, vsum, rot, sidx, nout,
@@ -780,7 +781,7 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
   prep_xy_kernel<Real><<<gb, 256, 0, s>>>(nv, N, Xs2, m->relax_in, nin);
   {
     WsCarver w = sub();
-    if ((rc = net_forward_run(m->relax, nv, nin, nout, w, s))) return rc;
+    if ((rc = net_forward_run(m->relax, nv, nin, nout, w, c->status, s))) return rc;
   }
   ves_count_launch();
   relax_post_kernel<Real><<<nv, 128, 0, s>>>(N, prm->dt, Xs2, nout, m->relax_out, scal2, rot2, rotc2, trn2, sidx2, Xa);

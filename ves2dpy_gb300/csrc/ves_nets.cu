@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "ves_internal.h"
+#include "ves_nets_tc.h"
 
 namespace {
 
@@ -196,6 +197,11 @@ struct ves_net {
   int cmax = 0;                 // largest channel count per group of any block output
   void* d_w = nullptr;
   size_t elem = 4;
+  // tensor-core path
+  std::vector<TcBlock> tcb;
+  unsigned char* d_tc = nullptr;
+  int mid_max = 0;
+  VesDeviceStatus* d_status = nullptr;
 };
 
 namespace {
@@ -269,11 +275,14 @@ int run_block(const ves_net* net, int bi, int nv, const Real* in, Real* out, cud
 }
 
 template <typename Real>
-int net_forward_t(const ves_net* net, int nv, const Real* in, Real* out, WsCarver& ws, cudaStream_t s) {
+int net_forward_t(const ves_net* net, int nv, const Real* in, Real* out, WsCarver& ws, VesDeviceStatus* st,
+                  cudaStream_t s) {
   const size_t buf = (size_t)nv * net->groups * net->cmax * net->length;
   const int nb = (int)net->blocks.size();
   Real* p0 = nb > 1 ? ws.take<Real>(buf) : nullptr;
   Real* p1 = nb > 2 ? ws.take<Real>(buf) : nullptr;
+  const bool tc = net->precision == VES_NET_BF16;
+  unsigned char* mid = tc ? ws.take<unsigned char>((size_t)nv * net->groups * net->mid_max) : nullptr;
   if (ws.sizing) return VES_OK;
   if (!ws.ok()) {
     ves_record_error(VES_ERR_WORKSPACE, "net_forward: workspace too small (%zu needed)", ws.off);
@@ -283,7 +292,15 @@ int net_forward_t(const ves_net* net, int nv, const Real* in, Real* out, WsCarve
   const Real* src = in;
   for (int bi = 0; bi < nb; ++bi) {
     Real* dst = (bi == nb - 1) ? out : ((bi & 1) ? p1 : p0);
-    int rc = run_block<Real>(net, bi, nv, src, dst, s);
+    int rc;
+    if (tc) {
+      const TcBlock& tb = net->tcb[bi];
+      rc = tcnet_run_block(tb, net->groups, nv, net->d_tc + tb.down_off, net->d_tc + tb.up_off,
+                           reinterpret_cast<const float*>(src), reinterpret_cast<float*>(dst), mid,
+                           st ? st : net->d_status, s);
+    } else {
+      rc = run_block<Real>(net, bi, nv, src, dst, s);
+    }
     if (rc) return rc;
     src = dst;
   }
@@ -292,10 +309,11 @@ int net_forward_t(const ves_net* net, int nv, const Real* in, Real* out, WsCarve
 
 }  // namespace
 
-int net_forward_run(const ves_net* net, int nv, const void* in, void* out, WsCarver& ws, cudaStream_t s) {
+int net_forward_run(const ves_net* net, int nv, const void* in, void* out, WsCarver& ws, VesDeviceStatus* st,
+                    cudaStream_t s) {
   if (net->precision == VES_NET_FP64)
-    return net_forward_t<double>(net, nv, (const double*)in, (double*)out, ws, s);
-  return net_forward_t<float>(net, nv, (const float*)in, (float*)out, ws, s);
+    return net_forward_t<double>(net, nv, (const double*)in, (double*)out, ws, st, s);
+  return net_forward_t<float>(net, nv, (const float*)in, (float*)out, ws, st, s);
 }
 
 int net_dims(const ves_net* net, int* groups, int* length, int* cin, int* cout) {
@@ -313,7 +331,7 @@ extern "C" int ves_net_create(int precision, int groups, int length, int nblocks
     return VES_ERR_ARG;
   }
   *out = nullptr;
-  if (precision != VES_NET_FP64 && precision != VES_NET_FP32) {
+  if (precision != VES_NET_FP64 && precision != VES_NET_FP32 && precision != VES_NET_BF16) {
     ves_record_error(VES_ERR_ARG, "net_create: precision %d not supported", precision);
     return VES_ERR_ARG;
   }
@@ -330,6 +348,7 @@ extern "C" int ves_net_create(int precision, int groups, int length, int nblocks
   net->groups = groups;
   net->length = length;
   net->elem = precision == VES_NET_FP64 ? 8 : 4;
+  const bool tc = precision == VES_NET_BF16;
   long long total = 0;
   int prev_out = blocks[0].cin;
   for (int i = 0; i < nblocks; ++i) {
@@ -348,7 +367,7 @@ extern "C" int ves_net_create(int precision, int groups, int length, int nblocks
       }
     BlockGeom g = make_geom(b);
     const size_t sh = precision == VES_NET_FP64 ? block_smem<double>(g, length) : block_smem<float>(g, length);
-    if (sh > 227 * 1024) {
+    if (!tc && sh > 227 * 1024) {
       ves_record_error(VES_ERR_ARG, "net_create: block %d needs %zu bytes of shared memory", i, sh);
       delete net;
       return VES_ERR_ARG;
@@ -359,11 +378,45 @@ extern "C" int ves_net_create(int precision, int groups, int length, int nblocks
     prev_out = b.cmix + b.npass;
     net->cmax = std::max(net->cmax, prev_out);
   }
-  std::vector<double> host((size_t)total);
-  for (int i = 0; i < nblocks; ++i) pack_block(net->blocks[i], groups, params + (size_t)i * 30, host.data() + net->boff[i]);
   int dev = 0;
   cudaGetDevice(&dev);
   net->device = dev;
+  int rc0 = ves_cuda_status(cudaMalloc(&net->d_status, sizeof(VesDeviceStatus)), "net status");
+  if (!rc0) rc0 = ves_cuda_status(cudaMemset(net->d_status, 0, sizeof(VesDeviceStatus)), "net status");
+  if (rc0) {
+    delete net;
+    return rc0;
+  }
+  if (tc) {
+    std::vector<unsigned char> img, down, up;
+    for (int i = 0; i < nblocks; ++i) {
+      TcBlock tb;
+      if (tcnet_pack(blocks[i], groups, length, params + (size_t)i * 30, down, up, tb)) {
+        ves_record_error(VES_ERR_ARG, "net_create: block %d does not fit the tensor-core kernels", i);
+        cudaFree(net->d_status);
+        delete net;
+        return VES_ERR_ARG;
+      }
+      tb.down_off = img.size();
+      img.insert(img.end(), down.begin(), down.end());
+      tb.up_off = img.size();
+      img.insert(img.end(), up.begin(), up.end());
+      net->mid_max = std::max(net->mid_max, tb.mid_bytes);
+      net->tcb.push_back(tb);
+    }
+    int rc = ves_cuda_status(cudaMalloc(&net->d_tc, img.size()), "net tc weights");
+    if (!rc) rc = ves_cuda_status(cudaMemcpy(net->d_tc, img.data(), img.size(), cudaMemcpyHostToDevice), "net upload");
+    if (rc) {
+      if (net->d_tc) cudaFree(net->d_tc);
+      cudaFree(net->d_status);
+      delete net;
+      return rc;
+    }
+    *out = net;
+    return VES_OK;
+  }
+  std::vector<double> host((size_t)total);
+  for (int i = 0; i < nblocks; ++i) pack_block(net->blocks[i], groups, params + (size_t)i * 30, host.data() + net->boff[i]);
   int rc = ves_cuda_status(cudaMalloc(&net->d_w, (size_t)total * net->elem), "net weights");
   if (rc) {
     delete net;
@@ -387,6 +440,8 @@ extern "C" int ves_net_create(int precision, int groups, int length, int nblocks
 extern "C" int ves_net_destroy(ves_net* net) {
   if (!net) return VES_OK;
   if (net->d_w) cudaFree(net->d_w);
+  if (net->d_tc) cudaFree(net->d_tc);
+  if (net->d_status) cudaFree(net->d_status);
   delete net;
   return VES_OK;
 }
@@ -401,7 +456,7 @@ extern "C" int ves_net_info(const ves_net* net, int* precision, int* groups, int
 extern "C" size_t ves_net_forward_workspace(const ves_net* net, int nv) {
   if (!net) return 0;
   WsCarver w(nullptr, 0);
-  net_forward_run(net, nv, nullptr, nullptr, w, 0);
+  net_forward_run(net, nv, nullptr, nullptr, w, nullptr, 0);
   return w.off + 256;
 }
 
@@ -417,5 +472,17 @@ extern "C" int ves_net_forward(const ves_net* net, int nv, const void* in, void*
   }
   char none = 0;  // a non-null base so that a one-block network (no workspace) runs
   WsCarver w(ws ? ws : (void*)&none, ws ? ws_bytes : 0);
-  return net_forward_run(net, nv, in, out, w, (cudaStream_t)stream);
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = net_forward_run(net, nv, in, out, w, nullptr, s);
+  if (rc || net->precision != VES_NET_BF16) return rc;
+  // the tensor-core kernels report bounded-wait timeouts in the status word
+  VesDeviceStatus h;
+  rc = ves_cuda_status(cudaMemcpyAsync(&h, net->d_status, sizeof(h), cudaMemcpyDeviceToHost, s), "net status");
+  if (!rc) rc = ves_cuda_status(cudaStreamSynchronize(s), "net status sync");
+  if (rc) return rc;
+  if (h.code != VES_OK) {
+    ves_record_error(h.code, "net_forward: tensor-core kernel reported status %d (site %d)", h.code, h.where);
+    return h.code;
+  }
+  return VES_OK;
 }

@@ -1,0 +1,23 @@
+// Host interface of the tensor-core network path (ves_nets_tc.cu).
+#pragma once
+
+#include <vector>
+
+#include "ves_internal.h"
+
+struct TcBlock {
+  int geo[64];          // opaque block geometry (tcnet::Geo)
+  int geo_bytes;
+  int dsize, usize;     // weight image bytes per group (down / up kernels)
+  int dsmem, usmem;     // dynamic shared memory of the two kernels
+  int mid_bytes;        // down -> up intermediate per (vesicle, group)
+  size_t down_off, up_off;  // byte offsets of the block's images in the device buffer
+};
+
+// Build the per-group weight images of one block (30 reference parameter
+// arrays, see ves_net_create) for sequence length L.
+int tcnet_pack(const ves_net_block& b, int G, int L, const float* const* params, std::vector<unsigned char>& down,
+               std::vector<unsigned char>& up, TcBlock& out);
+// One block: x [nv][G*cin][L] -> out [nv][G*cout][L] (FP32), mid = scratch of nv*G*mid_bytes.
+int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_down, const unsigned char* d_up,
+                    const float* x, float* out, unsigned char* mid, VesDeviceStatus* st, cudaStream_t s);

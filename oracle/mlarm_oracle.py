@@ -34,15 +34,16 @@ RELAX_DT_SCALE = 1e-5  # get_network_torch.py:77: DX / 1E-5 * dt
 # networks (model_zoo/*.py) through torch.nn.functional in float64
 # --------------------------------------------------------------------------
 
-def net_forward(spec, sd, x):
+def net_forward(spec, sd, x, dtype=np.float64):
     """Forward of a network described by ``spec`` (mlarm_weights.NetSpec) with
-    state dict ``sd`` on input x (nv, rep*cin, L); float64 numpy in/out."""
+    state dict ``sd`` on input x (nv, rep*cin, L); numpy in/out in ``dtype``
+    (float64 for parity, float32 to time the reference networks' precision)."""
     import torch
     import torch.nn.functional as F
 
     G = spec.rep
-    t = torch.from_numpy(np.asarray(x, dtype=np.float64))
-    W = {k: torch.from_numpy(np.asarray(v, dtype=np.float64)) for k, v in sd.items()}
+    t = torch.from_numpy(np.asarray(x, dtype=dtype))
+    W = {k: torch.from_numpy(np.asarray(v, dtype=dtype)) for k, v in sd.items()}
     nv = t.shape[0]
 
     def conv(inp, name, pad, dil):

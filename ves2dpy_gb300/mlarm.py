@@ -95,7 +95,8 @@ class MLARM_manyfree_py:
     Extra keyword arguments: ``state_dicts`` ({name: state dict} for the five
     networks "relax", "adv", "near", "selften", "advten"; default: the
     reference's TorchScript files under ``model_dir``), ``net_precision``
-    ("fp32", the reference networks' type, or "fp64"), ``farfield_precision``
+    ("fp32", the reference networks' type, "fp64", or "bf16" on the tensor
+    cores), ``farfield_precision``
     ("fp32c" or "fp64") and ``eval_near_net`` (evaluate the near-field
     network as the reference does; its output enters the step only through
     the repulsion force).

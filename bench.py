@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-net-timing", action="store_true", help="skip the per-network forward timings")
+    ap.add_argument("--only-net", default=None, help="time one network's forward pass at --nv and exit "
+                    "(relax, adv, near, selften, advten)")
     return ap.parse_args()
 
 
@@ -260,7 +263,7 @@ def run_mlarm(a, dev, X0, state_dicts):
 
     # networks alone at this nv (forward passes on the step's own input sizes)
     net_ms = {}
-    for n, net in m.nets.items():
+    for n, net in ({} if a.no_net_timing else m.nets).items():
         spec = NETS[n]
         x = torch.randn(nv, spec.rep * spec.cin, spec.L, device=dev, dtype=net.dtype)
         net(x)
@@ -285,7 +288,7 @@ def run_mlarm(a, dev, X0, state_dicts):
         Xback.copy_(Xn, non_blocking=True)
         tback.copy_(tn, non_blocking=True)
         torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / a.e2e_steps
+    e2e_s = (time.perf_counter() - t0) / max(a.e2e_steps, 1)
     io = Xh.numel() * 8 + th.numel() * 8
     X1_m = Xback.clone()
     return dict(ms=ms, stats=st, launches=launches, clocks=clk.summary(), net_ms=net_ms, e2e_s=e2e_s, io=io,
@@ -381,7 +384,7 @@ def run_gb300(a, rank, world):
     bf16_peak = peaks.get("bf16_tflops", 1900.0)
     flops = {n: net_flops(NETS[n]) * a.nv for n in NETS}
     net_total_ms = sum(r["net_ms"].values())
-    net_tflops = sum(flops.values()) / (net_total_ms * 1e-3) / 1e12
+    net_tflops = sum(flops.values()) / (net_total_ms * 1e-3) / 1e12 if net_total_ms > 0 else None
     out = {
         "metric": METRIC,
         "value": value,
@@ -410,7 +413,7 @@ def run_gb300(a, rank, world):
                       "farfield_ms_per_eval": ff_ms, "farfield_evals_per_step": st.farfield_launches / a.steps},
         },
         "e2e": {"value": world * a.nv / r["e2e_s"], "unit": "vesicle-steps/s", "h2d_bytes_per_step": r["io"],
-                "d2h_bytes_per_step": r["io"]},
+                "d2h_bytes_per_step": r["io"]} if r["e2e_s"] > 0 else None,
         "gpu_launches": int(r["launches"]),
         "roofline": {"bound": "sfu", "kernel": "ff_main_kernel<float> (all-pairs Stokeslet sum)",
                      "achieved": mufu_rate / 1e9, "peak": sfu_peak / 1e9, "unit": "Gop/s (MUFU lg2+rcp)",
@@ -422,7 +425,8 @@ def run_gb300(a, rank, world):
                      "peak_source": "measured by ves_probe_sfu_peak on this GPU",
                      "share_of_step": st.farfield_ms / r["ms"] if r["ms"] else None},
         "roofline_networks": {"bound": "tensor", "achieved": net_tflops, "peak": bf16_peak, "unit": "TFLOP/s",
-                              "frac": net_tflops / bf16_peak, "flops_per_step": sum(flops.values()),
+                              "frac": net_tflops / bf16_peak if net_tflops else None,
+                              "flops_per_step": sum(flops.values()),
                               "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured",
                               "kernels": "tcnet down_kernel / up_kernel (tcgen05.mma kind::f16, BF16)"},
         "clocks": r["clocks"],
@@ -464,10 +468,35 @@ def run_cpu_reference(a, rank):
             "e2e": {"value": v, "unit": "vesicle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_only_net(a):
+    """One network's forward pass (BF16 unless --nets fp32) at --nv, twice;
+    prints the second pass's CUDA-event time (a profiling target)."""
+    import torch
+    from ves2dpy_gb300.mlarm import Network
+    from ves2dpy_gb300.mlarm_weights import NETS, synthetic_state_dict
+    dev = torch.device("cuda", 0)
+    spec = NETS[a.only_net]
+    net = Network(a.only_net, synthetic_state_dict(a.only_net, 0), a.nets, dev)
+    x = torch.randn(a.nv, spec.rep * spec.cin, spec.L, device=dev, dtype=net.dtype)
+    net(x)
+    e0, e1 = _events()
+    torch.cuda.synchronize()
+    e0.record()
+    net(x)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    print(json.dumps({"network": a.only_net, "nv": a.nv, "precision": a.nets, "ms": ms,
+                      "tflops": net_flops(spec) * a.nv / (ms * 1e-3) / 1e12}), flush=True)
+
+
 def main():
     a = parse()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
+    if a.only_net:
+        run_only_net(a)
+        return
     if a.impl == "reference":
         out = run_cpu_reference(a, rank)
         if out is not None:

@@ -236,7 +236,7 @@ extern "C" int ves_ctx_create(int N, ves_ctx** out) {
   // host tables
   std::vector<double> d1N(N), d1Nup(Nup), pc(Nup), pcd(Nup), qw(c->nquad), cq(14 * Nup),
       ad(14 * Nup), Rm((size_t)N * Nup), Pm((size_t)Nup * N), lag(49), c6(6 * N), c6d(6 * N), cos6(6 * N),
-      sin6(6 * N);
+      sin6(6 * N), cosU(Nup), sinU(Nup);
   for (int r = 0; r < 6 * N; ++r) {
     const double t = 2.0 * VES_PI * r / (6 * N);
     c6[r] = cardinal(N, t);
@@ -250,6 +250,8 @@ extern "C" int ves_ctx_create(int N, ves_ctx** out) {
     double t = 2.0 * VES_PI * r / Nup;
     pc[r] = cardinal(N, t);
     pcd[r] = cardinal_deriv(N, t);
+    cosU[r] = cos(t);
+    sinU[r] = sin(t);
   }
   {
     const double h = 2.0 * VES_PI / Nup;
@@ -277,7 +279,7 @@ extern "C" int ves_ctx_create(int N, ves_ctx** out) {
 
   // one device buffer
   size_t nd = d1N.size() + d1Nup.size() + pc.size() + pcd.size() + qw.size() + cq.size() + ad.size() +
-              Rm.size() + Pm.size() + lag.size() + 4 * c6.size();
+              Rm.size() + Pm.size() + lag.size() + 4 * c6.size() + 2 * cosU.size();
   size_t nf = Rm.size() + Pm.size() + ad.size() + qw.size();
   size_t bytes = nd * sizeof(double) + nf * sizeof(float) + 1024;
   rc = ves_cuda_status(cudaMalloc(&c->d_buf, bytes), "cudaMalloc tables");
@@ -306,6 +308,8 @@ extern "C" int ves_ctx_create(int N, ves_ctx** out) {
   c->c6d = put(c6d);
   c->cos6 = put(cos6);
   c->sin6 = put(sin6);
+  c->cosU = put(cosU);
+  c->sinU = put(sinU);
   float* pf = (float*)p;
   auto putf = [&](std::vector<double>& v) {
     std::vector<float> h(v.begin(), v.end());

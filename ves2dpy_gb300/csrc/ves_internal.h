@@ -29,6 +29,8 @@ struct ves_ctx {
   double* c6d;     // [6N]  its derivative
   double* cos6;    // [6N]  cos(2 pi r / 6N)
   double* sin6;    // [6N]  sin(2 pi r / 6N)
+  double* cosU;    // [Nup] cos(2 pi r / Nup)
+  double* sinU;    // [Nup] sin(2 pi r / Nup)
   // FP32 copies used by the mixed-precision Alpert build
   float* Rm32;
   float* Pm32;

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "ves_internal.h"
+#include "ves_fft.cuh"
 
 // engine entry points (ves_nets.cu)
 int net_forward_run(const ves_net* net, int nv, const void* in, void* out, WsCarver& ws, VesDeviceStatus* st,
@@ -58,62 +59,77 @@ __device__ double bsum(double v, double* red) {
 // ---------------------------------------------------------------------------
 // fBend (:1007-1013): bending of the shape upsampled to Nup points
 // (capsules.bendingTerm, capsules.py:62-68, on capsules(upsample_fft(X, Nup)))
-// truncated back to N modes (downsample_fft, filter.py:197-219).
+// truncated back to N modes (downsample_fft, filter.py:197-219).  x and y are
+// packed as z = x + i y: the arc derivative (isa * ifft(ik fft(.)) with the
+// Nyquist mode zeroed) maps real sequences to real ones, so one complex FFT
+// pair per derivative serves both; the truncation keeps the real-part
+// semantics of each component's Nyquist coefficient separately.
 __global__ void bend_up_kernel(int N, int Nup, int m, const double* __restrict__ pc, const double* __restrict__ pcd,
-                               const double* __restrict__ d1up, double kappa, const double* __restrict__ X,
-                               double* __restrict__ fB) {
+                               const double* __restrict__ cosU, const double* __restrict__ sinU, double kappa,
+                               const double* __restrict__ X, double* __restrict__ fB) {
   extern __shared__ double sh[];
-  double* d = sh;        // [Nup]
-  double* is = d + Nup;  // [Nup]
-  double* a = is + Nup;  // [Nup]
-  double* b = a + Nup;   // [Nup]
-  double* xy = b + Nup;  // [2N]
+  double* is = sh;          // [Nup]
+  double* zr = is + Nup;    // [Nup]
+  double* zi = zr + Nup;    // [Nup]
+  double* tre = zi + Nup;   // [Nup]
+  double* tim = tre + Nup;  // [Nup]
+  double* xy = tim + Nup;   // [2N]
   const int k = blockIdx.x;
   const double* Xk = X + (long long)k * 2 * N;
-  for (int i = threadIdx.x; i < Nup; i += blockDim.x) d[i] = d1up[i];
   for (int i = threadIdx.x; i < 2 * N; i += blockDim.x) xy[i] = Xk[i];
   __syncthreads();
-  // |dXup/dtheta| of the interpolant on the Nup grid
+  // the interpolant and |dXup/dtheta| on the Nup grid
   for (int u = threadIdx.x; u < Nup; u += blockDim.x) {
-    double dx = 0, dy = 0;
+    double x = 0, y = 0, dx = 0, dy = 0;
     int r = u;
     for (int i = 0; i < N; ++i) {
+      x = fma(pc[r], xy[i], x);
+      y = fma(pc[r], xy[N + i], y);
       dx = fma(pcd[r], xy[i], dx);
       dy = fma(pcd[r], xy[N + i], dy);
       r -= m;
       if (r < 0) r += Nup;
     }
+    zr[u] = x;
+    zi[u] = y;
     is[u] = 1.0 / sqrt(dx * dx + dy * dy);
   }
-  for (int comp = 0; comp < 2; ++comp) {
-    __syncthreads();
+  // four arc derivatives: z <- isa * ifft(i k fft(z)), Nyquist zeroed
+  for (int it = 0; it < 4; ++it) {
+    ves_fft(zr, zi, tre, tim, Nup, cosU, sinU, -1);
     for (int u = threadIdx.x; u < Nup; u += blockDim.x) {
-      double v = 0;
-      int r = u;
-      for (int i = 0; i < N; ++i) {
-        v = fma(pc[r], xy[comp * N + i], v);
-        r -= m;
-        if (r < 0) r += Nup;
-      }
-      a[u] = v;
+      const double kk = (u < Nup / 2) ? (double)u : (u == Nup / 2 ? 0.0 : (double)(u - Nup));
+      const double a = zr[u], b = zi[u];
+      zr[u] = -kk * b / Nup;
+      zi[u] = kk * a / Nup;
     }
-    for (int it = 0; it < 4; ++it) {
-      __syncthreads();
-      for (int j = threadIdx.x; j < Nup; j += blockDim.x) b[j] = is[j] * circ(d, a, Nup, j);
-      __syncthreads();
-      for (int j = threadIdx.x; j < Nup; j += blockDim.x) a[j] = b[j];
+    ves_fft(zr, zi, tre, tim, Nup, cosU, sinU, +1);
+    for (int u = threadIdx.x; u < Nup; u += blockDim.x) {
+      zr[u] *= is[u];
+      zi[u] *= is[u];
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < N; i += blockDim.x) {
-      double v = 0;
-      for (int u = 0; u < Nup; ++u) {
-        int r = u - m * i;
-        r %= Nup;
-        if (r < 0) r += Nup;
-        v = fma(pc[r], a[u], v);
-      }
-      fB[(long long)k * 2 * N + comp * N + i] = -kappa * (v * ((double)N / Nup));
+  }
+  // downsample to N modes: frequencies -N/2+1..N/2-1 as they are, the -N/2
+  // slot carrying Re(X_-N/2) + i Re(Y_-N/2) of the two real components
+  ves_fft(zr, zi, tre, tim, Nup, cosU, sinU, -1);
+  double* wr = is;  // [N]; isa no longer needed
+  double* wi = is + N;
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    if (j < N / 2) {
+      wr[j] = zr[j];
+      wi[j] = zi[j];
+    } else if (j == N / 2) {
+      wr[j] = 0.5 * (zr[Nup - N / 2] + zr[N / 2]);
+      wi[j] = 0.5 * (zi[Nup - N / 2] + zi[N / 2]);
+    } else {
+      wr[j] = zr[Nup - N + j];
+      wi[j] = zi[Nup - N + j];
     }
+  }
+  ves_fft(wr, wi, tre, tim, N, cosU, sinU, +1, Nup / N);
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    fB[(long long)k * 2 * N + j] = -kappa * (wr[j] / Nup);
+    fB[(long long)k * 2 * N + N + j] = -kappa * (wi[j] / Nup);
   }
 }
 
@@ -687,14 +703,14 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
   // fTen = tensionTerm(tenOld); fBend = downsample(bendingTerm on Nup)  (:1007-1013)
   launch_trac_jump(c, nv, 0.0, isa, tang, X, 2LL * N, ten, N, fT, s);
   {
-    const size_t sh = (size_t)(4 * Nup + 2 * N) * sizeof(double);
+    const size_t sh = (size_t)(5 * Nup + 2 * N) * sizeof(double);
     if (sh > 48 * 1024) {
       rc = ves_cuda_status(cudaFuncSetAttribute(bend_up_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh),
                            "bend smem");
       if (rc) return rc;
     }
     ves_count_launch();
-    bend_up_kernel<<<nv, 512, sh, s>>>(N, Nup, c->m, c->pc, c->pcd, c->d1Nup, prm->kappa, X, fB);
+    bend_up_kernel<<<nv, 256, sh, s>>>(N, Nup, c->m, c->pc, c->pcd, c->cosU, c->sinU, prm->kappa, X, fB);
   }
   const unsigned gb = ceil_div(nn2, 256);
   ves_count_launch();
@@ -852,7 +868,7 @@ extern "C" int ves_mlarm_create(ves_ctx* ctx, const ves_net* relax, const ves_ne
     return VES_ERR_ARG;
   }
   *out = nullptr;
-  if (ctx->N != kN) {
+  if (ctx->N != kN || !ves_fft_size_ok(ctx->Nup)) {
     ves_record_error(VES_ERR_SHAPE, "mlarm_create: the networks are built for N = %d, context has N = %d", kN,
                      ctx->N);
     return VES_ERR_SHAPE;

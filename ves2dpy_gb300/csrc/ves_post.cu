@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "ves_internal.h"
+#include "ves_fft.cuh"
 
 namespace {
 
@@ -120,14 +121,15 @@ __global__ void redistribute_kernel(int N, const double* __restrict__ d1, const 
   double* d = sh;
   double* x = d + N;
   double* y = x + N;
-  double* arc = y + N;   // [M]
-  double* al = arc + M;  // [M]
-  double* Ck = al + M;   // [M/2]
-  double* Sk = Ck + M / 2;
-  double* th = Sk + M / 2;  // [N]
-  double* zr = th + N;      // [N]
-  double* zi = zr + N;      // [N]
-  double* red = zi + N;     // [blockDim]
+  double* are = y + N;     // [M] spectrum work arrays
+  double* aim = are + M;   // [M]
+  double* tre = aim + M;   // [M] FFT scratch
+  double* tim = tre + M;   // [M]
+  double* al = tim + M;    // [M]
+  double* th = al + M;     // [N]
+  double* zr = th + N;     // [N]
+  double* zi = zr + N;     // [N]
+  double* red = zi + N;    // [blockDim]
   const int k = blockIdx.x;
   const double* Xk = X + (long long)k * 2 * N;
   double* Ok = Xout + (long long)k * 2 * N;
@@ -141,9 +143,7 @@ __global__ void redistribute_kernel(int N, const double* __restrict__ d1, const 
   double js = 0.0;
   for (int j = threadIdx.x; j < N; j += blockDim.x) {
     const double dx = circ(d, x, N, j), dy = circ(d, y, N, j);
-    const double jac = sqrt(dx * dx + dy * dy);
-    arc[j] = jac;  // temporary
-    js += jac;
+    js += sqrt(dx * dx + dy * dy);
   }
   const double jsum = bsum(js, red);
   const double mean = jsum / N;
@@ -163,34 +163,24 @@ __global__ void redistribute_kernel(int N, const double* __restrict__ d1, const 
       r -= 6;
       if (r < 0) r += M;
     }
-    arc[u] = sqrt(dx * dx + dy * dy);
+    are[u] = sqrt(dx * dx + dy * dy);
+    aim[u] = 0.0;
   }
-  __syncthreads();
-  // Fourier coefficients C_k - i S_k of arc, k < M/2
-  for (int kk = threadIdx.x; kk < M / 2; kk += blockDim.x) {
-    double cs = 0, ss = 0;
-    int r = 0;
-    for (int u = 0; u < M; ++u) {
-      cs = fma(arc[u], cos6[r], cs);
-      ss = fma(arc[u], sin6[r], ss);
-      r += kk;
-      if (r >= M) r -= M;
-    }
-    Ck[kk] = cs;
-    Sk[kk] = ss;
+  // Fourier coefficients X_k = C_k - i S_k of arc (FFT of length 6N)
+  ves_fft(are, aim, tre, tim, M, cos6, sin6, -1);
+  const double C0 = are[0];
+  // al(t_u) = int_0^{t_u} arc = (C_0/M) t_u + sum_{k=1}^{M/2-1} 2/(k M) [C_k sin(k t_u) - S_k (cos(k t_u) - 1)]
+  //         = (C_0/M) t_u + sum_k 2/(k M) S_k + Im sum_k (2/(k M)) X_k e^{i k t_u}
+  double cpart = 0.0;
+  for (int kk = 1 + threadIdx.x; kk < M / 2; kk += blockDim.x) cpart += 2.0 / ((double)kk * M) * (-aim[kk]);
+  const double K0 = bsum(cpart, red);
+  for (int kk = threadIdx.x; kk < M; kk += blockDim.x) {
+    const double f = (kk >= 1 && kk < M / 2) ? 2.0 / ((double)kk * M) : 0.0;
+    are[kk] *= f;
+    aim[kk] *= f;
   }
-  __syncthreads();
-  // al(t_u) = int_0^{t_u} arc: (C_0/M) t + sum_k 2/(k M) [C_k sin(k t) - S_k (cos(k t) - 1)]
-  for (int u = threadIdx.x; u < M; u += blockDim.x) {
-    double s = Ck[0] / M * (2.0 * VES_PI * u / M);
-    int r = 0;
-    for (int kk = 1; kk < M / 2; ++kk) {
-      r += u;
-      if (r >= M) r -= M;
-      s += 2.0 / ((double)kk * M) * (Ck[kk] * sin6[r] - Sk[kk] * (cos6[r] - 1.0));
-    }
-    al[u] = s;
-  }
+  ves_fft(are, aim, tre, tim, M, cos6, sin6, +1);
+  for (int u = threadIdx.x; u < M; u += blockDim.x) al[u] = C0 / M * (2.0 * VES_PI * u / M) + K0 + aim[u];
   __syncthreads();
   // theta: lower_bound of i*L/N in al, linear step with slope 2 pi (the
   // reference's unit-length assumption, curve_batch_compile.py:1085-1087)
@@ -211,30 +201,38 @@ __global__ void redistribute_kernel(int N, const double* __restrict__ d1, const 
     const int idx = (lo == 0) ? 0 : lo - 1;  // torch gathers idx-1 (wraps to -1 only if target <= al[0])
     th[i] = 2.0 * VES_PI * idx / M + (target - al[idx]) * (2.0 * VES_PI);
   }
-  // fft(z)/N with the modes 0..N/2-1, -N/2..-1
+  // fft(z)/N with the modes 0..N/2-1, -N/2..-1 (length-N FFT, twiddles from the 6N table)
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    zr[j] = x[j];
+    zi[j] = y[j];
+  }
+  ves_fft(zr, zi, tre, tim, N, cos6, sin6, -1, 6);
   for (int m = threadIdx.x; m < N; m += blockDim.x) {
-    double rr = 0, ii = 0;
-    int r = 0;
-    for (int j = 0; j < N; ++j) {
-      // e^{-2 pi i m j / N} = cos6[6mj] - i sin6[6mj]
-      const double c = cos6[r], s = sin6[r];
-      rr += x[j] * c + y[j] * s;
-      ii += y[j] * c - x[j] * s;
-      r += 6 * m;
-      r %= M;
-    }
-    zr[m] = rr / N;
-    zi[m] = ii / N;
+    zr[m] /= N;
+    zi[m] /= N;
   }
   __syncthreads();
+  // z(theta_i) = sum_m zh_m e^{i m theta_i}; powers of e^{i theta} by recurrence
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
-    double re = 0, im = 0;
-    for (int mi = 0; mi < N; ++mi) {
-      const int mode = (mi < N / 2) ? mi : mi - N;
-      double s, c;
-      sincos(mode * th[i], &s, &c);
-      re += zr[mi] * c - zi[mi] * s;
-      im += zr[mi] * s + zi[mi] * c;
+    double s1, c1;
+    sincos(th[i], &s1, &c1);
+    double er = 1.0, ei = 0.0;
+    double re = zr[0], im = zi[0];
+    for (int kk = 1; kk < N / 2; ++kk) {
+      const double nr = er * c1 - ei * s1;
+      ei = er * s1 + ei * c1;
+      er = nr;
+      re += zr[kk] * er - zi[kk] * ei;  // mode +kk
+      im += zr[kk] * ei + zi[kk] * er;
+      re += zr[N - kk] * er + zi[N - kk] * ei;  // mode -kk: conjugate power
+      im += zi[N - kk] * er - zr[N - kk] * ei;
+    }
+    {
+      const double nr = er * c1 - ei * s1;  // mode -N/2
+      ei = er * s1 + ei * c1;
+      er = nr;
+      re += zr[N / 2] * er + zi[N / 2] * ei;
+      im += zi[N / 2] * er - zr[N / 2] * ei;
     }
     Ok[i] = re;
     Ok[N + i] = im;
@@ -496,12 +494,16 @@ int post_redistribute(ves_ctx* c, int nv, const double* X, double* Xout, int* fl
     return VES_ERR_WORKSPACE;
   }
   if (nv <= 0) return VES_OK;
+  if (!ves_fft_size_ok(M) || !ves_fft_size_ok(N)) {
+    ves_record_error(VES_ERR_SHAPE, "redistribute: N = %d must be a power of two", N);
+    return VES_ERR_SHAPE;
+  }
   const int threads = pow2_threads(N);
   ves_count_launch(3);
   jac_dev_kernel<<<nv, threads, (size_t)(4 * N + threads) * sizeof(double), s>>>(N, c->d1N, X, dev);
   dev_rowsum_kernel<<<nchunk, 128, 0, s>>>(nv, N, dev, partial);
   spread_kernel<<<1, 256, 0, s>>>(nchunk, N, partial, spread);
-  const size_t sh = (size_t)(3 * N + 2 * M + M + 3 * N + threads) * sizeof(double);
+  const size_t sh = (size_t)(6 * N + 5 * M + threads) * sizeof(double);
   if (sh > 32 * 1024) {
     int rc = ves_cuda_status(cudaFuncSetAttribute(redistribute_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                   (int)sh),

@@ -40,27 +40,46 @@
 
 namespace tcnet {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 256;  // two warp groups of four warps
+constexpr int kGroupThreads = 128;
+constexpr int kMinSmem = 117 * 1024;
 constexpr int kOffsets = 11;  // input shifts of a conv pair: -6..6 without +-5
 __host__ __device__ constexpr int shift_of(int oi) { return oi < 2 ? -6 + 2 * oi : (oi < 9 ? oi - 5 : 2 * oi - 14); }
 
 __host__ __device__ constexpr int rup(int a, int b) { return (a + b - 1) / b * b; }
 
 // Geometry of one block, shared by host packing and kernels (bytes unless noted).
+// Shared memory holds one weight image and, per warp group, its own
+// activation arrays (each warp group runs its own (group, vesicle) items).
 struct Geo {
-  int cin, c1, c2, cmix, residual, npass, L;
+  int cin, c1, c2, cmix, residual, npass, L, lgL;
   int n1, d;             // conv-pair output channels
   int kcin, kc1, kcd;    // 8-channel K chunks of the three GEMM inputs (even)
   // down image: W1 [11][kcin][n1][16B], W2 [11][kc1][d][16B], consts [6][128] f32
   int dw1, dw2, dcst, dsize;
-  // down smem: image, xs [2][kcin][L/2+6][16B], as [2][kc1][L/4+6][16B], stage [kcd][L/4][16B], tail
-  int dxs, das, dstage, dsmem;
-  // up image: D1 [2][5][kcd][d][16B], D2 same, M [3][kcd][cmix][16B], consts [7][128] f32
-  int uw1, uw2, uwm, ucst, usize;
-  // up smem: image, bs [kcd][L/4+4][16B], cs [kcd][L/2+4][16B], ds [kcd][L+2][16B], tail
-  int ubs, ucs, uds, uxr, usmem;  // uxr: FP32 residual x[0:cmix][L] of the current item
+  // down arrays of warp group 0 (group 1 at + dgrp): xs [2][kcin][L/2+6][16B],
+  // as [2][kc1][L/4+6][16B], stage [kcd][L/4][16B], xf [cin][L] f32 (the
+  // block input as it arrives by bulk copy); then a tail
+  int dxs, das, dstage, dxf, dgrp, dsmem;
+  // up image: D1, D2 (transposed convs), M [3][kcd][cmix][16B], consts [7][128] f32.
+  // D layout: umerge = 1: [5][kcd][2*kcd*8][16B], both output parities in one
+  // operand of N = 2*kcd*8 rows (parity r at row r*kcd*8); umerge = 0 (when the
+  // padded image does not fit): [2][5][kcd][d][16B]
+  int umerge, uw1, uw2, uwm, ucst, usize;
+  // up arrays of warp group 0 (group 1 at + ugrp): bs [kcd][L/4+4][16B],
+  // cs [kcd][L/2+4][16B], ds [kcd][L+2][16B]; then a tail
+  int ubs, ucs, uds, ugrp, usmem;
   int mid_bytes;         // down -> up intermediate per (vesicle, group): [kcd][L/4][16B]
 };
+
+constexpr int kMaxSmem = 227 * 1024 - 256;  // dynamic shared memory available next to the static part
+
+// byte offset of row o of K chunk kc of tap u, output parity r, in transposed conv `layer`
+__host__ __device__ inline int up_w_off(const Geo& g, int layer, int r, int u, int kc, int o) {
+  const int base = layer ? g.uw2 : g.uw1;
+  if (g.umerge) return base + ((u * g.kcd + kc) * 2 * g.kcd * 8 + r * g.kcd * 8 + o) * 16;
+  return base + (((r * 5 + u) * g.kcd + kc) * g.d + o) * 16;
+}
 
 inline Geo make_geo(const ves_net_block& b, int L) {
   Geo g;
@@ -71,6 +90,8 @@ inline Geo make_geo(const ves_net_block& b, int L) {
   g.residual = b.residual;
   g.npass = b.npass;
   g.L = L;
+  g.lgL = 0;
+  while ((1 << g.lgL) < L) ++g.lgL;
   g.n1 = 2 * b.c1;
   g.d = 2 * b.c2;
   g.kcin = rup(b.cin, 16) / 8;
@@ -90,26 +111,30 @@ inline Geo make_geo(const ves_net_block& b, int L) {
   o += 2 * g.kc1 * (L / 4 + 6) * 16;
   g.dstage = o;
   o += g.kcd * (L / 4) * 16;
-  g.dsmem = o + 128 * 16;
-  o = 0;
-  g.uw1 = o;
-  o += 10 * g.kcd * g.d * 16;
-  g.uw2 = o;
-  o += 10 * g.kcd * g.d * 16;
-  g.uwm = o;
-  o += 3 * g.kcd * g.cmix * 16;
-  g.ucst = o;
-  o += 7 * 128 * 4;
-  g.usize = o;
-  g.ubs = o;
-  o += g.kcd * (L / 4 + 4) * 16;
-  g.ucs = o;
-  o += g.kcd * (L / 2 + 4) * 16;
-  g.uds = o;
-  o += g.kcd * (L + 2) * 16;
-  g.uxr = o + 128 * 16;  // after the tail that A-operand reads may run into
-  o = g.uxr + rup(b.cmix * L * 4, 16);
-  g.usmem = o;
+  g.dxf = o;
+  o += rup(g.cin * L * 4, 16);
+  g.dgrp = o - g.dxs;
+  g.dsmem = g.dxs + 2 * g.dgrp + 128 * 16;
+  g.ugrp = g.kcd * (L / 4 + 4) * 16 + g.kcd * (L / 2 + 4) * 16 + g.kcd * (L + 2) * 16;
+  for (g.umerge = 1; g.umerge >= 0; --g.umerge) {
+    o = 0;
+    const int dbytes = g.umerge ? 5 * g.kcd * 2 * g.kcd * 8 * 16 : 10 * g.kcd * g.d * 16;
+    g.uw1 = o;
+    o += dbytes;
+    g.uw2 = o;
+    o += dbytes;
+    g.uwm = o;
+    o += 3 * g.kcd * g.cmix * 16;
+    g.ucst = o;
+    o += 7 * 128 * 4;
+    g.usize = o;
+    g.usmem = g.usize + 2 * g.ugrp + 128 * 16;
+    if (g.usmem <= kMaxSmem) break;
+  }
+  if (g.umerge < 0) g.umerge = 0;
+  g.ubs = g.usize;
+  g.ucs = g.ubs + g.kcd * (L / 4 + 4) * 16;
+  g.uds = g.ucs + g.kcd * (L / 2 + 4) * 16;
   g.mid_bytes = g.kcd * (L / 4) * 16;
   return g;
 }
@@ -125,10 +150,6 @@ struct KArgs {
   VesDeviceStatus* st;
 };
 
-__device__ __forceinline__ uint16_t f2bf(float f) {
-  return __bfloat16_as_ushort(__float2bfloat16_rn(f));
-}
-
 __device__ __forceinline__ void copy16(unsigned char* dst, const unsigned char* src, int bytes) {
   const uint4* s = reinterpret_cast<const uint4*>(src);
   uint4* d = reinterpret_cast<uint4*>(dst);
@@ -140,12 +161,38 @@ __device__ __forceinline__ void zero16(unsigned char* dst, int bytes) {
   for (int i = threadIdx.x; i < bytes / 16; i += blockDim.x) d[i] = z;
 }
 
-// all writes to shared memory so far -> visible to the tensor core; CTA barrier
-__device__ __forceinline__ void sync_for_mma() {
+// barrier of one warp group (named barrier 1 + group, 128 threads)
+__device__ __forceinline__ void group_sync(int wg) {
+  asm volatile("bar.sync %0, %1;" ::"r"(1 + wg), "r"(kGroupThreads) : "memory");
+}
+// all of the group's writes to shared memory so far -> visible to the tensor core
+__device__ __forceinline__ void group_sync_for_mma(int wg) {
   tc_fence_async_smem();
   tc_fence_before_sync();
-  __syncthreads();
+  group_sync(wg);
   tc_fence_after_sync();
+}
+__device__ __forceinline__ void copy16_g(unsigned char* dst, const unsigned char* src, int bytes, int t) {
+  const uint4* s = reinterpret_cast<const uint4*>(src);
+  uint4* d = reinterpret_cast<uint4*>(dst);
+  for (int i = t; i < bytes / 16; i += kGroupThreads) d[i] = s[i];
+}
+// Bounded waits of one warp group on an mbarrier; true when the phase
+// completed (the answer is uniform across the group).  group_wait: every
+// thread polls (data landed by bulk copy, normally already there);
+// group_wait_one: thread 0 of the group polls and the others sleep in the
+// group barrier (MMA completion, hundreds of cycles away).
+__device__ __forceinline__ bool group_wait(uint64_t* bar, unsigned phase, VesDeviceStatus* st, int site, int wg,
+                                           int* flag) {
+  if (!tc_mbar_wait(bar, phase, st, site)) atomicExch(flag, 1);
+  group_sync(wg);
+  return *(volatile int*)flag == 0;
+}
+__device__ __forceinline__ bool group_wait_one(uint64_t* bar, unsigned phase, VesDeviceStatus* st, int site, int wg,
+                                               int gt, int* flag) {
+  if (gt == 0 && !tc_mbar_wait(bar, phase, st, site)) atomicExch(flag, 1);
+  group_sync(wg);
+  return *(volatile int*)flag == 0;
 }
 
 struct Range {
@@ -164,6 +211,12 @@ __device__ __forceinline__ Range my_items(long long items) {
 // channels at a time, which is one 16-byte row of the next layer's K-major
 // operand.
 
+// two FP32 values -> one 32-bit word of two BF16 (round to nearest even), low half first
+__device__ __forceinline__ uint32_t pack_bf2(float lo, float hi) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&h);
+}
+
 // 8 channels [8kc, 8kc+8) of this thread's position: relu(v + b) * s + t, 0 beyond nreal
 __device__ __forceinline__ uint4 act8(const float* v, const float* cst, int kc, int nreal, int ob, int os, int ot) {
   float b[8], sc[8], sh[8];
@@ -173,327 +226,420 @@ __device__ __forceinline__ uint4 act8(const float* v, const float* cst, int kc, 
   *reinterpret_cast<float4*>(sc + 4) = *reinterpret_cast<const float4*>(cst + os + 8 * kc + 4);
   *reinterpret_cast<float4*>(sh) = *reinterpret_cast<const float4*>(cst + ot + 8 * kc);
   *reinterpret_cast<float4*>(sh + 4) = *reinterpret_cast<const float4*>(cst + ot + 8 * kc + 4);
-  uint32_t w[4];
+  float y[8];
+  if (8 * kc + 8 <= nreal) {  // uniform across the warp
 #pragma unroll
-  for (int e = 0; e < 8; e += 2) {
-    const int c0 = 8 * kc + e;
-    const float y0 = c0 < nreal ? fmaf(fmaxf(v[e] + b[e], 0.f), sc[e], sh[e]) : 0.f;
-    const float y1 = c0 + 1 < nreal ? fmaf(fmaxf(v[e + 1] + b[e + 1], 0.f), sc[e + 1], sh[e + 1]) : 0.f;
-    w[e >> 1] = (uint32_t)f2bf(y0) | ((uint32_t)f2bf(y1) << 16);
+    for (int e = 0; e < 8; ++e) y[e] = fmaf(fmaxf(v[e] + b[e], 0.f), sc[e], sh[e]);
+  } else {  // the chunk that holds the padding channels (TMEM columns past nreal are not defined)
+#pragma unroll
+    for (int e = 0; e < 8; ++e) y[e] = 8 * kc + e < nreal ? fmaf(fmaxf(v[e] + b[e], 0.f), sc[e], sh[e]) : 0.f;
   }
-  return make_uint4(w[0], w[1], w[2], w[3]);
+  return make_uint4(pack_bf2(y[0], y[1]), pack_bf2(y[2], y[3]), pack_bf2(y[4], y[5]), pack_bf2(y[6], y[7]));
 }
 
 // ---------------------------------------------------------------------------
+// Segments: the CTA's contiguous item range split where the channel group
+// changes; the weight image is reloaded (whole CTA) at each segment start and
+// the two warp groups take the segment's items alternately.
+struct Seg {
+  long long lo, hi;
+  int grp;
+};
+__device__ __forceinline__ Seg next_seg(long long lo, long long hi, int nv) {
+  const int grp = (int)(lo / nv);
+  const long long end = (long long)(grp + 1) * nv;
+  return {lo, end < hi ? end : hi, grp};
+}
+
 __global__ void __launch_bounds__(kThreads, 1) down_kernel(KArgs a) {
   extern __shared__ __align__(128) unsigned char sm[];
-  __shared__ uint64_t bar;
+  __shared__ uint64_t bar[2], xbar[2];  // per warp group: MMA completion, input arrival
   __shared__ uint32_t tbase;
+  __shared__ int fail[2];
   const Geo& g = a.g;
   const int L = g.L, L2 = L / 2, L4 = L / 4;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int qd = warp & 3, hf = warp >> 2;  // lane quarter (positions), column half
+  const int wg = tid / kGroupThreads, gt = tid % kGroupThreads;  // warp group, thread within it
+  const int qd = warp & 3;                                       // TMEM lane quarter = position block
   const Range rg = my_items(a.items);
   if (rg.lo >= rg.hi) return;
-  const uint32_t ncols = 128;
+  const uint32_t ncols = 512;  // 256 columns per warp group (one CTA per SM)
   if (tid == 0) {
-    tc_mbar_init(&bar, 1);
+    for (int k = 0; k < 2; ++k) {
+      tc_mbar_init(&bar[k], 1);
+      tc_mbar_init(&xbar[k], 1);
+    }
     tc_mbar_fence_init();
+    fail[0] = fail[1] = 0;
   }
   if (warp == 0) tc_tmem_alloc(&tbase, ncols);
   zero16(sm + g.dxs, g.dsmem - g.dxs);  // K padding of the activation arrays stays zero
+  tc_fence_async_smem();
   tc_fence_before_sync();
   __syncthreads();
   tc_fence_after_sync();
-  const uint32_t t0 = tbase;
   const int N1 = g.kc1 * 8, N2 = g.kcd * 8;
-  const uint32_t d1 = t0, d2 = t0 + N1;
+  const uint32_t tcol = tbase + 256 * wg;
+  const uint32_t d1 = tcol, d2 = tcol + N1;
   const uint32_t sbase = tc_smem_u32(sm);
+  const int goff = wg * g.dgrp;
   const float* cst = reinterpret_cast<const float*>(sm + g.dcst);
-  unsigned phase = 0;
-  bool failed = false;
-  int cur_g = -1;
   const int P1 = L2 + 6, P2 = L4 + 6;
-  uint4* xs = reinterpret_cast<uint4*>(sm + g.dxs);
-  uint4* as = reinterpret_cast<uint4*>(sm + g.das);
-  uint4* stage = reinterpret_cast<uint4*>(sm + g.dstage);
-  // input x[v][grp*cin + c][pos] -> parity-split BF16 rows with circular halos;
-  // one thread per (position, 8-channel chunk)
-  auto load_x = [&](long long item) {
-    const int grp = (int)(item / a.nv);
-    const long long v = item % a.nv;
-    const float* __restrict__ xin = a.x + ((long long)v * a.G + grp) * (long long)g.cin * L;
-    for (int i = tid; i < g.kcin * L; i += blockDim.x) {
-      const int kc = i / L, pos = i - kc * L;
-      float y[8];
+  uint4* xs = reinterpret_cast<uint4*>(sm + g.dxs + goff);
+  uint4* as = reinterpret_cast<uint4*>(sm + g.das + goff);
+  uint4* stage = reinterpret_cast<uint4*>(sm + g.dstage + goff);
+  float* xf = reinterpret_cast<float*>(sm + g.dxf + goff);
+  const uint32_t xbytes = (uint32_t)(g.cin * L * 4);
+  unsigned phase = 0, xphase = 0;
+  bool xpend = false;  // a bulk copy into xf is in flight
+  // block input x[v][grp*cin + c][pos] (cin*L contiguous floats) -> xf
+  auto fetch_x = [&](long long item) {
+    if (gt == 0) {
+      const int grp = (int)(item / a.nv);
+      const long long v = item % a.nv;
+      tc_expect_tx(&xbar[wg], xbytes);
+      tc_bulk_g2s(xf, a.x + ((long long)v * a.G + grp) * (long long)g.cin * L, xbytes, &xbar[wg]);
+    }
+    xpend = true;
+  };
+  // xf -> parity-split BF16 rows with circular halos of 3; one thread per
+  // (8-channel chunk, position pair 2m, 2m+1)
+  auto convert_x = [&]() {
+    const int lg2 = g.lgL - 1;
+    for (int i = gt; i < g.kcin * L2; i += kGroupThreads) {
+      const int kc = i >> lg2, m = i & (L2 - 1);
+      float2 y[8];
 #pragma unroll
-      for (int e = 0; e < 8; ++e) y[e] = (8 * kc + e < g.cin) ? __ldg(xin + (size_t)(8 * kc + e) * L + pos) : 0.f;
-      uint32_t w[4];
-#pragma unroll
-      for (int e = 0; e < 8; e += 2) w[e >> 1] = (uint32_t)f2bf(y[e]) | ((uint32_t)f2bf(y[e + 1]) << 16);
-      const uint4 val = make_uint4(w[0], w[1], w[2], w[3]);
-      const int par = pos & 1, q = pos >> 1;
-      uint4* base = xs + (size_t)(par * g.kcin + kc) * P1;
-      base[q + 3] = val;
-      if (q >= L2 - 3) base[q + 3 - L2] = val;
-      if (q < 3) base[q + 3 + L2] = val;
+      for (int e = 0; e < 8; ++e)
+        y[e] = (8 * kc + e < g.cin) ? *reinterpret_cast<const float2*>(xf + (8 * kc + e) * L + 2 * m)
+                                    : make_float2(0.f, 0.f);
+      const uint4 v0 = make_uint4(pack_bf2(y[0].x, y[1].x), pack_bf2(y[2].x, y[3].x), pack_bf2(y[4].x, y[5].x),
+                                  pack_bf2(y[6].x, y[7].x));
+      const uint4 v1 = make_uint4(pack_bf2(y[0].y, y[1].y), pack_bf2(y[2].y, y[3].y), pack_bf2(y[4].y, y[5].y),
+                                  pack_bf2(y[6].y, y[7].y));
+      uint4* b0 = xs + (size_t)kc * P1;
+      uint4* b1 = xs + (size_t)(g.kcin + kc) * P1;
+      b0[m + 3] = v0;
+      b1[m + 3] = v1;
+      if (m >= L2 - 3) {
+        b0[m + 3 - L2] = v0;
+        b1[m + 3 - L2] = v1;
+      }
+      if (m < 3) {
+        b0[m + 3 + L2] = v0;
+        b1[m + 3 + L2] = v1;
+      }
     }
   };
-  load_x(rg.lo);
-  for (long long it = rg.lo; it < rg.hi && !failed; ++it) {
-    const int grp = (int)(it / a.nv);
-    const long long v = it % a.nv;
-    if (grp != cur_g) {  // weights and constants of this group
-      __syncthreads();
-      copy16(sm, a.img + (size_t)grp * g.dsize, g.dsize);
-      cur_g = grp;
-    }
-    sync_for_mma();
-    // conv pair 1: D1[p][o], p < L/2 on the lanes, o < n1 in the columns
-    if (tid == 0) {
-      const uint32_t idesc = tc_idesc_bf16(128, N1);
-      const uint32_t lboA = P1 * 16, lboB = g.n1 * 16;
-      for (int oi = 0; oi < kOffsets; ++oi) {
-        const int s = shift_of(oi);
-        const int par = s & 1, row = 3 + (s >> 1);
-        for (int j = 0; j < g.kcin / 2; ++j) {
-          const uint64_t ad = tc_desc(sbase + g.dxs + (par * g.kcin + 2 * j) * lboA + row * 16, lboA, 128);
-          const uint64_t bd = tc_desc(sbase + g.dw1 + (oi * g.kcin + 2 * j) * lboB, lboB, 128);
-          tc_mma_bf16(d1, ad, bd, idesc, (oi | j) ? 1u : 0u);
-        }
-      }
-      tc_commit(&bar);
-    }
-    if (__syncthreads_or(!tc_mbar_wait(&bar, phase, a.st, 21))) {
-      failed = true;
-      break;
-    }
-    phase ^= 1;
-    tc_fence_after_sync();
-    if (32 * qd < L2 && 4 * hf < g.kc1) {  // half hf: channel chunks [4hf, 4hf+4)
-      const int p = 32 * qd + lane;
-      const int par = p & 1, q = p >> 1;
-      float vv[32];
-      tc_ld32(d1 + ((uint32_t)(32 * qd) << 16) + 32 * hf, vv);
-      for (int k = 0; k < 4 && 4 * hf + k < g.kc1; ++k) {
-        const int kc = 4 * hf + k;
-        const uint4 val = act8(vv + 8 * k, cst, kc, g.n1, 0, 128, 256);
-        uint4* base = as + (size_t)(par * g.kc1 + kc) * P2;
-        base[q + 3] = val;
-        if (q >= L4 - 3) base[q + 3 - L4] = val;
-        if (q < 3) base[q + 3 + L4] = val;
-      }
-    }
-    sync_for_mma();
-    // conv pair 2: D2[p][o], p < L/4, o < d
-    if (tid == 0) {
-      const uint32_t idesc = tc_idesc_bf16(128, N2);
-      const uint32_t lboA = P2 * 16, lboB = g.d * 16;
-      for (int oi = 0; oi < kOffsets; ++oi) {
-        const int s = shift_of(oi);
-        const int par = s & 1, row = 3 + (s >> 1);
-        for (int j = 0; j < g.kc1 / 2; ++j) {
-          const uint64_t ad = tc_desc(sbase + g.das + (par * g.kc1 + 2 * j) * lboA + row * 16, lboA, 128);
-          const uint64_t bd = tc_desc(sbase + g.dw2 + (oi * g.kc1 + 2 * j) * lboB, lboB, 128);
-          tc_mma_bf16(d2, ad, bd, idesc, (oi | j) ? 1u : 0u);
-        }
-      }
-      tc_commit(&bar);
-    }
-    // xs is free once conv pair 1 has completed: stage the next item's input
-    if (it + 1 < rg.hi) load_x(it + 1);
-    if (__syncthreads_or(!tc_mbar_wait(&bar, phase, a.st, 22))) {
-      failed = true;
-      break;
-    }
-    phase ^= 1;
-    tc_fence_after_sync();
-    if (32 * qd < L4 && 4 * hf < g.kcd) {
-      const int p = 32 * qd + lane;
-      float vv[32];
-      tc_ld32(d2 + ((uint32_t)(32 * qd) << 16) + 32 * hf, vv);
-      for (int k = 0; k < 4 && 4 * hf + k < g.kcd; ++k) {
-        const int kc = 4 * hf + k;
-        stage[(size_t)kc * L4 + p] = act8(vv + 8 * k, cst, kc, g.d, 384, 512, 640);
-      }
-    }
+  bool failed = false, stuck = false;  // stuck: this warp group's own MMA wait timed out
+  for (long long lo = rg.lo; lo < rg.hi && !failed;) {
+    const Seg sg = next_seg(lo, rg.hi, a.nv);
     __syncthreads();
-    copy16(a.mid + ((size_t)v * a.G + grp) * g.mid_bytes, sm + g.dstage, g.mid_bytes);
+    copy16(sm, a.img + (size_t)sg.grp * g.dsize, g.dsize);  // whole CTA
+    tc_fence_async_smem();  // weights (and the zeroed padding) -> tensor core, for both groups
+    __syncthreads();
+    if (sg.lo + wg < sg.hi) fetch_x(sg.lo + wg);
+    for (long long it = sg.lo + wg; it < sg.hi; it += 2) {
+      const long long v = it % a.nv;
+      if (!group_wait(&xbar[wg], xphase, a.st, 20, wg, &fail[wg])) {
+        failed = true;
+        break;
+      }
+      xphase ^= 1;
+      xpend = false;
+      convert_x();
+      group_sync_for_mma(wg);  // xs complete; xf fully read
+      if (it + 2 < sg.hi) fetch_x(it + 2);
+      // conv pair 1: D1[p][o], p < L/2 on the lanes, o < n1 in the columns
+      if (gt == 0) {
+        const uint32_t idesc = tc_idesc_bf16(128, N1);
+        const uint32_t lboA = P1 * 16, lboB = g.n1 * 16;
+        for (int oi = 0; oi < kOffsets; ++oi) {
+          const int s = shift_of(oi);
+          const int par = s & 1, row = 3 + (s >> 1);
+          for (int j = 0; j < g.kcin / 2; ++j) {
+            const uint64_t ad = tc_desc(sbase + g.dxs + goff + (par * g.kcin + 2 * j) * lboA + row * 16, lboA, 128);
+            const uint64_t bd = tc_desc(sbase + g.dw1 + (oi * g.kcin + 2 * j) * lboB, lboB, 128);
+            tc_mma_bf16(d1, ad, bd, idesc, (oi | j) ? 1u : 0u);
+          }
+        }
+        tc_commit(&bar[wg]);
+      }
+      if (!group_wait_one(&bar[wg], phase, a.st, 21, wg, gt, &fail[wg])) {
+        failed = stuck = true;
+        break;
+      }
+      phase ^= 1;
+      tc_fence_after_sync();
+      if (32 * qd < L2) {
+        const int p = 32 * qd + lane;
+        const int par = p & 1, q = p >> 1;
+        for (int k0 = 0; k0 < g.kc1; k0 += 4) {
+          float vv[32];
+          tc_ld32(d1 + ((uint32_t)(32 * qd) << 16) + 8 * k0, vv);
+          for (int k = 0; k < 4 && k0 + k < g.kc1; ++k) {
+            const int kc = k0 + k;
+            const uint4 val = act8(vv + 8 * k, cst, kc, g.n1, 0, 128, 256);
+            uint4* base = as + (size_t)(par * g.kc1 + kc) * P2;
+            base[q + 3] = val;
+            if (q >= L4 - 3) base[q + 3 - L4] = val;
+            if (q < 3) base[q + 3 + L4] = val;
+          }
+        }
+      }
+      group_sync_for_mma(wg);
+      // conv pair 2: D2[p][o], p < L/4, o < d
+      if (gt == 0) {
+        const uint32_t idesc = tc_idesc_bf16(128, N2);
+        const uint32_t lboA = P2 * 16, lboB = g.d * 16;
+        for (int oi = 0; oi < kOffsets; ++oi) {
+          const int s = shift_of(oi);
+          const int par = s & 1, row = 3 + (s >> 1);
+          for (int j = 0; j < g.kc1 / 2; ++j) {
+            const uint64_t ad = tc_desc(sbase + g.das + goff + (par * g.kc1 + 2 * j) * lboA + row * 16, lboA, 128);
+            const uint64_t bd = tc_desc(sbase + g.dw2 + (oi * g.kc1 + 2 * j) * lboB, lboB, 128);
+            tc_mma_bf16(d2, ad, bd, idesc, (oi | j) ? 1u : 0u);
+          }
+        }
+        tc_commit(&bar[wg]);
+      }
+      if (!group_wait_one(&bar[wg], phase, a.st, 22, wg, gt, &fail[wg])) {
+        failed = stuck = true;
+        break;
+      }
+      phase ^= 1;
+      tc_fence_after_sync();
+      if (32 * qd < L4) {
+        const int p = 32 * qd + lane;
+        for (int k0 = 0; k0 < g.kcd; k0 += 4) {
+          float vv[32];
+          tc_ld32(d2 + ((uint32_t)(32 * qd) << 16) + 8 * k0, vv);
+          for (int k = 0; k < 4 && k0 + k < g.kcd; ++k)
+            stage[(size_t)(k0 + k) * L4 + p] = act8(vv + 8 * k, cst, k0 + k, g.d, 384, 512, 640);
+        }
+      }
+      tc_fence_before_sync();
+      group_sync(wg);
+      copy16_g(a.mid + ((size_t)v * a.G + sg.grp) * g.mid_bytes, reinterpret_cast<unsigned char*>(stage), g.mid_bytes,
+               gt);
+    }
+    lo = sg.hi;
+    failed = __syncthreads_or(failed ? 1 : 0) != 0;  // every thread takes part
   }
-  if (failed) tc_mbar_wait(&bar, phase, nullptr, 0);  // bounded: let outstanding MMAs drain
+  // bounded drains: this group's MMAs and bulk copies still in flight after a failure
+  if (stuck) tc_mbar_wait(&bar[wg], phase, nullptr, 0);
+  if (xpend) tc_mbar_wait(&xbar[wg], xphase, nullptr, 0);
   tc_fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc_tmem_dealloc(t0, ncols);
+  if (warp == 0) tc_tmem_dealloc(tbase, ncols);
 }
 
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
   extern __shared__ __align__(128) unsigned char sm[];
-  __shared__ uint64_t bar;
+  __shared__ uint64_t bar[2], mbar[2];  // per warp group: MMA completion, intermediate arrival
   __shared__ uint32_t tbase;
+  __shared__ int fail[2];
   const Geo& g = a.g;
   const int L = g.L, L2 = L / 2, L4 = L / 4;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int qd = warp & 3, hf = warp >> 2;
+  const int wg = tid / kGroupThreads, gt = tid % kGroupThreads;
+  const int qd = warp & 3;
   const Range rg = my_items(a.items);
   if (rg.lo >= rg.hi) return;
-  const uint32_t ncols = 128;
+  const uint32_t ncols = 512;
   if (tid == 0) {
-    tc_mbar_init(&bar, 1);
+    for (int k = 0; k < 2; ++k) {
+      tc_mbar_init(&bar[k], 1);
+      tc_mbar_init(&mbar[k], 1);
+    }
     tc_mbar_fence_init();
+    fail[0] = fail[1] = 0;
   }
   if (warp == 0) tc_tmem_alloc(&tbase, ncols);
   zero16(sm + g.ubs, g.usmem - g.ubs);  // halos and K padding stay zero
+  tc_fence_async_smem();
   tc_fence_before_sync();
   __syncthreads();
   tc_fence_after_sync();
-  const uint32_t dt = tbase;
+  const uint32_t dt = tbase + 256 * wg;
   const uint32_t sbase = tc_smem_u32(sm);
+  const int goff = wg * g.ugrp;
   const float* cst = reinterpret_cast<const float*>(sm + g.ucst);
   const int PB = L4 + 4, PC = L2 + 4, PD = L + 2;
   const int Nd = g.kcd * 8, Nm = rup(g.cmix, 16);
   const int cout = g.cmix + g.npass;
-  uint4* bs = reinterpret_cast<uint4*>(sm + g.ubs);
-  uint4* cs = reinterpret_cast<uint4*>(sm + g.ucs);
-  uint4* ds = reinterpret_cast<uint4*>(sm + g.uds);
-  float* xres = reinterpret_cast<float*>(sm + g.uxr);
-  // intermediate [kcd][L/4][16B] of an item -> bs rows 2 .. L/4+1
-  auto load_mid = [&](long long item) {
-    const int grp = (int)(item / a.nv);
-    const long long v = item % a.nv;
-    const uint4* __restrict__ src = reinterpret_cast<const uint4*>(a.mid + ((size_t)v * a.G + grp) * g.mid_bytes);
-    for (int i = tid; i < g.kcd * L4; i += blockDim.x) {
-      const int kc = i / L4, q = i - kc * L4;
-      bs[kc * PB + q + 2] = __ldg(src + i);
+  const int nh = L / 128;      // 128-position halves of the mix
+  const int mcol = 2 * Nd;     // first TMEM column of the mix accumulators
+  uint4* bs = reinterpret_cast<uint4*>(sm + g.ubs + goff);
+  uint4* cs = reinterpret_cast<uint4*>(sm + g.ucs + goff);
+  uint4* ds = reinterpret_cast<uint4*>(sm + g.uds + goff);
+  unsigned phase = 0, mphase = 0;
+  bool mpend = false;  // bulk copies into bs in flight
+  // intermediate [kcd][L/4][16B] of an item -> bs rows 2 .. L/4+1 of each chunk
+  auto fetch_mid = [&](long long item) {
+    if (gt == 0) {
+      const int grp = (int)(item / a.nv);
+      const long long v = item % a.nv;
+      const unsigned char* src = a.mid + ((size_t)v * a.G + grp) * g.mid_bytes;
+      tc_expect_tx(&mbar[wg], (uint32_t)g.mid_bytes);
+      for (int kc = 0; kc < g.kcd; ++kc) tc_bulk_g2s(bs + kc * PB + 2, src + kc * L4 * 16, L4 * 16, &mbar[wg]);
     }
+    mpend = true;
   };
-  unsigned phase = 0;
-  bool failed = false;
-  int cur_g = -1;
-  load_mid(rg.lo);
-  for (long long it = rg.lo; it < rg.hi && !failed; ++it) {
-    const int grp = (int)(it / a.nv);
-    const long long v = it % a.nv;
-    if (grp != cur_g) {
-      __syncthreads();
-      copy16(sm, a.img + (size_t)grp * g.usize, g.usize);
-      cur_g = grp;
-    }
-    const float* __restrict__ xin = a.x + ((long long)v * a.G + grp) * (long long)g.cin * L;
-    float* __restrict__ op = a.out + ((long long)v * a.G + grp) * (long long)cout * L;
-    sync_for_mma();
-    // transposed conv 1: parity r in TMEM columns [r*Nd, (r+1)*Nd), rows q < L/4
-    if (tid == 0) {
+  // One transposed conv over npos input rows: output parity r in TMEM columns
+  // [r*Nd, (r+1)*Nd).  When both parities fit in 128 lanes (2*npos <= 128)
+  // parity r's operand starts r*npos rows early, so its valid rows land on
+  // lanes [r*npos, (r+1)*npos) and twice as many warps share the epilogue;
+  // otherwise both parities share one MMA of N = 2*Nd (merged image) or run
+  // as two MMAs on the same lanes.
+  auto deconv_mma = [&](int layer, uint32_t a_off, uint32_t lboA, int npos) {
+    const bool msplit = 2 * npos <= 128;
+    if (g.umerge && !msplit) {
+      const uint32_t idesc = tc_idesc_bf16(128, 2 * Nd);
+      const uint32_t lboB = 2 * Nd * 16;
+      for (int u = 0; u < 5; ++u)
+        for (int j = 0; j < g.kcd / 2; ++j) {
+          const uint64_t ad = tc_desc(sbase + a_off + 2 * j * lboA + (4 - u) * 16, lboA, 128);
+          const uint64_t bd = tc_desc(sbase + up_w_off(g, layer, 0, u, 2 * j, 0), lboB, 128);
+          tc_mma_bf16(dt, ad, bd, idesc, (u | j) ? 1u : 0u);
+        }
+    } else {
       const uint32_t idesc = tc_idesc_bf16(128, Nd);
-      const uint32_t lboA = PB * 16, lboB = g.d * 16;
-      for (int r = 0; r < 2; ++r)
+      const uint32_t lboB = (g.umerge ? 2 * Nd : g.d) * 16;
+      for (int r = 0; r < 2; ++r) {
+        const int lift = msplit ? r * npos * 16 : 0;
         for (int u = 0; u < 5; ++u)
           for (int j = 0; j < g.kcd / 2; ++j) {
-            const uint64_t ad = tc_desc(sbase + g.ubs + 2 * j * lboA + (4 - u) * 16, lboA, 128);
-            const uint64_t bd = tc_desc(sbase + g.uw1 + ((r * 5 + u) * g.kcd + 2 * j) * lboB, lboB, 128);
+            const uint64_t ad = tc_desc(sbase + a_off + 2 * j * lboA + (4 - u) * 16 - lift, lboA, 128);
+            const uint64_t bd = tc_desc(sbase + up_w_off(g, layer, r, u, 2 * j, 0), lboB, 128);
             tc_mma_bf16(dt + r * Nd, ad, bd, idesc, (u | j) ? 1u : 0u);
           }
-      tc_commit(&bar);
+      }
     }
-    // while the tensor core runs: residual channels to shared memory, pass-through channels
-    if (g.residual) {
-      const float4* __restrict__ src = reinterpret_cast<const float4*>(xin);
-      float4* dst = reinterpret_cast<float4*>(xres);
-      for (int i = tid; i < g.cmix * L / 4; i += blockDim.x) dst[i] = __ldg(src + i);
-    }
-    {
-      const float4* __restrict__ src = reinterpret_cast<const float4*>(xin + (size_t)(g.cin - g.npass) * L);
-      float4* dst = reinterpret_cast<float4*>(op + (size_t)g.cmix * L);
-      for (int i = tid; i < g.npass * L / 4; i += blockDim.x) dst[i] = __ldg(src + i);
-    }
-    if (__syncthreads_or(!tc_mbar_wait(&bar, phase, a.st, 23))) {
-      failed = true;
-      break;
-    }
-    phase ^= 1;
-    tc_fence_after_sync();
-    if (32 * qd < L4) {  // half hf = output parity r
-      const int q = 32 * qd + lane, r = hf;
+    tc_commit(&bar[wg]);
+  };
+  // epilogue of a transposed conv: out(8 channels, position 2q + r) for this
+  // thread's lane; `dst` rows are 2q + r + row0, chunk stride `pitch`
+  auto deconv_epi = [&](int npos, uint4* dst, int pitch, int row0, int ob, int os, int ot) {
+    const bool msplit = 2 * npos <= 128;
+    const int lane0 = 32 * qd;
+    for (int r = 0; r < 2; ++r) {
+      int q;
+      if (msplit) {
+        if (lane0 < r * npos || lane0 >= (r + 1) * npos) continue;  // uniform per warp
+        q = lane0 + lane - r * npos;
+      } else {
+        if (lane0 >= npos) continue;
+        q = lane0 + lane;
+      }
       for (int k0 = 0; k0 < g.kcd; k0 += 4) {
         float vv[32];
-        tc_ld32(dt + ((uint32_t)(32 * qd) << 16) + r * Nd + 8 * k0, vv);
+        tc_ld32(dt + ((uint32_t)lane0 << 16) + r * Nd + 8 * k0, vv);
         for (int k = 0; k < 4 && k0 + k < g.kcd; ++k)
-          cs[(size_t)(k0 + k) * PC + 2 * q + r + 2] = act8(vv + 8 * k, cst, k0 + k, g.d, 0, 128, 256);
+          dst[(size_t)(k0 + k) * pitch + 2 * q + r + row0] = act8(vv + 8 * k, cst, k0 + k, g.d, ob, os, ot);
       }
     }
-    sync_for_mma();
-    // transposed conv 2: parity r in columns [r*Nd, (r+1)*Nd), rows q < L/2
-    if (tid == 0) {
-      const uint32_t idesc = tc_idesc_bf16(128, Nd);
-      const uint32_t lboA = PC * 16, lboB = g.d * 16;
-      for (int r = 0; r < 2; ++r)
-        for (int u = 0; u < 5; ++u)
-          for (int j = 0; j < g.kcd / 2; ++j) {
-            const uint64_t ad = tc_desc(sbase + g.ucs + 2 * j * lboA + (4 - u) * 16, lboA, 128);
-            const uint64_t bd = tc_desc(sbase + g.uw2 + ((r * 5 + u) * g.kcd + 2 * j) * lboB, lboB, 128);
-            tc_mma_bf16(dt + r * Nd, ad, bd, idesc, (u | j) ? 1u : 0u);
-          }
-      tc_commit(&bar);
-    }
-    if (__syncthreads_or(!tc_mbar_wait(&bar, phase, a.st, 24))) {
-      failed = true;
-      break;
-    }
-    phase ^= 1;
-    tc_fence_after_sync();
-    if (32 * qd < L2) {
-      for (int qq = 32 * qd; qq < L2; qq += 128) {  // L/2 = 128 positions fill all four lane quarters
-        const int q = qq + lane, r = hf;
-        for (int k0 = 0; k0 < g.kcd; k0 += 4) {
-          float vv[32];
-          tc_ld32(dt + ((uint32_t)(32 * qd) << 16) + r * Nd + 8 * k0, vv);
-          for (int k = 0; k < 4 && k0 + k < g.kcd; ++k)
-            ds[(size_t)(k0 + k) * PD + 2 * q + r + 1] = act8(vv + 8 * k, cst, k0 + k, g.d, 384, 512, 640);
-        }
-      }
-    }
-    sync_for_mma();
-    // mix: D[p][o] = sum_t d[p + t - 1] M_t; positions in halves of 128 rows
-    if (tid == 0) {
-      const uint32_t idesc = tc_idesc_bf16(128, Nm);
-      const uint32_t lboA = PD * 16, lboB = g.cmix * 16;
-      for (int h = 0; h < L / 128; ++h)
-        for (int t = 0; t < 3; ++t)
-          for (int j = 0; j < g.kcd / 2; ++j) {
-            const uint64_t ad = tc_desc(sbase + g.uds + 2 * j * lboA + (t + 128 * h) * 16, lboA, 128);
-            const uint64_t bd = tc_desc(sbase + g.uwm + (t * g.kcd + 2 * j) * lboB, lboB, 128);
-            tc_mma_bf16(dt + h * Nm, ad, bd, idesc, (t | j) ? 1u : 0u);
-          }
-      tc_commit(&bar);
-    }
-    // bs is free once the first transposed conv has completed: next item's input
-    if (it + 1 < rg.hi) load_mid(it + 1);
-    if (__syncthreads_or(!tc_mbar_wait(&bar, phase, a.st, 25))) {
-      failed = true;
-      break;
-    }
-    phase ^= 1;
-    tc_fence_after_sync();
-    for (int h = 0; h < L / 128; ++h) {
-      // L = 256: half hf takes position half h; L = 128: half hf takes channels [16hf, 16hf+16)
-      if (L == 256 && h != hf) continue;
-      const int p = 128 * h + 32 * qd + lane;
-      float vv[32];
-      tc_ld32(dt + ((uint32_t)(32 * qd) << 16) + h * Nm, vv);
-      const int o0 = (L == 256) ? 0 : 16 * hf, o1 = (L == 256) ? Nm : 16 * hf + 16;
-      for (int o = o0; o < o1 && o < g.cmix; ++o) {
-        float y = vv[o] + cst[768 + o];
-        if (g.residual) y += xres[(size_t)o * L + p];
-        op[(size_t)o * L + p] = y;
-      }
-    }
-    tc_fence_before_sync();
+  };
+  bool failed = false, stuck = false;
+  for (long long lo = rg.lo; lo < rg.hi && !failed;) {
+    const Seg sg = next_seg(lo, rg.hi, a.nv);
     __syncthreads();
+    copy16(sm, a.img + (size_t)sg.grp * g.usize, g.usize);
+    tc_fence_async_smem();
+    __syncthreads();
+    if (sg.lo + wg < sg.hi) fetch_mid(sg.lo + wg);
+    for (long long it = sg.lo + wg; it < sg.hi; it += 2) {
+      const long long v = it % a.nv;
+      const float* __restrict__ xin = a.x + ((long long)v * a.G + sg.grp) * (long long)g.cin * L;
+      float* __restrict__ op = a.out + ((long long)v * a.G + sg.grp) * (long long)cout * L;
+      if (!group_wait(&mbar[wg], mphase, a.st, 26, wg, &fail[wg])) {
+        failed = true;
+        break;
+      }
+      mphase ^= 1;
+      mpend = false;
+      tc_fence_after_sync();
+      // transposed conv 1: rows q < L/4
+      if (gt == 0) deconv_mma(0, g.ubs + goff, PB * 16, L4);
+      // while the tensor core runs: pass-through channels, and the mix
+      // accumulator preset to residual + bias (columns [mcol, mcol + nh*Nm))
+      {
+        const float4* __restrict__ src = reinterpret_cast<const float4*>(xin + (size_t)(g.cin - g.npass) * L);
+        float4* dst = reinterpret_cast<float4*>(op + (size_t)g.cmix * L);
+        for (int i = gt; i < g.npass * L / 4; i += kGroupThreads) dst[i] = __ldg(src + i);
+        float r0[32], r1[32];
+        const int p0 = 32 * qd + lane;
+#pragma unroll
+        for (int o = 0; o < 32; ++o) {
+          const bool on = o < g.cmix;
+          const float b = on ? cst[768 + o] : 0.f;
+          r0[o] = (on && g.residual ? __ldg(xin + (size_t)o * L + p0) : 0.f) + b;
+          r1[o] = (on && g.residual && nh > 1 ? __ldg(xin + (size_t)o * L + 128 + p0) : 0.f) + b;
+        }
+        tc_st32(dt + ((uint32_t)(32 * qd) << 16) + mcol, r0);
+        if (nh > 1) tc_st32(dt + ((uint32_t)(32 * qd) << 16) + mcol + Nm, r1);
+        tc_wait_st();
+      }
+      if (!group_wait_one(&bar[wg], phase, a.st, 23, wg, gt, &fail[wg])) {
+        failed = stuck = true;
+        break;
+      }
+      phase ^= 1;
+      tc_fence_after_sync();
+      // bs is free once the first transposed conv has completed: this group's next item
+      if (it + 2 < sg.hi) fetch_mid(it + 2);
+      deconv_epi(L4, cs, PC, 2, 0, 128, 256);
+      group_sync_for_mma(wg);
+      // transposed conv 2: rows q < L/2
+      if (gt == 0) deconv_mma(1, g.ucs + goff, PC * 16, L2);
+      if (!group_wait_one(&bar[wg], phase, a.st, 24, wg, gt, &fail[wg])) {
+        failed = stuck = true;
+        break;
+      }
+      phase ^= 1;
+      tc_fence_after_sync();
+      deconv_epi(L2, ds, PD, 1, 384, 512, 640);
+      group_sync_for_mma(wg);
+      // mix: D[p][o] = sum_t d[p + t - 1] M_t; positions in halves of 128 rows
+      if (gt == 0) {
+        const uint32_t idesc = tc_idesc_bf16(128, Nm);
+        const uint32_t lboA = PD * 16, lboB = g.cmix * 16;
+        for (int h = 0; h < nh; ++h)
+          for (int t = 0; t < 3; ++t)
+            for (int j = 0; j < g.kcd / 2; ++j) {
+              const uint64_t ad = tc_desc(sbase + g.uds + goff + 2 * j * lboA + (t + 128 * h) * 16, lboA, 128);
+              const uint64_t bd = tc_desc(sbase + g.uwm + (t * g.kcd + 2 * j) * lboB, lboB, 128);
+              tc_mma_bf16(dt + mcol + h * Nm, ad, bd, idesc, 1u);  // onto residual + bias
+            }
+        tc_commit(&bar[wg]);
+      }
+      if (!group_wait_one(&bar[wg], phase, a.st, 25, wg, gt, &fail[wg])) {
+        failed = stuck = true;
+        break;
+      }
+      phase ^= 1;
+      tc_fence_after_sync();
+      for (int h = 0; h < nh; ++h) {
+        const int p = 128 * h + 32 * qd + lane;
+        float vv[32];
+        tc_ld32(dt + ((uint32_t)(32 * qd) << 16) + mcol + h * Nm, vv);
+#pragma unroll
+        for (int o = 0; o < 32; ++o)
+          if (o < g.cmix) op[(size_t)o * L + p] = vv[o];
+      }
+      tc_fence_before_sync();
+      group_sync(wg);
+    }
+    lo = sg.hi;
+    failed = __syncthreads_or(failed ? 1 : 0) != 0;  // every thread takes part
   }
-  if (failed) tc_mbar_wait(&bar, phase, nullptr, 0);  // bounded: let outstanding MMAs drain
+  // bounded drains: this group's MMAs and bulk copies still in flight after a failure
+  if (stuck) tc_mbar_wait(&bar[wg], phase, nullptr, 0);
+  if (mpend) tc_mbar_wait(&mbar[wg], mphase, nullptr, 0);
   tc_fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc_tmem_dealloc(dt, ncols);
+  if (warp == 0) tc_tmem_dealloc(tbase, ncols);
 }
 
 }  // namespace tcnet
@@ -531,8 +677,11 @@ int tcnet_pack(const ves_net_block& b, int G, int L, const float* const* p, std:
   out.dsmem = g.dsmem;
   out.usmem = g.usmem;
   out.mid_bytes = g.mid_bytes;
-  if (g.n1 > 128 || g.d > 128 || g.cmix > 128 || g.dsmem > 227 * 1024 || g.usmem > 227 * 1024 || L > 256 ||
-      (L / 4) % 16 != 0)
+  // TMEM per warp group: N1 + N2 (down) and 2 * N2 + the mix halves (up)
+  // columns of 256; the mix epilogue reads 32 columns; each lane quarter
+  // holds 32 whole positions
+  if (g.n1 > 128 || g.d > 128 || g.cmix > 32 || 2 * g.kcd * 8 + (L / 128) * rup(g.cmix, 16) > 256 || g.dsmem > kMaxSmem || g.usmem > kMaxSmem || L > 256 ||
+      (L / 4) % 32 != 0)
     return VES_ERR_ARG;
   const int c1 = b.c1, c2 = b.c2, d = g.d, cin = b.cin, cmix = b.cmix;
   down.assign((size_t)g.dsize * G, 0);
@@ -602,7 +751,6 @@ int tcnet_pack(const ves_net_block& b, int G, int L, const float* const* p, std:
     // transposed convs: A[o][c] = W[grp*d + c][o][r + 2u]
     for (int layer = 0; layer < 2; ++layer) {
       const float* W = p[8 + 2 * layer];
-      const int base = layer ? g.uw2 : g.uw1;
       for (int r = 0; r < 2; ++r)
         for (int u = 0; u < 5; ++u)
           for (int kc = 0; kc < g.kcd; ++kc)
@@ -611,7 +759,7 @@ int tcnet_pack(const ves_net_block& b, int G, int L, const float* const* p, std:
                 const int c = kc * 8 + e;
                 v8[e] = c < d ? W[((size_t)(grp * d + c) * d + o) * 10 + r + 2 * u] : 0.f;
               }
-              put_row(U, base + ((size_t)((r * 5 + u) * g.kcd + kc) * d + o) * 16, v8);
+              put_row(U, up_w_off(g, layer, r, u, kc, o), v8);
             }
     }
     for (int t = 0; t < 3; ++t)
@@ -638,6 +786,11 @@ int tcnet_pack(const ves_net_block& b, int G, int L, const float* const* p, std:
 int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_down, const unsigned char* d_up,
                     const float* x, float* out, unsigned char* mid, VesDeviceStatus* st, cudaStream_t s) {
   using namespace tcnet;
+  // the block input and the intermediate are fetched by 16-byte bulk copies
+  if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(mid)) & 15u) {
+    ves_record_error(VES_ERR_ARG, "net_forward: input and workspace must be 16-byte aligned");
+    return VES_ERR_ARG;
+  }
   KArgs a;
   memcpy(&a.g, tb.geo, sizeof(Geo));
   a.G = G;
@@ -650,20 +803,20 @@ int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_dow
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  int rc = ves_cuda_status(cudaFuncSetAttribute(down_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tb.dsmem),
+  int rc = ves_cuda_status(cudaFuncSetAttribute(down_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, std::max(tb.dsmem, kMinSmem)),
                            "tc down smem");
   if (rc) return rc;
-  rc = ves_cuda_status(cudaFuncSetAttribute(up_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tb.usmem),
+  rc = ves_cuda_status(cudaFuncSetAttribute(up_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, std::max(tb.usmem, kMinSmem)),
                        "tc up smem");
   if (rc) return rc;
-  auto grid_for = [&](int smem) {
-    const int per_sm = std::max(1, std::min(2, (227 * 1024) / (smem + 1024)));
-    return (int)std::min<long long>(a.items, (long long)nsm * per_sm);
-  };
+  // one CTA per SM (it allocates all 512 TMEM columns): at least 117 KB of
+  // shared memory per CTA keeps a second one off the SM
+  const int dsm = std::max(tb.dsmem, kMinSmem), usm = std::max(tb.usmem, kMinSmem);
+  const int grid = (int)std::min<long long>(a.items, (long long)nsm);
   a.img = d_down;
   ves_count_launch(2);
-  down_kernel<<<grid_for(tb.dsmem), kThreads, tb.dsmem, s>>>(a);
+  down_kernel<<<grid, kThreads, dsm, s>>>(a);
   a.img = d_up;
-  up_kernel<<<grid_for(tb.usmem), kThreads, tb.usmem, s>>>(a);
+  up_kernel<<<grid, kThreads, usm, s>>>(a);
   return ves_launch_check("tc net block");
 }

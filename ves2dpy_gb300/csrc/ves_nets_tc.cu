@@ -67,7 +67,8 @@ struct Geo {
   // padded image does not fit): [2][5][kcd][d][16B]
   int umerge, uw1, uw2, uwm, ucst, usize;
   // up arrays of warp group 0 (group 1 at + ugrp): bs [kcd][L/4+4][16B],
-  // cs [kcd][L/2+4][16B], ds [kcd][L+2][16B]; then a tail
+  // cs [kcd][L/2+4][16B], ds [kcd][L+2][16B] (at least cin*L*4 bytes: it
+  // first receives the block input); then a tail
   int ubs, ucs, uds, ugrp, usmem;
   int mid_bytes;         // down -> up intermediate per (vesicle, group): [kcd][L/4][16B]
 };
@@ -115,7 +116,9 @@ inline Geo make_geo(const ves_net_block& b, int L) {
   o += rup(g.cin * L * 4, 16);
   g.dgrp = o - g.dxs;
   g.dsmem = g.dxs + 2 * g.dgrp + 128 * 16;
-  g.ugrp = g.kcd * (L / 4 + 4) * 16 + g.kcd * (L / 2 + 4) * 16 + g.kcd * (L + 2) * 16;
+  // ds doubles as the landing area of the block input x (FP32 [cin][L]) from
+  // the start of an item until the first transposed conv's epilogue
+  g.ugrp = g.kcd * (L / 4 + 4) * 16 + g.kcd * (L / 2 + 4) * 16 + std::max(g.kcd * (L + 2) * 16, rup(g.cin * L * 4, 16));
   for (g.umerge = 1; g.umerge >= 0; --g.umerge) {
     o = 0;
     const int dbytes = g.umerge ? 5 * g.kcd * 2 * g.kcd * 8 * 16 : 10 * g.kcd * g.d * 16;
@@ -190,10 +193,66 @@ __device__ __forceinline__ bool group_wait(uint64_t* bar, unsigned phase, VesDev
 }
 __device__ __forceinline__ bool group_wait_one(uint64_t* bar, unsigned phase, VesDeviceStatus* st, int site, int wg,
                                                int gt, int* flag) {
-  if (gt == 0 && !tc_mbar_wait(bar, phase, st, site)) atomicExch(flag, 1);
+  if (gt == 0 && !tc_mbar_wait_sleep(bar, phase, st, site)) atomicExch(flag, 1);
   group_sync(wg);
   return *(volatile int*)flag == 0;
 }
+
+// MMA issue sequences.  The issuing lane runs them as straight-line code:
+// each is a template on the number of 16-channel K steps (NK), picked by one
+// switch, so that no loop branch sits between two tcgen05.mma (a branching
+// loop in the single issuing lane costs more than the tensor core's time per
+// MMA).  Descriptors advance by adds: the start address is the low 14 bits of
+// a descriptor, in 16-byte units.
+
+// conv pair: 11 input shifts x NK K steps.  A at a0 + par*aPar + row,
+// B at b0 + oi*bOi; K steps at stepA / stepB.
+template <int NK>
+__device__ __forceinline__ void issue_conv(uint32_t d, uint64_t a0, uint64_t b0, uint32_t aPar, uint32_t bOi,
+                                           uint32_t stepA, uint32_t stepB, uint32_t idesc) {
+#pragma unroll
+  for (int oi = 0; oi < kOffsets; ++oi) {
+    const int s = shift_of(oi);
+    const uint64_t ad = a0 + (uint32_t)((s & 1) * aPar + 3 + (s >> 1));
+    const uint64_t bd = b0 + (uint32_t)oi * bOi;
+#pragma unroll
+    for (int j = 0; j < NK; ++j) tc_mma_bf16(d, ad + j * stepA, bd + j * stepB, idesc, (oi | j) ? 1u : 0u);
+  }
+}
+// transposed conv, one output parity: 5 taps u (A rows 4 - u) x NK K steps.
+template <int NK>
+__device__ __forceinline__ void issue_deconv(uint32_t d, uint64_t a0, uint64_t b0, uint32_t bTap, uint32_t stepA,
+                                             uint32_t stepB, uint32_t idesc) {
+#pragma unroll
+  for (int u = 0; u < 5; ++u) {
+    const uint64_t ad = a0 + (uint32_t)(4 - u), bd = b0 + (uint32_t)u * bTap;
+#pragma unroll
+    for (int j = 0; j < NK; ++j) tc_mma_bf16(d, ad + j * stepA, bd + j * stepB, idesc, (u | j) ? 1u : 0u);
+  }
+}
+// mix of one 128-position half: 3 taps t (A rows t) x NK K steps, onto the
+// preset accumulator
+template <int NK>
+__device__ __forceinline__ void issue_mix(uint32_t d, uint64_t a0, uint64_t b0, uint32_t bTap, uint32_t stepA,
+                                          uint32_t stepB, uint32_t idesc) {
+#pragma unroll
+  for (int t = 0; t < 3; ++t) {
+    const uint64_t ad = a0 + (uint32_t)t, bd = b0 + (uint32_t)t * bTap;
+#pragma unroll
+    for (int j = 0; j < NK; ++j) tc_mma_bf16(d, ad + j * stepA, bd + j * stepB, idesc, 1u);
+  }
+}
+#define VES_TC_NK_SWITCH(nk, call)                                                                            \
+  switch (nk) {                                                                                               \
+    case 1: call(1); break;                                                                                   \
+    case 2: call(2); break;                                                                                   \
+    case 3: call(3); break;                                                                                   \
+    case 4: call(4); break;                                                                                   \
+    case 5: call(5); break;                                                                                   \
+    case 6: call(6); break;                                                                                   \
+    case 7: call(7); break;                                                                                   \
+    default: call(8); break;                                                                                  \
+  }
 
 struct Range {
   long long lo, hi;
@@ -354,15 +413,10 @@ __global__ void __launch_bounds__(kThreads, 1) down_kernel(KArgs a) {
       if (gt == 0) {
         const uint32_t idesc = tc_idesc_bf16(128, N1);
         const uint32_t lboA = P1 * 16, lboB = g.n1 * 16;
-        for (int oi = 0; oi < kOffsets; ++oi) {
-          const int s = shift_of(oi);
-          const int par = s & 1, row = 3 + (s >> 1);
-          for (int j = 0; j < g.kcin / 2; ++j) {
-            const uint64_t ad = tc_desc(sbase + g.dxs + goff + (par * g.kcin + 2 * j) * lboA + row * 16, lboA, 128);
-            const uint64_t bd = tc_desc(sbase + g.dw1 + (oi * g.kcin + 2 * j) * lboB, lboB, 128);
-            tc_mma_bf16(d1, ad, bd, idesc, (oi | j) ? 1u : 0u);
-          }
-        }
+        const uint64_t a0 = tc_desc(sbase + g.dxs + goff, lboA, 128), b0 = tc_desc(sbase + g.dw1, lboB, 128);
+#define VES_CONV1(NK) issue_conv<NK>(d1, a0, b0, (g.kcin * lboA) >> 4, (g.kcin * lboB) >> 4, (2 * lboA) >> 4, (2 * lboB) >> 4, idesc)
+        VES_TC_NK_SWITCH(g.kcin / 2, VES_CONV1)
+#undef VES_CONV1
         tc_commit(&bar[wg]);
       }
       if (!group_wait_one(&bar[wg], phase, a.st, 21, wg, gt, &fail[wg])) {
@@ -377,8 +431,10 @@ __global__ void __launch_bounds__(kThreads, 1) down_kernel(KArgs a) {
         for (int k0 = 0; k0 < g.kc1; k0 += 4) {
           float vv[32];
           tc_ld32(d1 + ((uint32_t)(32 * qd) << 16) + 8 * k0, vv);
-          for (int k = 0; k < 4 && k0 + k < g.kc1; ++k) {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
             const int kc = k0 + k;
+            if (kc >= g.kc1) break;
             const uint4 val = act8(vv + 8 * k, cst, kc, g.n1, 0, 128, 256);
             uint4* base = as + (size_t)(par * g.kc1 + kc) * P2;
             base[q + 3] = val;
@@ -392,15 +448,10 @@ __global__ void __launch_bounds__(kThreads, 1) down_kernel(KArgs a) {
       if (gt == 0) {
         const uint32_t idesc = tc_idesc_bf16(128, N2);
         const uint32_t lboA = P2 * 16, lboB = g.d * 16;
-        for (int oi = 0; oi < kOffsets; ++oi) {
-          const int s = shift_of(oi);
-          const int par = s & 1, row = 3 + (s >> 1);
-          for (int j = 0; j < g.kc1 / 2; ++j) {
-            const uint64_t ad = tc_desc(sbase + g.das + goff + (par * g.kc1 + 2 * j) * lboA + row * 16, lboA, 128);
-            const uint64_t bd = tc_desc(sbase + g.dw2 + (oi * g.kc1 + 2 * j) * lboB, lboB, 128);
-            tc_mma_bf16(d2, ad, bd, idesc, (oi | j) ? 1u : 0u);
-          }
-        }
+        const uint64_t a0 = tc_desc(sbase + g.das + goff, lboA, 128), b0 = tc_desc(sbase + g.dw2, lboB, 128);
+#define VES_CONV2(NK) issue_conv<NK>(d2, a0, b0, (g.kc1 * lboA) >> 4, (g.kc1 * lboB) >> 4, (2 * lboA) >> 4, (2 * lboB) >> 4, idesc)
+        VES_TC_NK_SWITCH(g.kc1 / 2, VES_CONV2)
+#undef VES_CONV2
         tc_commit(&bar[wg]);
       }
       if (!group_wait_one(&bar[wg], phase, a.st, 22, wg, gt, &fail[wg])) {
@@ -414,8 +465,9 @@ __global__ void __launch_bounds__(kThreads, 1) down_kernel(KArgs a) {
         for (int k0 = 0; k0 < g.kcd; k0 += 4) {
           float vv[32];
           tc_ld32(d2 + ((uint32_t)(32 * qd) << 16) + 8 * k0, vv);
-          for (int k = 0; k < 4 && k0 + k < g.kcd; ++k)
-            stage[(size_t)(k0 + k) * L4 + p] = act8(vv + 8 * k, cst, k0 + k, g.d, 384, 512, 640);
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            if (k0 + k < g.kcd) stage[(size_t)(k0 + k) * L4 + p] = act8(vv + 8 * k, cst, k0 + k, g.d, 384, 512, 640);
         }
       }
       tc_fence_before_sync();
@@ -437,7 +489,7 @@ __global__ void __launch_bounds__(kThreads, 1) down_kernel(KArgs a) {
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
   extern __shared__ __align__(128) unsigned char sm[];
-  __shared__ uint64_t bar[2], mbar[2];  // per warp group: MMA completion, intermediate arrival
+  __shared__ uint64_t bar[2], mbar[2], rbar[2];  // per warp group: MMA completion, intermediate, block input
   __shared__ uint32_t tbase;
   __shared__ int fail[2];
   const Geo& g = a.g;
@@ -452,6 +504,7 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
     for (int k = 0; k < 2; ++k) {
       tc_mbar_init(&bar[k], 1);
       tc_mbar_init(&mbar[k], 1);
+      tc_mbar_init(&rbar[k], 1);
     }
     tc_mbar_fence_init();
     fail[0] = fail[1] = 0;
@@ -470,12 +523,15 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
   const int Nd = g.kcd * 8, Nm = rup(g.cmix, 16);
   const int cout = g.cmix + g.npass;
   const int nh = L / 128;      // 128-position halves of the mix
-  const int mcol = 2 * Nd;     // first TMEM column of the mix accumulators
+  const int mcol = 2 * Nd;     // first TMEM column of the mix accumulators (after the transposed convs')
   uint4* bs = reinterpret_cast<uint4*>(sm + g.ubs + goff);
   uint4* cs = reinterpret_cast<uint4*>(sm + g.ucs + goff);
   uint4* ds = reinterpret_cast<uint4*>(sm + g.uds + goff);
-  unsigned phase = 0, mphase = 0;
-  bool mpend = false;  // bulk copies into bs in flight
+  const float* xf = reinterpret_cast<const float*>(ds);  // block input while it sits in ds
+  const bool need_x = g.residual || g.npass > 0;
+  const uint32_t xbytes = (uint32_t)(g.cin * L * 4);
+  unsigned phase = 0, mphase = 0, rphase = 0;
+  bool mpend = false, rpend = false;  // bulk copies into bs / ds in flight
   // intermediate [kcd][L/4][16B] of an item -> bs rows 2 .. L/4+1 of each chunk
   auto fetch_mid = [&](long long item) {
     if (gt == 0) {
@@ -495,26 +551,25 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
   // as two MMAs on the same lanes.
   auto deconv_mma = [&](int layer, uint32_t a_off, uint32_t lboA, int npos) {
     const bool msplit = 2 * npos <= 128;
+    const uint32_t bTap = (uint32_t)(up_w_off(g, layer, 0, 1, 0, 0) - up_w_off(g, layer, 0, 0, 0, 0)) >> 4;
+    const uint32_t stepA = (2 * lboA) >> 4;
     if (g.umerge && !msplit) {
       const uint32_t idesc = tc_idesc_bf16(128, 2 * Nd);
       const uint32_t lboB = 2 * Nd * 16;
-      for (int u = 0; u < 5; ++u)
-        for (int j = 0; j < g.kcd / 2; ++j) {
-          const uint64_t ad = tc_desc(sbase + a_off + 2 * j * lboA + (4 - u) * 16, lboA, 128);
-          const uint64_t bd = tc_desc(sbase + up_w_off(g, layer, 0, u, 2 * j, 0), lboB, 128);
-          tc_mma_bf16(dt, ad, bd, idesc, (u | j) ? 1u : 0u);
-        }
+      const uint64_t a0 = tc_desc(sbase + a_off, lboA, 128), b0 = tc_desc(sbase + up_w_off(g, layer, 0, 0, 0, 0), lboB, 128);
+#define VES_DEC(NK) issue_deconv<NK>(dt, a0, b0, bTap, stepA, (2 * lboB) >> 4, idesc)
+      VES_TC_NK_SWITCH(g.kcd / 2, VES_DEC)
+#undef VES_DEC
     } else {
       const uint32_t idesc = tc_idesc_bf16(128, Nd);
       const uint32_t lboB = (g.umerge ? 2 * Nd : g.d) * 16;
       for (int r = 0; r < 2; ++r) {
         const int lift = msplit ? r * npos * 16 : 0;
-        for (int u = 0; u < 5; ++u)
-          for (int j = 0; j < g.kcd / 2; ++j) {
-            const uint64_t ad = tc_desc(sbase + a_off + 2 * j * lboA + (4 - u) * 16 - lift, lboA, 128);
-            const uint64_t bd = tc_desc(sbase + up_w_off(g, layer, r, u, 2 * j, 0), lboB, 128);
-            tc_mma_bf16(dt + r * Nd, ad, bd, idesc, (u | j) ? 1u : 0u);
-          }
+        const uint64_t a0 = tc_desc(sbase + a_off - lift, lboA, 128);
+        const uint64_t b0 = tc_desc(sbase + up_w_off(g, layer, r, 0, 0, 0), lboB, 128);
+#define VES_DEC(NK) issue_deconv<NK>(dt + r * Nd, a0, b0, bTap, stepA, (2 * lboB) >> 4, idesc)
+        VES_TC_NK_SWITCH(g.kcd / 2, VES_DEC)
+#undef VES_DEC
       }
     }
     tc_commit(&bar[wg]);
@@ -536,8 +591,10 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
       for (int k0 = 0; k0 < g.kcd; k0 += 4) {
         float vv[32];
         tc_ld32(dt + ((uint32_t)lane0 << 16) + r * Nd + 8 * k0, vv);
-        for (int k = 0; k < 4 && k0 + k < g.kcd; ++k)
-          dst[(size_t)(k0 + k) * pitch + 2 * q + r + row0] = act8(vv + 8 * k, cst, k0 + k, g.d, ob, os, ot);
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (k0 + k < g.kcd)
+            dst[(size_t)(k0 + k) * pitch + 2 * q + r + row0] = act8(vv + 8 * k, cst, k0 + k, g.d, ob, os, ot);
       }
     }
   };
@@ -553,6 +610,14 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
       const long long v = it % a.nv;
       const float* __restrict__ xin = a.x + ((long long)v * a.G + sg.grp) * (long long)g.cin * L;
       float* __restrict__ op = a.out + ((long long)v * a.G + sg.grp) * (long long)cout * L;
+      // the block input lands in ds (free since the previous item's mix completed)
+      if (need_x) {
+        if (gt == 0) {
+          tc_expect_tx(&rbar[wg], xbytes);
+          tc_bulk_g2s(ds, xin, xbytes, &rbar[wg]);
+        }
+        rpend = true;
+      }
       if (!group_wait(&mbar[wg], mphase, a.st, 26, wg, &fail[wg])) {
         failed = true;
         break;
@@ -562,25 +627,6 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
       tc_fence_after_sync();
       // transposed conv 1: rows q < L/4
       if (gt == 0) deconv_mma(0, g.ubs + goff, PB * 16, L4);
-      // while the tensor core runs: pass-through channels, and the mix
-      // accumulator preset to residual + bias (columns [mcol, mcol + nh*Nm))
-      {
-        const float4* __restrict__ src = reinterpret_cast<const float4*>(xin + (size_t)(g.cin - g.npass) * L);
-        float4* dst = reinterpret_cast<float4*>(op + (size_t)g.cmix * L);
-        for (int i = gt; i < g.npass * L / 4; i += kGroupThreads) dst[i] = __ldg(src + i);
-        float r0[32], r1[32];
-        const int p0 = 32 * qd + lane;
-#pragma unroll
-        for (int o = 0; o < 32; ++o) {
-          const bool on = o < g.cmix;
-          const float b = on ? cst[768 + o] : 0.f;
-          r0[o] = (on && g.residual ? __ldg(xin + (size_t)o * L + p0) : 0.f) + b;
-          r1[o] = (on && g.residual && nh > 1 ? __ldg(xin + (size_t)o * L + 128 + p0) : 0.f) + b;
-        }
-        tc_st32(dt + ((uint32_t)(32 * qd) << 16) + mcol, r0);
-        if (nh > 1) tc_st32(dt + ((uint32_t)(32 * qd) << 16) + mcol + Nm, r1);
-        tc_wait_st();
-      }
       if (!group_wait_one(&bar[wg], phase, a.st, 23, wg, gt, &fail[wg])) {
         failed = stuck = true;
         break;
@@ -590,7 +636,34 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
       // bs is free once the first transposed conv has completed: this group's next item
       if (it + 2 < sg.hi) fetch_mid(it + 2);
       deconv_epi(L4, cs, PC, 2, 0, 128, 256);
-      group_sync_for_mma(wg);
+      if (need_x) {
+        if (!group_wait(&rbar[wg], rphase, a.st, 27, wg, &fail[wg])) {
+          failed = true;
+          break;
+        }
+        rphase ^= 1;
+        rpend = false;
+        // pass-through channels
+        const float4* src = reinterpret_cast<const float4*>(xf + (size_t)(g.cin - g.npass) * L);
+        float4* dst = reinterpret_cast<float4*>(op + (size_t)g.cmix * L);
+        for (int i = gt; i < g.npass * L / 4; i += kGroupThreads) dst[i] = src[i];
+      }
+      {
+        // mix accumulators preset to residual + bias (columns [mcol, mcol + nh*Nm))
+        float r0[32], r1[32];
+        const int p0 = 32 * qd + lane;
+#pragma unroll
+        for (int o = 0; o < 32; ++o) {
+          const bool on = o < g.cmix;
+          const float b = on ? cst[768 + o] : 0.f;
+          r0[o] = (on && g.residual ? xf[o * L + p0] : 0.f) + b;
+          r1[o] = (on && g.residual && nh > 1 ? xf[o * L + 128 + p0] : 0.f) + b;
+        }
+        tc_st32(dt + ((uint32_t)(32 * qd) << 16) + mcol, r0);
+        if (nh > 1) tc_st32(dt + ((uint32_t)(32 * qd) << 16) + mcol + Nm, r1);
+        tc_wait_st();
+      }
+      group_sync_for_mma(wg);  // also: every read of the block input in ds is done
       // transposed conv 2: rows q < L/2
       if (gt == 0) deconv_mma(1, g.ucs + goff, PC * 16, L2);
       if (!group_wait_one(&bar[wg], phase, a.st, 24, wg, gt, &fail[wg])) {
@@ -600,18 +673,19 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
       phase ^= 1;
       tc_fence_after_sync();
       deconv_epi(L2, ds, PD, 1, 384, 512, 640);
+      // the halo rows of ds (zero padding of the mix) held block input
+      if (gt < 2 * g.kcd) ds[(gt >> 1) * PD + ((gt & 1) ? L + 1 : 0)] = make_uint4(0, 0, 0, 0);
       group_sync_for_mma(wg);
       // mix: D[p][o] = sum_t d[p + t - 1] M_t; positions in halves of 128 rows
       if (gt == 0) {
         const uint32_t idesc = tc_idesc_bf16(128, Nm);
         const uint32_t lboA = PD * 16, lboB = g.cmix * 16;
-        for (int h = 0; h < nh; ++h)
-          for (int t = 0; t < 3; ++t)
-            for (int j = 0; j < g.kcd / 2; ++j) {
-              const uint64_t ad = tc_desc(sbase + g.uds + goff + 2 * j * lboA + (t + 128 * h) * 16, lboA, 128);
-              const uint64_t bd = tc_desc(sbase + g.uwm + (t * g.kcd + 2 * j) * lboB, lboB, 128);
-              tc_mma_bf16(dt + mcol + h * Nm, ad, bd, idesc, 1u);  // onto residual + bias
-            }
+        const uint64_t a0 = tc_desc(sbase + g.uds + goff, lboA, 128), b0 = tc_desc(sbase + g.uwm, lboB, 128);
+        for (int h = 0; h < nh; ++h) {  // onto residual + bias
+#define VES_MIX(NK) issue_mix<NK>(dt + mcol + h * Nm, a0 + (uint32_t)(128 * h), b0, (g.kcd * lboB) >> 4, (2 * lboA) >> 4, (2 * lboB) >> 4, idesc)
+          VES_TC_NK_SWITCH(g.kcd / 2, VES_MIX)
+#undef VES_MIX
+        }
         tc_commit(&bar[wg]);
       }
       if (!group_wait_one(&bar[wg], phase, a.st, 25, wg, gt, &fail[wg])) {
@@ -637,6 +711,7 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
   // bounded drains: this group's MMAs and bulk copies still in flight after a failure
   if (stuck) tc_mbar_wait(&bar[wg], phase, nullptr, 0);
   if (mpend) tc_mbar_wait(&mbar[wg], mphase, nullptr, 0);
+  if (rpend) tc_mbar_wait(&rbar[wg], rphase, nullptr, 0);
   tc_fence_before_sync();
   __syncthreads();
   if (warp == 0) tc_tmem_dealloc(tbase, ncols);

@@ -46,6 +46,19 @@ __device__ __forceinline__ bool tc_mbar_wait(uint64_t* bar, unsigned parity, Ves
   return false;
 }
 
+// Bounded wait with a short sleep between polls, for a single thread that
+// waits on MMA completion (hundreds of cycles) while other warps of the SM
+// issue: the sleep leaves the issue slots to them.  The bound (2^20 polls of
+// at least 64 ns) is far above any MMA batch of these kernels.
+__device__ __forceinline__ bool tc_mbar_wait_sleep(uint64_t* bar, unsigned parity, VesDeviceStatus* st, int site) {
+  for (int it = 0; it < (1 << 20); ++it) {
+    if (tc_mbar_try_wait(bar, parity)) return true;
+    __nanosleep(64);
+  }
+  ves_set_error(st, VES_ERR_TIMEOUT, site, (long long)blockIdx.x);
+  return false;
+}
+
 // --- bulk copies (cp.async.bulk, completion counted in bytes on an mbarrier) --
 // The issuing thread arrives once on `bar` and announces `bytes` of transfer;
 // the phase completes when every copy charged to it has landed.
@@ -59,6 +72,11 @@ __device__ __forceinline__ void tc_bulk_g2s(void* dst, const void* src, uint32_t
                    tc_smem_u32(dst)),
                "l"(src), "r"(bytes), "r"(tc_smem_u32(bar))
                : "memory");
+}
+
+// Prefetch `bytes` (multiple of 16, 16-byte aligned) of global memory into L2.
+__device__ __forceinline__ void tc_prefetch_l2(const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
 }
 
 // --- fences -----------------------------------------------------------------

@@ -49,7 +49,8 @@ def parse():
     ap.add_argument("--N", type=int, default=128)
     ap.add_argument("--area-fraction", type=float, default=0.15)
     ap.add_argument("--nets", default="bf16", choices=["bf16", "fp32"])
-    ap.add_argument("--precision", default="fp32c")
+    ap.add_argument("--precision", default="fp32m", choices=["fp32m", "fp32c", "fp64"],
+                    help="all-pairs sums: fp32m (multipole for separated vesicle pairs), fp32c (direct), fp64")
     ap.add_argument("--biem-steps", type=int, default=1)
     ap.add_argument("--biem-warmup", type=int, default=0)
     ap.add_argument("--biem-tol", type=float, default=1e-8)
@@ -283,14 +284,16 @@ def run_mlarm(a, dev, X0, state_dicts):
     torch.cuda.synchronize()
     barrier()
     t0 = time.perf_counter()
+    X1_m = None
     for _ in range(a.e2e_steps):
         Xn, tn = m.time_step_many_noinfo(Xh.to(dev, non_blocking=True), th.to(dev, non_blocking=True), 3)
         Xback.copy_(Xn, non_blocking=True)
         tback.copy_(tn, non_blocking=True)
         torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / max(a.e2e_steps, 1)
+    e2e_s = (time.perf_counter() - t0) / a.e2e_steps if a.e2e_steps > 0 else None
     io = Xh.numel() * 8 + th.numel() * 8
-    X1_m = Xback.clone()
+    if a.e2e_steps > 0:
+        X1_m = Xback.clone()
     return dict(ms=ms, stats=st, launches=launches, clocks=clk.summary(), net_ms=net_ms, e2e_s=e2e_s, io=io,
                 drift=drift, near_pairs=near_pairs, X1=X1_m, nets=m.nets)
 
@@ -307,7 +310,7 @@ def run_biem(a, dev, X0):
     prams = dict(STEP, viscCont=[1.0] * nv, gmresTol=a.biem_tol)
     Xd = torch.tensor(X0, dtype=torch.float64, device=dev)
     tt = TStepBiem(Xd, None, options, prams, near="py_hh", farfield_precision=a.precision,
-                   sl_precision=a.precision)
+                   sl_precision="fp64" if a.precision == "fp64" else "fp32c")
     ctx = nat.context(N, dev)
     ws = ctx.workspace(tt.workspace_bytes())
     Xv = to_vm(Xd)
@@ -385,6 +388,49 @@ def run_gb300(a, rank, world):
     flops = {n: net_flops(NETS[n]) * a.nv for n in NETS}
     net_total_ms = sum(r["net_ms"].values())
     net_tflops = sum(flops.values()) / (net_total_ms * 1e-3) / 1e12 if net_total_ms > 0 else None
+    # networks, timed live inside the timed MLARM steps (CUDA events around each forward pass)
+    nl_tflops = (st.networks_flops / (st.networks_ms * 1e-3) / 1e12) if st.networks_ms > 0 else None
+    roof_net = {"bound": "tensor", "kernel": "tcnet::down_kernel / up_kernel (tcgen05.mma kind::f16, BF16)",
+                "achieved": nl_tflops, "peak": bf16_peak, "unit": "TFLOP/s",
+                "frac": nl_tflops / bf16_peak if nl_tflops else None, "traffic": None,
+                "traffic_note": "ncu (profiles/tcnet_adv_block_nv64_full.md): one down+up launch pair of an "
+                                "advection-network block at nv=64 moves 215 + 383 MB of DRAM, the FP32 block input "
+                                "read twice, the output written once and the BF16 intermediate written and read "
+                                "(no re-reads); per launch it scales with nv",
+                "flops_per_step": st.networks_flops / a.steps, "ms_per_step": st.networks_ms / a.steps,
+                "passes_per_step": st.networks_launches / a.steps,
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured",
+                "share_of_step": st.networks_ms / r["ms"] if r["ms"] else None}
+    # all-pairs sums
+    sm_mhz = (r["clocks"] or {}).get("sm_max_mhz") or 2070.0
+    if a.precision == "fp32m":
+        # FP32 work actually done: 16 FMA per series term (four complex Horner
+        # steps) and 12 FP32 operations per direct-rule pair
+        ff_flops = 2.0 * (16.0 * st.farfield_mp_terms + 12.0 * st.farfield_direct_pairs) / max(st.farfield_launches, 1)
+        fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6
+        ach = ff_flops / (ff_ms * 1e-3) if ff_ms > 0 else 0.0
+        roof_ff = {"bound": "fp32", "kernel": "mp_eval_kernel (multipole series + direct rule for close pairs)",
+                   "achieved": ach / 1e12, "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
+                   "frac": ach / fp32_peak, "traffic": None,
+                   "traffic_note": "compute-bound: sources, moments and targets stay in L2",
+                   "peak_source": "nominal: 152 SMs x 128 FP32 lanes x 2 x max SM clock (no measured figure)",
+                   "ms_per_launch": ff_ms, "series_terms_per_launch": st.farfield_mp_terms / max(st.farfield_launches, 1),
+                   "direct_pairs_per_launch": st.farfield_direct_pairs / max(st.farfield_launches, 1),
+                   "reference_pairs_per_launch": ff_pairs,
+                   "reference_pairs_per_s": ff_pairs / (ff_ms * 1e-3) if ff_ms > 0 else None,
+                   "share_of_step": st.farfield_ms / r["ms"] if r["ms"] else None}
+    else:
+        roof_ff = {"bound": "sfu", "kernel": "ff_main_kernel (all-pairs Stokeslet sum, direct)",
+                   "achieved": mufu_rate / 1e9, "peak": sfu_peak / 1e9, "unit": "Gop/s (MUFU lg2+rcp)",
+                   "frac": mufu_rate / sfu_peak if sfu_peak else None, "traffic": None,
+                   "traffic_note": "compute-bound; ncu measured 6.7 MB DRAM per launch at nv=256 "
+                                   "(sources L2-resident), see profiles/ff_main_kernel_nv256_N128_full.md",
+                   "pairs_per_launch": ff_pairs, "ms_per_launch": ff_ms,
+                   "gpairs_per_s": ff_pairs / (ff_ms * 1e-3) / 1e9 if ff_ms > 0 else None,
+                   "peak_source": "measured by ves_probe_sfu_peak on this GPU",
+                   "share_of_step": st.farfield_ms / r["ms"] if r["ms"] else None}
+    # the dominant kernel of the step carries the main roofline
+    roof_main = roof_ff if (roof_ff.get("share_of_step") or 0) > (roof_net.get("share_of_step") or 0) else roof_net
     out = {
         "metric": METRIC,
         "value": value,
@@ -396,7 +442,10 @@ def run_gb300(a, rank, world):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "bf16 networks (fp32 accumulation) + f32 compensated all-pairs sums + f64 geometry",
+        "dtype": ("bf16 networks (fp32 accumulation) + f32 all-pairs sums (" +
+                  ("multipole series for separated vesicle pairs, compensated direct sums for close pairs"
+                   if a.precision == "fp32m" else "compensated direct sums" if a.precision == "fp32c" else "f64") +
+                  ") + f64 geometry"),
         "data": "synthetic (seeded suspension generator and seeded network weights of the reference "
                 "architectures; the reference's trained weights and initial conditions are absent)",
         "config": {
@@ -413,34 +462,26 @@ def run_gb300(a, rank, world):
                       "farfield_ms_per_eval": ff_ms, "farfield_evals_per_step": st.farfield_launches / a.steps},
         },
         "e2e": {"value": world * a.nv / r["e2e_s"], "unit": "vesicle-steps/s", "h2d_bytes_per_step": r["io"],
-                "d2h_bytes_per_step": r["io"]} if r["e2e_s"] > 0 else None,
+                "d2h_bytes_per_step": r["io"]} if r["e2e_s"] else None,
         "gpu_launches": int(r["launches"]),
-        "roofline": {"bound": "sfu", "kernel": "ff_main_kernel<float> (all-pairs Stokeslet sum)",
-                     "achieved": mufu_rate / 1e9, "peak": sfu_peak / 1e9, "unit": "Gop/s (MUFU lg2+rcp)",
-                     "frac": mufu_rate / sfu_peak if sfu_peak else None, "traffic": None,
-                     "traffic_note": "compute-bound; ncu measured 6.7 MB DRAM per launch at nv=256 "
-                                     "(sources L2-resident), see profiles/ff_main_kernel_nv256_N128_full.md",
-                     "pairs_per_launch": ff_pairs, "ms_per_launch": ff_ms,
-                     "gpairs_per_s": ff_pairs / (ff_ms * 1e-3) / 1e9 if ff_ms > 0 else None,
-                     "peak_source": "measured by ves_probe_sfu_peak on this GPU",
-                     "share_of_step": st.farfield_ms / r["ms"] if r["ms"] else None},
-        "roofline_networks": {"bound": "tensor", "achieved": net_tflops, "peak": bf16_peak, "unit": "TFLOP/s",
-                              "frac": net_tflops / bf16_peak if net_tflops else None,
-                              "flops_per_step": sum(flops.values()),
-                              "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured",
-                              "kernels": "tcnet down_kernel / up_kernel (tcgen05.mma kind::f16, BF16)"},
+        "roofline": roof_main,
+        "roofline_networks": roof_net,
+        "roofline_farfield": roof_ff,
         "clocks": r["clocks"],
     }
     if b is not None:
         out["config"]["biem"] = {"value": vb, "unit": "vesicle-steps/s", "ms_per_step": tb / a.biem_steps,
                                  "steps": a.biem_steps, "warmup": a.biem_warmup, "matvecs_per_step": b["matvecs"],
                                  "gmres_info_resid": b["info"], "gmres_tol": a.biem_tol,
-                                 "note": "the context, kernels and workspace are warm from the MLARM run; GMRES "
-                                         "tol 1e-8 because the FP32-compensated all-pairs operator is accurate to "
-                                         "~5e-9 on unit-length vesicles (at tol 1e-10 GMRES stalls there and stops "
-                                         "after 106 matvecs; the FP64 operator converges in 38-50 at nv=256)"}
+                                 "note": "the context, kernels and workspace are warm from the MLARM run; same "
+                                         "all-pairs precision as the MLARM arm; GMRES tol 1e-8 because the FP32 "
+                                         "all-pairs operators are accurate to ~1e-8 on unit-length vesicles (with "
+                                         "the direct FP32 sums GMRES stalls near 5e-9 at tol 1e-10 and stops after "
+                                         "106 matvecs; the FP64 operator converges in 38-50 at nv=256)"}
         out["config"]["mlarm_over_biem"] = value / vb
         try:
+            if r["X1"] is None:
+                raise ValueError("no end-to-end step")
             out["config"]["centroid_velocity_error_vs_biem"] = centroid_velocity_error(
                 X0, r["X1"].numpy(), b["X1"].numpy(), STEP["dt"])
             out["config"]["velocity_error_note"] = ("networks carry synthetic untrained weights, so the surrogate "

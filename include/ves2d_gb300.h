@@ -50,6 +50,10 @@ extern "C" {
 /* arithmetic of the all-pairs Stokeslet sum */
 #define VES_PREC_FP64 0            /* FP64 throughout                              */
 #define VES_PREC_FP32C 1           /* FP32 pair terms, per-vesicle-pair centre      */
+#define VES_PREC_FP32M 2           /* all-pairs sums only: multipole expansion of   *
+                                    * separated source vesicles (truncation below    *
+                                    * 1e-10 of the source's density magnitude), the  *
+                                    * FP32C direct sum for close pairs               */
                                    /* shift, compensated accumulation              */
 
 /* near-singular schemes */
@@ -165,7 +169,8 @@ VES_API size_t ves_near_zone_workspace(ves_ctx* ctx, int nv);
  * self_idx[nt] (or NULL): source vesicle skipped for target column t.
  * nl (or NULL): candidate lists whose excl_mask removes (target point, source
  * vesicle) pairs (requires nt == nsrc, ntp == N of ctx).  Result written to
- * out[nt][2][ntp].  precision: VES_PREC_FP64 or VES_PREC_FP32C. */
+ * out[nt][2][ntp].  precision: VES_PREC_FP64, VES_PREC_FP32C or VES_PREC_FP32M
+ * (FP32M: at most 128 target points per column). */
 VES_API int ves_farfield(ves_ctx* ctx, int precision, int nsrc, int ns, const double* Xsrc,
                  const double* den, int nt, int ntp, const double* Xtar, const int* self_idx,
                  const ves_near_lists* nl, double* out, void* ws, size_t ws_bytes, void* stream);
@@ -375,9 +380,17 @@ typedef struct ves_stats {
   long long farfield_launches;/* all-pairs kernel launches timed on this context        */
   double farfield_ms;         /* their summed CUDA-event duration                       */
   double farfield_pairs;      /* (target point, source point) pairs they evaluated      */
+  double farfield_mp_terms;   /* VES_PREC_FP32M: series terms evaluated, summed over    *
+                               * (target point, source vesicle) pairs (orders + 1)      */
+  double farfield_direct_pairs;/* VES_PREC_FP32M: (target point, source point) pairs of *
+                               * the direct rule (close vesicle pairs)                  */
+  long long networks_launches;/* network forward passes timed on this context (MLARM)  */
+  double networks_ms;         /* their summed CUDA-event duration                       */
+  double networks_flops;      /* their useful work: 2 x multiply-adds of the layers     */
 } ves_stats;
-/* Enable/disable CUDA-event timing of the all-pairs kernel on ``ctx`` (events
- * are recorded on the launching stream around each launch; off by default). */
+/* Enable/disable CUDA-event timing of the all-pairs kernel and of the MLARM
+ * step's network forward passes on ``ctx`` (events are recorded on the
+ * launching stream around each launch; off by default). */
 VES_API int ves_ctx_set_timing(ves_ctx* ctx, int on);
 /* Read (and with reset != 0 clear) the counters; synchronises pending events. */
 VES_API int ves_ctx_stats(ves_ctx* ctx, ves_stats* out, int reset);

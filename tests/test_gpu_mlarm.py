@@ -125,16 +125,18 @@ def test_mlarm_step_fp32_networks(golden):
         assert rel(t1, g["ten1"]) < tol_t, (fixture, rel(t1, g["ten1"]))
 
 
-def test_mlarm_step_bf16_networks(golden):
+@pytest.mark.parametrize("farfield", ["fp32c", "fp32m"])
+def test_mlarm_step_bf16_networks(golden, farfield):
     """Tensor-core networks: the step stays within BF16 network noise of the
     FP64 reference (the networks move the shape by dt * velocity and the
     relaxation by a 2e-4-scaled correction, so the shape error is small while
-    the predicted tension carries the networks' relative error)."""
+    the predicted tension carries the networks' relative error).  Both FP32
+    all-pairs paths (direct, multipole) keep the far field within 1e-5."""
     g = golden("mlarm_fp64")
-    m = _mlarm("bf16", "fp32c")
+    m = _mlarm("bf16", farfield)
     m.area0 = torch.from_numpy(g["area0"])
     m.len0 = torch.from_numpy(g["len0"])
     t = m.time_step_trace(torch.from_numpy(g["Xinit"]).to(DEV), torch.zeros(128, 4, dtype=torch.float64, device=DEV))
-    assert rel(t["far1"], g["far1"]) < 1e-5          # geometry only: FP32C far field
+    assert rel(t["far1"], g["far1"]) < 1e-5          # geometry only: FP32 far field
     assert rel(t["X"], g["X1"]) < 1e-4, rel(t["X"], g["X1"])
     assert rel(t["ten"], g["ten1"]) < 5e-2, rel(t["ten"], g["ten1"])

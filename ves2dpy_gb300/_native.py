@@ -27,7 +27,7 @@ VES_ERR_TIMEOUT = 7
 VES_ERR_SINGULAR = 8
 VES_ERR_WORKSPACE = 9
 
-PREC = {"fp64": 0, "fp32c": 1}
+PREC = {"fp64": 0, "fp32c": 1, "fp32m": 2}
 NEAR = {"none": 0, "py_hh": 1, "matlab": 2}
 FLOW = {"relaxation": 0, "extensional": 1, "parabolic": 2, "taylorGreen": 3, "shear": 4, "vortex": 5}
 
@@ -100,6 +100,11 @@ class Stats(ctypes.Structure):
         ("farfield_launches", ctypes.c_longlong),
         ("farfield_ms", ctypes.c_double),
         ("farfield_pairs", ctypes.c_double),
+        ("farfield_mp_terms", ctypes.c_double),
+        ("farfield_direct_pairs", ctypes.c_double),
+        ("networks_launches", ctypes.c_longlong),
+        ("networks_ms", ctypes.c_double),
+        ("networks_flops", ctypes.c_double),
     ]
 
 

@@ -30,6 +30,31 @@ static void ff_drain(ves_ctx* c) {
   c->n_ev = 0;
 }
 
+static void net_drain(ves_ctx* c) {
+  for (int i = 0; i < c->n_nev; ++i) {
+    float ms = 0.f;
+    cudaEventSynchronize(c->nev[2 * i + 1]);
+    cudaEventElapsedTime(&ms, c->nev[2 * i], c->nev[2 * i + 1]);
+    c->net_ms += ms;
+    c->net_flops += c->nev_flops[i];
+    c->net_launches += 1;
+  }
+  c->n_nev = 0;
+}
+
+void ves_net_timing_begin(ves_ctx* c, cudaStream_t s) {
+  if (!c || !c->timing) return;
+  if (c->n_nev == 64) net_drain(c);
+  cudaEventRecord(c->nev[2 * c->n_nev], s);
+}
+
+void ves_net_timing_end(ves_ctx* c, cudaStream_t s, double flops) {
+  if (!c || !c->timing) return;
+  cudaEventRecord(c->nev[2 * c->n_nev + 1], s);
+  c->nev_flops[c->n_nev] = flops;
+  c->n_nev++;
+}
+
 void ves_ff_timing_begin(ves_ctx* c, cudaStream_t s) {
   if (!c->timing) return;
   if (c->n_ev == 256) ff_drain(c);
@@ -51,7 +76,19 @@ extern "C" int ves_ctx_set_timing(ves_ctx* c, int on) {
       if (rc) return rc;
     }
   }
+  if (on && !c->nev[0]) {
+    for (int i = 0; i < 2 * 64; ++i) {
+      int rc = ves_cuda_status(cudaEventCreate(&c->nev[i]), "cudaEventCreate");
+      if (rc) return rc;
+    }
+  }
+  if (on && !c->d_mp) {
+    int rc = ves_cuda_status(cudaMalloc(&c->d_mp, 2 * sizeof(unsigned long long)), "counters");
+    if (!rc) rc = ves_cuda_status(cudaMemset(c->d_mp, 0, 2 * sizeof(unsigned long long)), "counters");
+    if (rc) return rc;
+  }
   if (!on && c->n_ev) ff_drain(c);
+  if (!on && c->n_nev) net_drain(c);
   c->timing = on ? 1 : 0;
   return VES_OK;
 }
@@ -59,14 +96,31 @@ extern "C" int ves_ctx_set_timing(ves_ctx* c, int on) {
 extern "C" int ves_ctx_stats(ves_ctx* c, ves_stats* out, int reset) {
   if (!c || !out) return VES_ERR_ARG;
   ff_drain(c);
+  net_drain(c);
   out->kernel_launches = g_launches.load();
+  out->networks_launches = c->net_launches;
+  out->networks_ms = c->net_ms;
+  out->networks_flops = c->net_flops;
   out->farfield_launches = c->ff_launches;
   out->farfield_ms = c->ff_ms;
   out->farfield_pairs = c->ff_pairs;
+  out->farfield_mp_terms = 0;
+  out->farfield_direct_pairs = 0;
+  if (c->d_mp) {
+    unsigned long long h[2] = {0, 0};
+    int rc = ves_cuda_status(cudaMemcpy(h, c->d_mp, sizeof(h), cudaMemcpyDeviceToHost), "counters");
+    if (rc) return rc;
+    out->farfield_mp_terms = (double)h[0];
+    out->farfield_direct_pairs = (double)h[1];
+  }
   if (reset) {
     c->ff_launches = 0;
     c->ff_ms = 0;
     c->ff_pairs = 0;
+    c->net_launches = 0;
+    c->net_ms = 0;
+    c->net_flops = 0;
+    if (c->d_mp) cudaMemset(c->d_mp, 0, 2 * sizeof(unsigned long long));
   }
   return VES_OK;
 }
@@ -344,6 +398,9 @@ extern "C" int ves_ctx_destroy(ves_ctx* c) {
   if (c->h_scal) cudaFreeHost(c->h_scal);
   if (c->ev[0])
     for (int i = 0; i < 2 * 256; ++i) cudaEventDestroy(c->ev[i]);
+  if (c->d_mp) cudaFree(c->d_mp);
+  if (c->nev[0])
+    for (int i = 0; i < 2 * 64; ++i) cudaEventDestroy(c->nev[i]);
   free(c);
   return VES_OK;
 }

@@ -481,6 +481,8 @@ int farfield_run_env(const FFEnv& env, int precision, int nsrc, int ns, const do
     return ff_run<double>(env, nsrc, ns, Xsrc, den, nt, ntp, Xtar, self_idx, nl, out, ws, s);
   if (precision == VES_PREC_FP32C)
     return ff_run<float>(env, nsrc, ns, Xsrc, den, nt, ntp, Xtar, self_idx, nl, out, ws, s);
+  if (precision == VES_PREC_FP32M)
+    return farfield_mp_run(env, nsrc, ns, Xsrc, den, nt, ntp, Xtar, self_idx, nl, out, ws, s);
   ves_record_error(VES_ERR_ARG, "farfield: bad precision %d", precision);
   return VES_ERR_ARG;
 }
@@ -492,7 +494,7 @@ int farfield_run(ves_ctx* c, int precision, int nsrc, int ns, const double* Xsrc
   env.status = c ? c->status : nullptr;
   env.N = c ? c->N : ntp;
   env.timing = c;
-  if (precision == VES_PREC_FP64 || precision == VES_PREC_FP32C)
+  if (precision == VES_PREC_FP64 || precision == VES_PREC_FP32C || precision == VES_PREC_FP32M)
     return farfield_run_env(env, precision, nsrc, ns, Xsrc, den, nt, ntp, Xtar, self_idx, nl, out, ws, s);
   ves_record_error(VES_ERR_ARG, "farfield: bad precision %d", precision);
   return VES_ERR_ARG;

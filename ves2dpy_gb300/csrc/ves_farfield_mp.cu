@@ -1,0 +1,425 @@
+// All-pairs Stokeslet sum (allExactStokesSLTarget_compare1/2,
+// mytorch/biem_support.py:7-272; Poten.exactStokesSL, mytorch/poten.py:280-336)
+// evaluated with a multipole expansion of each source vesicle for the
+// vesicle pairs that are well separated, and by the direct FP32 sum for the
+// others (precision VES_PREC_FP32M).
+//
+// The sum is the reference's: for a target x and a source vesicle with
+// upsampled points w_j and quadrature-weighted densities f_j (complex
+// notation, f = fx + i fy),
+//
+//   u(x) = sum_j [ -1/2 log|r_j|^2 f_j + (r_j . f_j) r_j / |r_j|^2 ],  r_j = x - w_j
+//        = sum_j [ -1/2 log|r_j|^2 f_j + 1/2 f_j + 1/2 conj(f_j) r_j / conj(r_j) ].
+//
+// With the source centre c, v_j = w_j - c, omega = x - c, R >= max |v_j|,
+// normalised vt_j = v_j / R and tau = R / omega (|tau| = rho < 1):
+//
+//   u = -log|omega| F0 + F0/2 + sum_{k>=1} [tau^k A_k + conj(tau)^k B_k] / (2k)
+//       + 1/2 (omega / conj(omega)) conj(sum_{k>=0} tau^k A_k)
+//       - 1/2 conj(tau sum_{k>=0} tau^k E_k)
+//
+//   F0 = sum f_j,  A_k = sum f_j vt_j^k,  B_k = sum f_j conj(vt_j)^k,
+//   E_k = sum f_j conj(vt_j) vt_j^k
+//
+// (series of log(1 - v/omega) and 1/(1 - conj(v/omega))).  Truncating at
+// order P leaves at most sum_j |f_j| rho^(P+1) / (1 - rho) per series.  A
+// (target vesicle, source vesicle) pair uses the expansion when
+// rho_pair = R_s / (|c_t - c_s| - R_t) <= kRhoMax, with P the smallest order
+// whose bound is below kEps (relative to sum |f_j|); every other pair, every
+// pair on the target's near-candidate list (where single target points are
+// excluded, biem_support.py:218-219), is summed directly over the
+// upsampled points in FP32 with the source-centred logarithm of the FP32C
+// path.  The moments are FP64 sums over exactly the upsampled points of the
+// direct rule, rounded to FP32; the series are evaluated in FP32 (Horner) and
+// the per-source contributions are added with Neumaier compensation.
+#include "ves_internal.h"
+
+namespace {
+
+constexpr int kPMax = 24;                 // highest expansion order
+constexpr float kRhoMax = 0.35f;          // 0.35^25 / 0.65 < 1e-11
+constexpr float kEps = 1e-10f;            // truncation bound relative to sum |f_j|
+constexpr int kStage = 16;                // source vesicles per shared-memory stage
+constexpr double kHalfLn2 = 0.34657359027997264;
+
+struct __align__(16) MPSrc {
+  float2 chi, clo;  // centre, high and low FP32 parts
+  float2 f0;        // sum of the density
+  float R;          // bound on |w_j - c| over the upsampled points
+  float pad;
+};
+
+// one order k of one source: Al = A_k/(2k) (0 at k=0), Bc = conj(B_k/(2k)) (0 at k=0), A_k, E_k
+struct __align__(16) MPMom {
+  float2 al, bc, ac, ec;
+};
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// ---------------------------------------------------------------------------
+// One CTA (256 threads) per source vesicle: centre, FP32 records for the
+// direct rule, density sum, radius bound and the normalised moments.
+__global__ void __launch_bounds__(256) mp_prep_kernel(int ns, const double* __restrict__ X,
+                                                      const double* __restrict__ den, float4* __restrict__ rec,
+                                                      MPSrc* __restrict__ src, MPMom* __restrict__ mom) {
+  __shared__ double red[3][256];
+  const int s = blockIdx.x, t = threadIdx.x;
+  const double* x = X + (long long)s * 2 * ns;
+  const double* f = den + (long long)s * 2 * ns;
+  double sx = 0, sy = 0;
+  for (int j = t; j < ns; j += 256) {
+    sx += x[j];
+    sy += x[ns + j];
+  }
+  red[0][t] = sx;
+  red[1][t] = sy;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (t < w) {
+      red[0][t] += red[0][t + w];
+      red[1][t] += red[1][t + w];
+    }
+    __syncthreads();
+  }
+  const double cx = red[0][0] / ns, cy = red[1][0] / ns;
+  __syncthreads();
+  double r2 = 0, fx = 0, fy = 0;
+  for (int j = t; j < ns; j += 256) {
+    const double lx = x[j] - cx, ly = x[ns + j] - cy;
+    rec[(long long)s * ns + j] = make_float4((float)lx, (float)ly, (float)f[j], (float)f[ns + j]);
+    r2 = fmax(r2, lx * lx + ly * ly);
+    fx += f[j];
+    fy += f[ns + j];
+  }
+  red[0][t] = r2;
+  red[1][t] = fx;
+  red[2][t] = fy;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (t < w) {
+      red[0][t] = fmax(red[0][t], red[0][t + w]);
+      red[1][t] += red[1][t + w];
+      red[2][t] += red[2][t + w];
+    }
+    __syncthreads();
+  }
+  double R = sqrt(red[0][0]) * (1.0 + 1e-6);
+  if (!(R > 0)) R = 1.0;
+  if (t == 0) {
+    MPSrc o;
+    o.chi = make_float2((float)cx, (float)cy);
+    o.clo = make_float2((float)(cx - (double)o.chi.x), (float)(cy - (double)o.chi.y));
+    o.f0 = make_float2((float)red[1][0], (float)red[2][0]);
+    o.R = (float)R;
+    o.pad = 0.f;
+    src[s] = o;
+  }
+  // moments: warp w takes orders k = w, w + 8, w + 16, ... (<= kPMax); lanes split the points
+  const int warp = t >> 5, lane = t & 31;
+  constexpr int kPer = (kPMax + 8) / 8;  // orders per warp
+  double2 A[kPer], B[kPer], E[kPer];
+#pragma unroll
+  for (int q = 0; q < kPer; ++q) A[q] = B[q] = E[q] = make_double2(0, 0);
+  const double iR = 1.0 / R;
+  for (int j = lane; j < ns; j += 32) {
+    const double2 v = make_double2((x[j] - cx) * iR, (x[ns + j] - cy) * iR);
+    const double2 fj = make_double2(f[j], f[ns + j]);
+    double2 pw = make_double2(1, 0), v8 = v;  // pw = v^warp, v8 = v^8
+    for (int e = 0; e < warp; ++e) pw = cmul(pw, v);
+    v8 = cmul(v8, v8);
+    v8 = cmul(v8, v8);
+    v8 = cmul(v8, v8);
+    const double2 fvb = cmul(fj, make_double2(v.x, -v.y));  // f conj(v)
+#pragma unroll
+    for (int q = 0; q < kPer; ++q) {
+      const double2 a = cmul(fj, pw);
+      const double2 b = cmul(fj, make_double2(pw.x, -pw.y));
+      const double2 e = cmul(fvb, pw);
+      A[q].x += a.x;
+      A[q].y += a.y;
+      B[q].x += b.x;
+      B[q].y += b.y;
+      E[q].x += e.x;
+      E[q].y += e.y;
+      pw = cmul(pw, v8);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < kPer; ++q) {
+    for (int o = 16; o > 0; o >>= 1) {
+      A[q].x += __shfl_xor_sync(0xffffffffu, A[q].x, o);
+      A[q].y += __shfl_xor_sync(0xffffffffu, A[q].y, o);
+      B[q].x += __shfl_xor_sync(0xffffffffu, B[q].x, o);
+      B[q].y += __shfl_xor_sync(0xffffffffu, B[q].y, o);
+      E[q].x += __shfl_xor_sync(0xffffffffu, E[q].x, o);
+      E[q].y += __shfl_xor_sync(0xffffffffu, E[q].y, o);
+    }
+    const int k = warp + 8 * q;
+    if (lane == 0 && k <= kPMax) {
+      MPMom m;
+      const double h = k > 0 ? 0.5 / k : 0.0;
+      m.al = make_float2((float)(A[q].x * h), (float)(A[q].y * h));
+      m.bc = make_float2((float)(B[q].x * h), (float)(-B[q].y * h));
+      m.ac = make_float2((float)A[q].x, (float)A[q].y);
+      m.ec = make_float2((float)E[q].x, (float)E[q].y);
+      mom[(long long)s * (kPMax + 1) + k] = m;
+    }
+  }
+}
+
+// target vesicles: centre (hi/lo) and FP32 local coordinates
+__global__ void __launch_bounds__(256) mp_prep_targets_kernel(int ntp, const double* __restrict__ X,
+                                                              float2* __restrict__ local, float2* __restrict__ chi,
+                                                              float2* __restrict__ clo) {
+  __shared__ double red[2][256];
+  const int k = blockIdx.x, t = threadIdx.x;
+  const double* x = X + (long long)k * 2 * ntp;
+  double sx = 0, sy = 0;
+  for (int j = t; j < ntp; j += 256) {
+    sx += x[j];
+    sy += x[ntp + j];
+  }
+  red[0][t] = sx;
+  red[1][t] = sy;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (t < w) {
+      red[0][t] += red[0][t + w];
+      red[1][t] += red[1][t + w];
+    }
+    __syncthreads();
+  }
+  const double cx = red[0][0] / ntp, cy = red[1][0] / ntp;
+  for (int j = t; j < ntp; j += 256) local[(long long)k * ntp + j] = make_float2((float)(x[j] - cx), (float)(x[ntp + j] - cy));
+  if (t == 0) {
+    const float hx = (float)cx, hy = (float)cy;
+    chi[k] = make_float2(hx, hy);
+    clo[k] = make_float2((float)(cx - (double)hx), (float)(cy - (double)hy));
+  }
+}
+
+struct MPArgs {
+  int nsrc, ns, ntp;
+  const float4* rec;
+  const MPSrc* src;
+  const MPMom* mom;
+  const float2* tloc;
+  const float2* thi;
+  const float2* tlo;
+  const int* self_idx;
+  const int* cand_count;
+  const int* cand_src;
+  const uint32_t* excl_mask;
+  int maxc, nwords;
+  double* out;               // [nt][2][ntp], scaled by 1/(4 pi)
+  unsigned long long* work;  // optional: series terms, direct pairs (per target point)
+};
+
+__device__ __forceinline__ void neumaier(float& tot, float& cmp, float v) {
+  const float t = tot + v;
+  cmp += (fabsf(tot) >= fabsf(v)) ? (tot - t) + v : (v - t) + tot;
+  tot = t;
+}
+
+// One CTA per target column (blockDim = ntp rounded up to a warp multiple).
+// Dynamic shared memory: the direct-rule records of one source (ns float4).
+__global__ void __launch_bounds__(128) mp_eval_kernel(MPArgs p) {
+  extern __shared__ __align__(16) float4 drec[];
+  __shared__ MPSrc ssrc[kStage];
+  __shared__ MPMom smom[kStage][kPMax + 1];
+  __shared__ float rmax_w[32];
+  const int col = blockIdx.x, i = threadIdx.x;
+  const bool valid = i < p.ntp;
+  const float2 tl = valid ? p.tloc[(long long)col * p.ntp + i] : make_float2(0.f, 0.f);
+  const float2 thi = p.thi[col], tlo = p.tlo[col];
+  // radius of the target vesicle about its centre
+  float rt = sqrtf(tl.x * tl.x + tl.y * tl.y);
+  for (int o = 16; o > 0; o >>= 1) rt = fmaxf(rt, __shfl_xor_sync(0xffffffffu, rt, o));
+  if ((i & 31) == 0) rmax_w[i >> 5] = rt;
+  __syncthreads();
+  float RT = 0.f;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) RT = fmaxf(RT, rmax_w[w]);
+  RT *= 1.0f + 1e-6f;
+  const int self = p.self_idx ? p.self_idx[col] : -1;
+  const int cend = p.cand_count ? min(p.cand_count[col], p.maxc) : 0;
+  const int* cands = p.cand_src ? p.cand_src + (long long)col * p.maxc : nullptr;
+  int cur = 0;
+  float tot_x = 0.f, tot_y = 0.f, cmp_x = 0.f, cmp_y = 0.f;
+  unsigned long long terms = 0, ndirect = 0;  // work of this column (uniform across the CTA)
+  for (int s0 = 0; s0 < p.nsrc; s0 += kStage) {
+    const int nst = min(kStage, p.nsrc - s0);
+    __syncthreads();
+    for (int q = i; q < nst; q += blockDim.x) ssrc[q] = p.src[s0 + q];
+    for (int q = i; q < nst * (kPMax + 1); q += blockDim.x)
+      (&smom[0][0])[q] = p.mom[(long long)s0 * (kPMax + 1) + q];
+    __syncthreads();
+    for (int q = 0; q < nst; ++q) {
+      const int s = s0 + q;
+      if (s == self) continue;
+      const MPSrc S = ssrc[q];
+      // target relative to the source centre (hi/lo: no cancellation from absolute positions)
+      const float ox = (thi.x - S.chi.x) + (tlo.x - S.clo.x);
+      const float oy = (thi.y - S.chi.y) + (tlo.y - S.clo.y);
+      // near-candidate list of this column: ascending source indices
+      bool cand = false;
+      int cidx = 0;
+      if (cend > 0) {
+        while (cur < cend && cands[cur] < s) ++cur;
+        cand = cur < cend && cands[cur] == s;
+        cidx = cur;
+      }
+      const float dc = sqrtf(ox * ox + oy * oy) - RT;
+      const float rp = dc > 0.f ? S.R / dc : 2.f;
+      if (!cand && rp <= kRhoMax) {
+        // expansion of order P: rp^(P+1) / (1 - rp) <= kEps
+        int P = rp > 0.f ? (int)ceilf(__logf(kEps * (1.f - rp)) / __logf(rp)) - 1 : 1;
+        P = max(1, min(P, kPMax));
+        terms += (unsigned long long)(P + 1);
+        const float tx = tl.x + ox, ty = tl.y + oy;  // omega
+        const float om2 = fmaf(tx, tx, ty * ty);
+        const float iom2 = mufu_rcp(om2);
+        const float ur = S.R * tx * iom2, ui = -S.R * ty * iom2;  // tau = R / omega
+        float2 hA = smom[q][P].al, hB = smom[q][P].bc, hC = smom[q][P].ac, hE = smom[q][P].ec;
+        for (int k = P - 1; k >= 0; --k) {
+          const MPMom m = smom[q][k];
+          float2 n;
+          n.x = fmaf(hA.x, ur, fmaf(-hA.y, ui, m.al.x));
+          n.y = fmaf(hA.x, ui, fmaf(hA.y, ur, m.al.y));
+          hA = n;
+          n.x = fmaf(hB.x, ur, fmaf(-hB.y, ui, m.bc.x));
+          n.y = fmaf(hB.x, ui, fmaf(hB.y, ur, m.bc.y));
+          hB = n;
+          n.x = fmaf(hC.x, ur, fmaf(-hC.y, ui, m.ac.x));
+          n.y = fmaf(hC.x, ui, fmaf(hC.y, ur, m.ac.y));
+          hC = n;
+          n.x = fmaf(hE.x, ur, fmaf(-hE.y, ui, m.ec.x));
+          n.y = fmaf(hE.x, ui, fmaf(hE.y, ur, m.ec.y));
+          hE = n;
+        }
+        const float lnom = (float)kHalfLn2 * mufu_lg2(om2);  // log|omega|
+        // (omega / conj(omega)) conj(hC) and conj(tau hE)
+        const float qr = (tx * tx - ty * ty) * iom2, qi = 2.f * tx * ty * iom2;
+        const float wcr = qr * hC.x + qi * hC.y, wci = qi * hC.x - qr * hC.y;
+        const float ter = ur * hE.x - ui * hE.y, tei = -(ur * hE.y + ui * hE.x);
+        const float px = fmaf(-lnom, S.f0.x, 0.5f * S.f0.x) + hA.x + hB.x + 0.5f * (wcr - ter);
+        const float py = fmaf(-lnom, S.f0.y, 0.5f * S.f0.y) + hA.y - hB.y + 0.5f * (wci - tei);
+        if (valid) {
+          neumaier(tot_x, cmp_x, px);
+          neumaier(tot_y, cmp_y, py);
+        }
+      } else {
+        // direct rule over the upsampled points (FP32, log relative to the source centre)
+        ++ndirect;
+        __syncthreads();
+        const float4* R4 = p.rec + (long long)s * p.ns;
+        for (int j = i; j < p.ns; j += blockDim.x) drec[j] = R4[j];
+        __syncthreads();
+        bool excl = false;
+        if (cand && valid) {
+          const uint32_t w = p.excl_mask[((long long)col * p.maxc + cidx) * p.nwords + (i >> 5)];
+          excl = (w >> (i & 31)) & 1u;
+        }
+        const float tx = tl.x + ox, ty = tl.y + oy;
+        const float rc2 = fmaf(tx, tx, ty * ty);
+        const float irc2 = mufu_rcp(rc2);
+        float acx = 0.f, acy = 0.f, alx = 0.f, aly = 0.f;
+#pragma unroll 4
+        for (int j = 0; j < p.ns; ++j) {
+          const float4 r = drec[j];
+          const float dx = tx - r.x, dy = ty - r.y;
+          const float r2 = fmaf(dx, dx, dy * dy);
+          const float inv = mufu_rcp(r2);
+          const float lg = mufu_lg2(r2 * irc2);
+          const float cc = fmaf(dx, r.z, dy * r.w) * inv;
+          acx = fmaf(cc, dx, acx);
+          acy = fmaf(cc, dy, acy);
+          alx = fmaf(lg, r.z, alx);
+          aly = fmaf(lg, r.w, aly);
+        }
+        if (valid && !excl) {
+          const float lgc = mufu_lg2(rc2);
+          const float px = acx - (float)kHalfLn2 * fmaf(lgc, S.f0.x, alx);
+          const float py = acy - (float)kHalfLn2 * fmaf(lgc, S.f0.y, aly);
+          neumaier(tot_x, cmp_x, px);
+          neumaier(tot_y, cmp_y, py);
+        }
+      }
+    }
+  }
+  if (p.work && i == 0) {
+    atomicAdd(&p.work[0], terms * (unsigned long long)p.ntp);
+    atomicAdd(&p.work[1], ndirect * (unsigned long long)p.ntp * (unsigned long long)p.ns);
+  }
+  if (valid) {
+    const double scale = 1.0 / (4.0 * VES_PI);
+    p.out[(long long)col * 2 * p.ntp + i] = ((double)tot_x + (double)cmp_x) * scale;
+    p.out[(long long)col * 2 * p.ntp + p.ntp + i] = ((double)tot_y + (double)cmp_y) * scale;
+  }
+}
+
+}  // namespace
+
+int farfield_mp_run(const FFEnv& env, int nsrc, int ns, const double* Xsrc, const double* den, int nt, int ntp,
+                    const double* Xtar, const int* self_idx, const ves_near_lists* nl, double* out, WsCarver& ws,
+                    cudaStream_t s) {
+  const long long total_pts = (long long)nt * ntp;
+  float4* rec = ws.take<float4>((size_t)nsrc * ns);
+  MPSrc* src = ws.take<MPSrc>(nsrc);
+  MPMom* mom = ws.take<MPMom>((size_t)nsrc * (kPMax + 1));
+  float2* tloc = ws.take<float2>((size_t)total_pts);
+  float2* thi = ws.take<float2>(nt);
+  float2* tlo = ws.take<float2>(nt);
+  if (ws.sizing) return VES_OK;
+  if (!ws.ok()) {
+    ves_record_error(VES_ERR_WORKSPACE, "farfield: workspace too small");
+    return VES_ERR_WORKSPACE;
+  }
+  if (total_pts == 0) return VES_OK;
+  if (nsrc == 0) return ves_cuda_status(cudaMemsetAsync(out, 0, (size_t)total_pts * 2 * sizeof(double), s), "ff zero");
+  if (ntp > 128) {
+    ves_record_error(VES_ERR_SHAPE, "farfield: the multipole path takes at most 128 points per target column");
+    return VES_ERR_SHAPE;
+  }
+  if (nl && ntp != env.N) {
+    ves_record_error(VES_ERR_SHAPE, "farfield: near lists need N target points per column");
+    return VES_ERR_SHAPE;
+  }
+  const size_t dsmem = (size_t)ns * sizeof(float4);
+  if (dsmem > 160 * 1024) {
+    ves_record_error(VES_ERR_SHAPE, "farfield: %d source points per vesicle exceed the multipole path", ns);
+    return VES_ERR_SHAPE;
+  }
+  ves_count_launch(2);
+  mp_prep_kernel<<<nsrc, 256, 0, s>>>(ns, Xsrc, den, rec, src, mom);
+  mp_prep_targets_kernel<<<nt, 256, 0, s>>>(ntp, Xtar, tloc, thi, tlo);
+  MPArgs a;
+  a.nsrc = nsrc;
+  a.ns = ns;
+  a.ntp = ntp;
+  a.rec = rec;
+  a.src = src;
+  a.mom = mom;
+  a.tloc = tloc;
+  a.thi = thi;
+  a.tlo = tlo;
+  a.self_idx = self_idx;
+  a.cand_count = nl ? nl->cand_count : nullptr;
+  a.cand_src = nl ? nl->cand_src : nullptr;
+  a.excl_mask = nl ? nl->excl_mask : nullptr;
+  a.maxc = nl ? nl->maxc : 0;
+  a.nwords = (env.N + 31) / 32;
+  a.out = out;
+  a.work = (env.timing && env.timing->timing) ? env.timing->d_mp : nullptr;
+  if (dsmem > 32 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(mp_eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem);
+    if (e != cudaSuccess) return ves_cuda_status(e, "farfield multipole smem attribute");
+  }
+  const int threads = ((ntp + 31) / 32) * 32;
+  ves_count_launch();
+  if (env.timing) ves_ff_timing_begin(env.timing, s);
+  mp_eval_kernel<<<nt, threads, dsmem, s>>>(a);
+  if (env.timing) ves_ff_timing_end(env.timing, s, (double)total_pts * ns * (double)nsrc);
+  return ves_launch_check("farfield multipole");
+}

@@ -46,6 +46,13 @@ struct ves_ctx {
   double ev_pairs[256];
   long long ff_launches;
   double ff_ms, ff_pairs;
+  unsigned long long* d_mp;  // multipole path work counters (device, 2), allocated with timing
+  // optional timing of the network forward passes (MLARM step)
+  int n_nev;
+  cudaEvent_t nev[2 * 64];
+  double nev_flops[64];
+  long long net_launches;
+  double net_ms, net_flops;
 };
 
 // launch accounting (every kernel launch site calls ves_count_launch)
@@ -53,6 +60,9 @@ void ves_count_launch(int n = 1);
 // all-pairs kernel timing hooks (no-ops unless timing is on)
 void ves_ff_timing_begin(ves_ctx* c, cudaStream_t s);
 void ves_ff_timing_end(ves_ctx* c, cudaStream_t s, double pairs);
+// network forward timing hooks (no-ops unless timing is on); flops = useful work of the pass
+void ves_net_timing_begin(ves_ctx* c, cudaStream_t s);
+void ves_net_timing_end(ves_ctx* c, cudaStream_t s, double flops);
 
 // status plumbing -----------------------------------------------------------
 int ves_reset_status(ves_ctx* ctx, cudaStream_t s);
@@ -121,11 +131,15 @@ int alpert_sl_matrix(ves_ctx* c, int nv, const double* X, int precision, double*
 struct FFEnv {
   VesDeviceStatus* status;
   int N;
-  ves_ctx* timing;
+  ves_ctx* timing;  // context whose timing hooks and counters record the launch (may be null)
 };
 int farfield_run_env(const FFEnv& env, int precision, int nsrc, int ns, const double* Xsrc, const double* den,
                      int nt, int ntp, const double* Xtar, const int* self_idx, const ves_near_lists* nl,
                      double* out, WsCarver& ws, cudaStream_t s);
+// multipole expansion for separated vesicle pairs, direct FP32 sum for the rest (VES_PREC_FP32M)
+int farfield_mp_run(const FFEnv& env, int nsrc, int ns, const double* Xsrc, const double* den, int nt, int ntp,
+                    const double* Xtar, const int* self_idx, const ves_near_lists* nl, double* out, WsCarver& ws,
+                    cudaStream_t s);
 int farfield_run(ves_ctx* c, int precision, int nsrc, int ns, const double* Xsrc, const double* den,
                  int nt, int ntp, const double* Xtar, const int* self_idx, const ves_near_lists* nl,
                  double* out, WsCarver& ws, cudaStream_t s);

@@ -28,6 +28,7 @@
 int net_forward_run(const ves_net* net, int nv, const void* in, void* out, WsCarver& ws, VesDeviceStatus* st,
                     cudaStream_t s);
 int net_dims(const ves_net* net, int* groups, int* length, int* cin, int* cout);
+double net_flops_per_vesicle(const ves_net* net);
 
 namespace {
 
@@ -726,7 +727,9 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
     prep_modes_kernel<Real><<<ceil_div((long long)nv * kNearModes * 2 * N, 256), 256, 0, s>>>(nv, N, kNearModes, Xs,
                                                                                              m->near_in, nin);
     WsCarver w = sub();
+    ves_net_timing_begin(c, s);
     if ((rc = net_forward_run(m->near, nv, nin, nout, w, c->status, s))) return rc;
+    ves_net_timing_end(c, s, net_flops_per_vesicle(m->near) * nv);
   }
   // near pairs (compare1 :429-536): target points of a vesicle closer than 1/N
   // to an upsampled point of another vesicle
@@ -755,13 +758,17 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
                                                                                        m->advten_in, nin);
   {
     WsCarver w = sub();
+    ves_net_timing_begin(c, s);
     if ((rc = net_forward_run(m->advten, nv, nin, nout, w, c->status, s))) return rc;
+    ves_net_timing_end(c, s, net_flops_per_vesicle(m->advten) * nv);
   }
   ves_count_launch();
   prep_xy_kernel<Real><<<gb, 256, 0, s>>>(nv, N, Xs, m->selften_in, nin);
   {
     WsCarver w = sub();
+    ves_net_timing_begin(c, s);
     if ((rc = net_forward_run(m->selften, nv, nin, nout2, w, c->status, s))) return rc;
+    ves_net_timing_end(c, s, net_flops_per_vesicle(m->selften) * nv);
   }
   ves_count_launch();
   tension_kernel<Real><<<nv, 128, (size_t)4 * N * sizeof(double), s>>>(
@@ -780,7 +787,9 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
   prep_adv_kernel<Real><<<ceil_div((long long)nv * kModes * 2 * 2 * N, 256), 256, 0, s>>>(nv, N, Xs, m->adv_in, nin);
   {
     WsCarver w = sub();
+    ves_net_timing_begin(c, s);
     if ((rc = net_forward_run(m->adv, nv, nin, nout, w, c->status, s))) return rc;
+    ves_net_timing_end(c, s, net_flops_per_vesicle(m->adv) * nv);
   }
   ves_count_launch();
   translate_kernel<Real><<<nv, 128, (size_t)6 * N * sizeof(double), s>>>(N, prm->dt, X, vsum, rot, sidx, nout,
@@ -797,7 +806,9 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
   prep_xy_kernel<Real><<<gb, 256, 0, s>>>(nv, N, Xs2, m->relax_in, nin);
   {
     WsCarver w = sub();
+    ves_net_timing_begin(c, s);
     if ((rc = net_forward_run(m->relax, nv, nin, nout, w, c->status, s))) return rc;
+    ves_net_timing_end(c, s, net_flops_per_vesicle(m->relax) * nv);
   }
   ves_count_launch();
   relax_post_kernel<Real><<<nv, 128, 0, s>>>(N, prm->dt, Xs2, nout, m->relax_out, scal2, rot2, rotc2, trn2, sidx2, Xa);
@@ -965,7 +976,8 @@ extern "C" int ves_mlarm_step(ves_mlarm* m, const ves_mlarm_params* prm, int nv,
     ves_record_error(VES_ERR_ARG, "mlarm_step: bad arguments");
     return VES_ERR_ARG;
   }
-  if (prm->farfield_precision != VES_PREC_FP64 && prm->farfield_precision != VES_PREC_FP32C) {
+  if (prm->farfield_precision != VES_PREC_FP64 && prm->farfield_precision != VES_PREC_FP32C &&
+      prm->farfield_precision != VES_PREC_FP32M) {
     ves_record_error(VES_ERR_ARG, "mlarm_step: bad far-field precision");
     return VES_ERR_ARG;
   }

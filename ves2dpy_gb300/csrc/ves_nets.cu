@@ -316,6 +316,19 @@ int net_forward_run(const ves_net* net, int nv, const void* in, void* out, WsCar
   return net_forward_t<float>(net, nv, (const float*)in, (float*)out, ws, st, s);
 }
 
+// useful work of one vesicle through the network: 2 x multiply-adds of the
+// conv pairs, the two transposed convs (5 taps per output) and the mix
+double net_flops_per_vesicle(const ves_net* net) {
+  const double L = net->length;
+  double f = 0;
+  for (const BlockGeom& b : net->blocks) {
+    const double d = 2.0 * b.c2;
+    f += 2 * (L / 2) * b.c1 * b.cin * 7 + 2 * (L / 4) * b.c2 * 2 * b.c1 * 7;
+    f += (L / 2) * d * d * 5 + L * d * d * 5 + L * b.cmix * d * 3;
+  }
+  return 2.0 * f * net->groups;
+}
+
 int net_dims(const ves_net* net, int* groups, int* length, int* cin, int* cout) {
   if (groups) *groups = net->groups;
   if (length) *length = net->length;

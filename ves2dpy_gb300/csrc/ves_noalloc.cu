@@ -58,7 +58,7 @@ extern "C" int ves_farfield_static_scratch(int precision, int nsrc, int ns, cons
     ves_record_error(VES_ERR_ARG, "ves_farfield_static_scratch: bad arguments");
     return VES_ERR_ARG;
   }
-  if (precision != VES_PREC_FP64 && precision != VES_PREC_FP32C) {
+  if (precision != VES_PREC_FP64 && precision != VES_PREC_FP32C && precision != VES_PREC_FP32M) {
     ves_record_error(VES_ERR_ARG, "ves_farfield_static_scratch: bad precision %d", precision);
     return VES_ERR_ARG;
   }

@@ -310,12 +310,17 @@ __device__ __forceinline__ Seg next_seg(long long lo, long long hi, int nv) {
   return {lo, end < hi ? end : hi, grp};
 }
 
+// KC1 / KCD: compile-time K chunk counts of the two conv pairs' outputs (0:
+// read them from the geometry); fixed counts let every epilogue and issue
+// loop unroll.
+template <int KC1, int KCD>
 __global__ void __launch_bounds__(kThreads, 1) down_kernel(KArgs a) {
   extern __shared__ __align__(128) unsigned char sm[];
   __shared__ uint64_t bar[2], xbar[2];  // per warp group: MMA completion, input arrival
   __shared__ uint32_t tbase;
   __shared__ int fail[2];
   const Geo& g = a.g;
+  const int kc1 = KC1 ? KC1 : kc1, kcd = KCD ? KCD : kcd;
   const int L = g.L, L2 = L / 2, L4 = L / 4;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int wg = tid / kGroupThreads, gt = tid % kGroupThreads;  // warp group, thread within it
@@ -337,7 +342,7 @@ __global__ void __launch_bounds__(kThreads, 1) down_kernel(KArgs a) {
   tc_fence_before_sync();
   __syncthreads();
   tc_fence_after_sync();
-  const int N1 = g.kc1 * 8, N2 = g.kcd * 8;
+  const int N1 = kc1 * 8, N2 = kcd * 8;
   const uint32_t tcol = tbase + 256 * wg;
   const uint32_t d1 = tcol, d2 = tcol + N1;
   const uint32_t sbase = tc_smem_u32(sm);
@@ -428,15 +433,16 @@ __global__ void __launch_bounds__(kThreads, 1) down_kernel(KArgs a) {
       if (32 * qd < L2) {
         const int p = 32 * qd + lane;
         const int par = p & 1, q = p >> 1;
-        for (int k0 = 0; k0 < g.kc1; k0 += 4) {
+#pragma unroll
+        for (int k0 = 0; k0 < kc1; k0 += 4) {
           float vv[32];
           tc_ld32(d1 + ((uint32_t)(32 * qd) << 16) + 8 * k0, vv);
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
             const int kc = k0 + k;
-            if (kc >= g.kc1) break;
+            if (kc >= kc1) break;
             const uint4 val = act8(vv + 8 * k, cst, kc, g.n1, 0, 128, 256);
-            uint4* base = as + (size_t)(par * g.kc1 + kc) * P2;
+            uint4* base = as + (size_t)(par * kc1 + kc) * P2;
             base[q + 3] = val;
             if (q >= L4 - 3) base[q + 3 - L4] = val;
             if (q < 3) base[q + 3 + L4] = val;
@@ -449,8 +455,8 @@ __global__ void __launch_bounds__(kThreads, 1) down_kernel(KArgs a) {
         const uint32_t idesc = tc_idesc_bf16(128, N2);
         const uint32_t lboA = P2 * 16, lboB = g.d * 16;
         const uint64_t a0 = tc_desc(sbase + g.das + goff, lboA, 128), b0 = tc_desc(sbase + g.dw2, lboB, 128);
-#define VES_CONV2(NK) issue_conv<NK>(d2, a0, b0, (g.kc1 * lboA) >> 4, (g.kc1 * lboB) >> 4, (2 * lboA) >> 4, (2 * lboB) >> 4, idesc)
-        VES_TC_NK_SWITCH(g.kc1 / 2, VES_CONV2)
+#define VES_CONV2(NK) issue_conv<NK>(d2, a0, b0, (kc1 * lboA) >> 4, (kc1 * lboB) >> 4, (2 * lboA) >> 4, (2 * lboB) >> 4, idesc)
+        VES_TC_NK_SWITCH(kc1 / 2, VES_CONV2)
 #undef VES_CONV2
         tc_commit(&bar[wg]);
       }
@@ -462,12 +468,13 @@ __global__ void __launch_bounds__(kThreads, 1) down_kernel(KArgs a) {
       tc_fence_after_sync();
       if (32 * qd < L4) {
         const int p = 32 * qd + lane;
-        for (int k0 = 0; k0 < g.kcd; k0 += 4) {
+#pragma unroll
+        for (int k0 = 0; k0 < kcd; k0 += 4) {
           float vv[32];
           tc_ld32(d2 + ((uint32_t)(32 * qd) << 16) + 8 * k0, vv);
 #pragma unroll
           for (int k = 0; k < 4; ++k)
-            if (k0 + k < g.kcd) stage[(size_t)(k0 + k) * L4 + p] = act8(vv + 8 * k, cst, k0 + k, g.d, 384, 512, 640);
+            if (k0 + k < kcd) stage[(size_t)(k0 + k) * L4 + p] = act8(vv + 8 * k, cst, k0 + k, g.d, 384, 512, 640);
         }
       }
       tc_fence_before_sync();
@@ -487,12 +494,15 @@ __global__ void __launch_bounds__(kThreads, 1) down_kernel(KArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// KCD: compile-time K chunk count of the transposed convs (0: from the geometry)
+template <int KCD>
 __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
   extern __shared__ __align__(128) unsigned char sm[];
   __shared__ uint64_t bar[2], mbar[2], rbar[2];  // per warp group: MMA completion, intermediate, block input
   __shared__ uint32_t tbase;
   __shared__ int fail[2];
   const Geo& g = a.g;
+  const int kcd = KCD ? KCD : kcd;
   const int L = g.L, L2 = L / 2, L4 = L / 4;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int wg = tid / kGroupThreads, gt = tid % kGroupThreads;
@@ -520,7 +530,7 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
   const int goff = wg * g.ugrp;
   const float* cst = reinterpret_cast<const float*>(sm + g.ucst);
   const int PB = L4 + 4, PC = L2 + 4, PD = L + 2;
-  const int Nd = g.kcd * 8, Nm = rup(g.cmix, 16);
+  const int Nd = kcd * 8, Nm = rup(g.cmix, 16);
   const int cout = g.cmix + g.npass;
   const int nh = L / 128;      // 128-position halves of the mix
   const int mcol = 2 * Nd;     // first TMEM column of the mix accumulators (after the transposed convs')
@@ -539,7 +549,7 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
       const long long v = item % a.nv;
       const unsigned char* src = a.mid + ((size_t)v * a.G + grp) * g.mid_bytes;
       tc_expect_tx(&mbar[wg], (uint32_t)g.mid_bytes);
-      for (int kc = 0; kc < g.kcd; ++kc) tc_bulk_g2s(bs + kc * PB + 2, src + kc * L4 * 16, L4 * 16, &mbar[wg]);
+      for (int kc = 0; kc < kcd; ++kc) tc_bulk_g2s(bs + kc * PB + 2, src + kc * L4 * 16, L4 * 16, &mbar[wg]);
     }
     mpend = true;
   };
@@ -558,7 +568,7 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
       const uint32_t lboB = 2 * Nd * 16;
       const uint64_t a0 = tc_desc(sbase + a_off, lboA, 128), b0 = tc_desc(sbase + up_w_off(g, layer, 0, 0, 0, 0), lboB, 128);
 #define VES_DEC(NK) issue_deconv<NK>(dt, a0, b0, bTap, stepA, (2 * lboB) >> 4, idesc)
-      VES_TC_NK_SWITCH(g.kcd / 2, VES_DEC)
+      VES_TC_NK_SWITCH(kcd / 2, VES_DEC)
 #undef VES_DEC
     } else {
       const uint32_t idesc = tc_idesc_bf16(128, Nd);
@@ -568,7 +578,7 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
         const uint64_t a0 = tc_desc(sbase + a_off - lift, lboA, 128);
         const uint64_t b0 = tc_desc(sbase + up_w_off(g, layer, r, 0, 0, 0), lboB, 128);
 #define VES_DEC(NK) issue_deconv<NK>(dt + r * Nd, a0, b0, bTap, stepA, (2 * lboB) >> 4, idesc)
-        VES_TC_NK_SWITCH(g.kcd / 2, VES_DEC)
+        VES_TC_NK_SWITCH(kcd / 2, VES_DEC)
 #undef VES_DEC
       }
     }
@@ -579,6 +589,7 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
   auto deconv_epi = [&](int npos, uint4* dst, int pitch, int row0, int ob, int os, int ot) {
     const bool msplit = 2 * npos <= 128;
     const int lane0 = 32 * qd;
+#pragma unroll
     for (int r = 0; r < 2; ++r) {
       int q;
       if (msplit) {
@@ -588,12 +599,13 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
         if (lane0 >= npos) continue;
         q = lane0 + lane;
       }
-      for (int k0 = 0; k0 < g.kcd; k0 += 4) {
+#pragma unroll
+      for (int k0 = 0; k0 < kcd; k0 += 4) {
         float vv[32];
         tc_ld32(dt + ((uint32_t)lane0 << 16) + r * Nd + 8 * k0, vv);
 #pragma unroll
         for (int k = 0; k < 4; ++k)
-          if (k0 + k < g.kcd)
+          if (k0 + k < kcd)
             dst[(size_t)(k0 + k) * pitch + 2 * q + r + row0] = act8(vv + 8 * k, cst, k0 + k, g.d, ob, os, ot);
       }
     }
@@ -674,7 +686,7 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
       tc_fence_after_sync();
       deconv_epi(L2, ds, PD, 1, 384, 512, 640);
       // the halo rows of ds (zero padding of the mix) held block input
-      if (gt < 2 * g.kcd) ds[(gt >> 1) * PD + ((gt & 1) ? L + 1 : 0)] = make_uint4(0, 0, 0, 0);
+      if (gt < 2 * kcd) ds[(gt >> 1) * PD + ((gt & 1) ? L + 1 : 0)] = make_uint4(0, 0, 0, 0);
       group_sync_for_mma(wg);
       // mix: D[p][o] = sum_t d[p + t - 1] M_t; positions in halves of 128 rows
       if (gt == 0) {
@@ -682,8 +694,8 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
         const uint32_t lboA = PD * 16, lboB = g.cmix * 16;
         const uint64_t a0 = tc_desc(sbase + g.uds + goff, lboA, 128), b0 = tc_desc(sbase + g.uwm, lboB, 128);
         for (int h = 0; h < nh; ++h) {  // onto residual + bias
-#define VES_MIX(NK) issue_mix<NK>(dt + mcol + h * Nm, a0 + (uint32_t)(128 * h), b0, (g.kcd * lboB) >> 4, (2 * lboA) >> 4, (2 * lboB) >> 4, idesc)
-          VES_TC_NK_SWITCH(g.kcd / 2, VES_MIX)
+#define VES_MIX(NK) issue_mix<NK>(dt + mcol + h * Nm, a0 + (uint32_t)(128 * h), b0, (kcd * lboB) >> 4, (2 * lboA) >> 4, (2 * lboB) >> 4, idesc)
+          VES_TC_NK_SWITCH(kcd / 2, VES_MIX)
 #undef VES_MIX
         }
         tc_commit(&bar[wg]);
@@ -878,20 +890,28 @@ int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_dow
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  int rc = ves_cuda_status(cudaFuncSetAttribute(down_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, std::max(tb.dsmem, kMinSmem)),
-                           "tc down smem");
-  if (rc) return rc;
-  rc = ves_cuda_status(cudaFuncSetAttribute(up_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, std::max(tb.usmem, kMinSmem)),
-                       "tc up smem");
-  if (rc) return rc;
+  // compiled chunk-count variants; others run the generic kernels
+  void (*dk)(KArgs) = down_kernel<0, 0>;
+  void (*uk)(KArgs) = up_kernel<0>;
+  const int kc1 = a.g.kc1, kcd = a.g.kcd;
+  if (kc1 == 4 && kcd == 6) dk = down_kernel<4, 6>;
+  if (kc1 == 6 && kcd == 6) dk = down_kernel<6, 6>;
+  if (kc1 == 6 && kcd == 8) dk = down_kernel<6, 8>;
+  if (kc1 == 8 && kcd == 8) dk = down_kernel<8, 8>;
+  if (kcd == 6) uk = up_kernel<6>;
+  if (kcd == 8) uk = up_kernel<8>;
   // one CTA per SM (it allocates all 512 TMEM columns): at least 117 KB of
   // shared memory per CTA keeps a second one off the SM
   const int dsm = std::max(tb.dsmem, kMinSmem), usm = std::max(tb.usmem, kMinSmem);
+  int rc = ves_cuda_status(cudaFuncSetAttribute(dk, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm), "tc down smem");
+  if (rc) return rc;
+  rc = ves_cuda_status(cudaFuncSetAttribute(uk, cudaFuncAttributeMaxDynamicSharedMemorySize, usm), "tc up smem");
+  if (rc) return rc;
   const int grid = (int)std::min<long long>(a.items, (long long)nsm);
   a.img = d_down;
   ves_count_launch(2);
-  down_kernel<<<grid, kThreads, dsm, s>>>(a);
+  dk<<<grid, kThreads, dsm, s>>>(a);
   a.img = d_up;
-  up_kernel<<<grid, kThreads, usm, s>>>(a);
+  uk<<<grid, kThreads, usm, s>>>(a);
   return ves_launch_check("tc net block");
 }

@@ -29,9 +29,10 @@
 // pair on the target's near-candidate list (where single target points are
 // excluded, biem_support.py:218-219), is summed directly over the
 // upsampled points in FP32 with the source-centred logarithm of the FP32C
-// path.  The moments are FP64 sums over exactly the upsampled points of the
-// direct rule, rounded to FP32; the series are evaluated in FP32 (Horner) and
-// the per-source contributions are added with Neumaier compensation.
+// path.  The moments are sums over exactly the upsampled points of the direct
+// rule (centre, radius and F0 in FP64, the others in FP32, stored in FP32);
+// the series are evaluated in FP32 (Horner) and the per-source contributions
+// are added with Neumaier compensation.
 #include "ves_internal.h"
 
 namespace {
@@ -54,8 +55,8 @@ struct __align__(16) MPMom {
   float2 al, bc, ac, ec;
 };
 
-__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
-  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
 
 // ---------------------------------------------------------------------------
@@ -116,34 +117,38 @@ __global__ void __launch_bounds__(256) mp_prep_kernel(int ns, const double* __re
     o.pad = 0.f;
     src[s] = o;
   }
-  // moments: warp w takes orders k = w, w + 8, w + 16, ... (<= kPMax); lanes split the points
+  // moments: warp w takes orders k = w, w + 8, w + 16, ... (<= kPMax); lanes
+  // split the points.  FP32 sums: a moment of order k enters the series
+  // multiplied by rho^k and is stored in FP32, so FP32 accumulation (errors
+  // of a few 1e-8 of sum |f| |v|^k) matches the storage; the monopole F0 is
+  // the FP64 density sum above.
   const int warp = t >> 5, lane = t & 31;
   constexpr int kPer = (kPMax + 8) / 8;  // orders per warp
-  double2 A[kPer], B[kPer], E[kPer];
+  float2 A[kPer], B[kPer], E[kPer];
 #pragma unroll
-  for (int q = 0; q < kPer; ++q) A[q] = B[q] = E[q] = make_double2(0, 0);
+  for (int q = 0; q < kPer; ++q) A[q] = B[q] = E[q] = make_float2(0.f, 0.f);
   const double iR = 1.0 / R;
   for (int j = lane; j < ns; j += 32) {
-    const double2 v = make_double2((x[j] - cx) * iR, (x[ns + j] - cy) * iR);
-    const double2 fj = make_double2(f[j], f[ns + j]);
-    double2 pw = make_double2(1, 0), v8 = v;  // pw = v^warp, v8 = v^8
-    for (int e = 0; e < warp; ++e) pw = cmul(pw, v);
-    v8 = cmul(v8, v8);
-    v8 = cmul(v8, v8);
-    v8 = cmul(v8, v8);
-    const double2 fvb = cmul(fj, make_double2(v.x, -v.y));  // f conj(v)
+    const float2 v = make_float2((float)((x[j] - cx) * iR), (float)((x[ns + j] - cy) * iR));
+    const float2 fj = make_float2((float)f[j], (float)f[ns + j]);
+    float2 pw = make_float2(1.f, 0.f), v8 = v;  // pw = v^warp, v8 = v^8
+    for (int e = 0; e < warp; ++e) pw = cmulf(pw, v);
+    v8 = cmulf(v8, v8);
+    v8 = cmulf(v8, v8);
+    v8 = cmulf(v8, v8);
+    const float2 fvb = cmulf(fj, make_float2(v.x, -v.y));  // f conj(v)
 #pragma unroll
     for (int q = 0; q < kPer; ++q) {
-      const double2 a = cmul(fj, pw);
-      const double2 b = cmul(fj, make_double2(pw.x, -pw.y));
-      const double2 e = cmul(fvb, pw);
+      const float2 a = cmulf(fj, pw);
+      const float2 b = cmulf(fj, make_float2(pw.x, -pw.y));
+      const float2 e = cmulf(fvb, pw);
       A[q].x += a.x;
       A[q].y += a.y;
       B[q].x += b.x;
       B[q].y += b.y;
       E[q].x += e.x;
       E[q].y += e.y;
-      pw = cmul(pw, v8);
+      pw = cmulf(pw, v8);
     }
   }
 #pragma unroll
@@ -159,11 +164,11 @@ __global__ void __launch_bounds__(256) mp_prep_kernel(int ns, const double* __re
     const int k = warp + 8 * q;
     if (lane == 0 && k <= kPMax) {
       MPMom m;
-      const double h = k > 0 ? 0.5 / k : 0.0;
-      m.al = make_float2((float)(A[q].x * h), (float)(A[q].y * h));
-      m.bc = make_float2((float)(B[q].x * h), (float)(-B[q].y * h));
-      m.ac = make_float2((float)A[q].x, (float)A[q].y);
-      m.ec = make_float2((float)E[q].x, (float)E[q].y);
+      const float h = k > 0 ? 0.5f / k : 0.f;
+      m.al = make_float2(A[q].x * h, A[q].y * h);
+      m.bc = make_float2(B[q].x * h, -B[q].y * h);
+      m.ac = k > 0 ? A[q] : make_float2((float)red[1][0], (float)red[2][0]);  // A_0 = F0 (FP64 sum)
+      m.ec = E[q];
       mom[(long long)s * (kPMax + 1) + k] = m;
     }
   }

@@ -374,6 +374,27 @@ VES_API int ves_farfield_static_scratch(int precision, int nsrc, int ns, const d
                                         int nt, int ntp, const double* Xtar, const int* self_idx, double* out,
                                         void* stream);
 
+/* ---- trajectory files ------------------------------------------------------
+ * The reference's binary trajectory format (driver_confined.py:204-206,
+ * 294-296; reader newtorch/tools/load_ves2d_file.py:4-72): little-endian
+ * float64; N, nv, the initial shapes, then per frame the time and the shapes.
+ * Shapes are vesicle by vesicle, N x then N y coordinates: X.T.flatten() of
+ * the reference's X[2N, nv] = this library's device layout [nv][2][N]. */
+typedef struct ves_traj ves_traj;
+/* Create (truncate) ``path`` and write the header and the initial shapes X0
+ * ([nv][2][N], on the device when x0_on_device != 0).  ``nslots`` pinned frame
+ * buffers (0: 3) decouple the step from the disk. */
+VES_API int ves_traj_create(const char* path, int N, int nv, const double* X0, int x0_on_device, int nslots,
+                            ves_traj** out);
+/* Queue one frame: ``time`` and X ([nv][2][N]).  A device X is copied
+ * asynchronously on ``stream`` (it must stay unchanged until that copy has run
+ * in stream order); a background thread writes frames in order.  Returns the
+ * first earlier write failure, if any. */
+VES_API int ves_traj_append(ves_traj* t, double time, const double* X, int on_device, void* stream);
+/* Wait until every queued frame is written and flushed; frames written so far. */
+VES_API int ves_traj_flush(ves_traj* t, long long* frames_written);
+VES_API int ves_traj_close(ves_traj* t);
+
 /* ---- measurement utilities (no counterpart in the reference) -------------- */
 typedef struct ves_stats {
   long long kernel_launches;  /* kernels launched through this library (all contexts) */

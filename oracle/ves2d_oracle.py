@@ -89,6 +89,69 @@ def geom_prop(X):
     return 4 * np.pi * area / length ** 2, area, length
 
 
+def ellipse(N: int, ra: float):
+    """Ellipse of reduced area ra with N points (curve_batch_compile.py:494-527),
+    including the reference's switch from (a cos t, sin t) to (cos t, a sin t)
+    and from a 1e-4 relative to a 1e-2 absolute acceptance after the first try."""
+    t = np.arange(N) * 2 * np.pi / N
+    a = (1 - np.sqrt(1 - ra ** 2)) / ra
+    X0 = np.concatenate((a * np.cos(t), np.sin(t)))[:, None]
+    ra_new = geom_prop(X0)[0][0]
+    cond = abs(ra_new - ra) / ra < 1e-4
+    it = 0
+    while not cond and it < 10:
+        it += 1
+        a = a * 0.9 if ra_new > ra else a * 1.05
+        X0 = np.concatenate((np.cos(t), a * np.sin(t)))[:, None]
+        ra_new = geom_prop(X0)[0][0]
+        cond = abs(ra_new - ra) < 1e-2
+    return X0
+
+
+def write_trajectory(filename, X0, frames):
+    """Trajectory bytes as the drivers write them: header and initial shapes
+    (driver_confined.py:204-206), then one (time, shapes) record per step
+    (:294-296); X arrays in the reference layout [2N, nv]."""
+    N, nv = X0.shape[0] // 2, X0.shape[1]
+    with open(filename, 'wb') as fid:
+        np.array([N, nv]).flatten().astype('float64').tofile(fid)
+        np.asarray(X0).T.flatten().astype('float64').tofile(fid)
+    for time_, X in frames:
+        output = np.concatenate(([time_], np.asarray(X).T.flatten())).astype('float64')
+        with open(filename, 'ab') as fid:
+            output.tofile(fid)
+
+
+def load_ves2d_file(filename):
+    """Reader of the trajectory format (newtorch/tools/load_ves2d_file.py:4-72),
+    element by element as there."""
+    val = np.fromfile(filename, dtype=np.float64)
+    N, nv = int(val[0]), int(val[1])
+    n_init = 2 * N * nv
+    Xinit = val[2:2 + n_init]
+    xinit, yinit = np.zeros((N, nv)), np.zeros((N, nv))
+    istart = 0
+    for iv in range(nv):
+        xinit[:, iv] = Xinit[istart:istart + N]
+        istart += N
+        yinit[:, iv] = Xinit[istart:istart + N]
+        istart += N
+    val = val[2 + n_init:]
+    stride = 2 * N * nv + 1
+    ntime = val.size // stride
+    vesx, vesy, time = np.zeros((N, nv, ntime)), np.zeros((N, nv, ntime)), np.zeros(ntime)
+    istart = 0
+    for it in range(ntime):
+        time[it] = val[istart]
+        istart += 1
+        for iv in range(nv):
+            vesx[:, iv, it] = val[istart:istart + N]
+            istart += N
+            vesy[:, iv, it] = val[istart:istart + N]
+            istart += N
+    return vesx, vesy, time, N, nv, xinit, yinit
+
+
 def interpft(x, N_new: int):
     """Fourier resampling along axis 0 (filter.py:221-249)."""
     N = x.shape[0]

@@ -375,7 +375,45 @@ def job_nets(precision):
     return out
 
 
+def job_io(promote):
+    """Geometry and trajectory tooling: ``Curve.ellipse`` (curve_batch_compile.py:494-527)
+    and ``load_ves2d_file`` (newtorch/tools/load_ves2d_file.py:4-72) reading a file
+    written with the drivers' statements (driver_confined.py:204-206, 294-296)."""
+    import importlib.util
+    import tempfile
+    import ref_shim
+    R = ref_shim.load(promote=promote)
+    torch = R.torch
+    oc = R.curve.Curve()
+    out = {}
+    for N, ra in ((32, 0.65), (64, 0.9), (128, 0.5), (16, 0.75)):
+        out[f"ellipse_{N}_{int(round(ra * 100))}"] = _np(oc.ellipse(N, torch.tensor([ra])))
+    rng = np.random.default_rng(5)
+    N, nv = 16, 3
+    X0 = rng.normal(size=(2 * N, nv))
+    frames = [(1e-5 * (k + 1), rng.normal(size=(2 * N, nv))) for k in range(4)]
+    path = os.path.join(tempfile.mkdtemp(), "traj.bin")
+    with open(path, 'wb') as fid:
+        np.array([N, nv]).flatten().astype('float64').tofile(fid)
+        X0.T.flatten().astype('float64').tofile(fid)
+    for time_, X in frames:
+        output = np.concatenate(([time_], X.T.flatten())).astype('float64')
+        with open(path, 'ab') as fid:
+            output.tofile(fid)
+    spec = importlib.util.spec_from_file_location(
+        "load_ves2d_file", os.path.join(ref_shim.REF_ROOT, "newtorch", "tools", "load_ves2d_file.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    vesx, vesy, time_, Nr, nvr, xinit, yinit = mod.load_ves2d_file(path)
+    out.update({"traj_bytes": np.fromfile(path, dtype=np.uint8), "traj_X0": X0,
+                "traj_frames": np.stack([X for _, X in frames]), "traj_times": np.array([t for t, _ in frames]),
+                "load_vesx": vesx, "load_vesy": vesy, "load_time": time_, "load_N": Nr, "load_nv": nvr,
+                "load_xinit": xinit, "load_yinit": yinit})
+    return out
+
+
 JOBS = {
+    'io_fp64': (job_io, True, ()),
     'mlarm_fp64': (job_mlarm, 'fp64', ()),
     'mlarm_mixed': (job_mlarm, 'mixed', ()),
     'nets_fp64': (job_nets, 'fp64', ()),

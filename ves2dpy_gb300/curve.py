@@ -45,6 +45,34 @@ class Curve:
                                         out[2].data_ptr(), nat.stream_ptr(X.device)), "geomProp")
         return out[0], out[1], out[2]
 
+    def ellipse(self, N, ra, device=None):
+        """Ellipse of reduced area ``ra`` with N points (curve_batch_compile.py:494-527).
+
+        Same steps as the reference: the first shape is (a cos t, sin t) with
+        a = (1 - sqrt(1 - ra^2)) / ra, accepted when its reduced area is within
+        1e-4 (relative); otherwise up to 10 rescalings of a (x 0.9 or x 1.05)
+        of the shape (cos t, a sin t), accepted within 1e-2 (absolute).  The
+        reduced areas come from ``geomProp`` on the device.  Returns [2N, 1].
+        """
+        dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        ra = torch.as_tensor(ra, dtype=torch.float64, device=dev).reshape(-1)[:1]
+        t = torch.arange(N, dtype=torch.float64, device=dev) * 2 * torch.pi / N
+        a = (1 - torch.sqrt(1 - ra ** 2)) / ra
+        X0 = torch.cat((a * torch.cos(t), torch.sin(t)))[:, None]
+        ra_new = self.geomProp(X0)[0]
+        cond = bool((torch.abs(ra_new - ra) / ra < 1e-4).item())
+        it = 0
+        while not cond and it < 10:
+            it += 1
+            if bool((ra_new > ra).item()):
+                a = a * 0.9
+            else:
+                a = a * 1.05
+            X0 = torch.cat((torch.cos(t), a * torch.sin(t)))[:, None]
+            ra_new = self.geomProp(X0)[0]
+            cond = bool((torch.abs(ra_new - ra) < 1e-2).item())
+        return X0
+
     # -- post-step conditioning -------------------------------------------------
     def getPhysicalCenter(self, X):
         """Physical centre (2, nv) (curve_batch_compile.py:84-100)."""

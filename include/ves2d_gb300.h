@@ -374,6 +374,14 @@ VES_API int ves_farfield_static_scratch(int precision, int nsrc, int ns, const d
                                         int nt, int ntp, const double* Xtar, const int* self_idx, double* out,
                                         void* stream);
 
+/* ---- repulsion (capsules.repulsionForce, capsules.py:209-252) ---------------
+ * Penalty-layer repulsion between vesicles: X, out [nv][2][N] on the device,
+ * strength W, layer thickness eta >= 0 (pairs farther apart than eta add 0).
+ * Workspace: ves_repulsion_force_workspace(nv) bytes. */
+VES_API size_t ves_repulsion_force_workspace(int nv);
+VES_API int ves_repulsion_force(int N, int nv, const double* X, double W, double eta, double* out, void* ws,
+                                size_t ws_bytes, void* stream);
+
 /* ---- trajectory files ------------------------------------------------------
  * The reference's binary trajectory format (driver_confined.py:204-206,
  * 294-296; reader newtorch/tools/load_ves2d_file.py:4-72): little-endian

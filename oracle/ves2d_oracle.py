@@ -108,6 +108,22 @@ def ellipse(N: int, ra: float):
     return X0
 
 
+def repulsion_force(X, W, eta):
+    """Penalty-layer repulsion (capsules.py:209-252), dense over all
+    (point, point, vesicle, vesicle) pairs as in the reference."""
+    N, nv = X.shape[0] // 2, X.shape[1]
+    dx = X[:N, :][:, None, :, None] - X[:N, :][None, :, None, :]
+    dy = X[N:, :][:, None, :, None] - X[N:, :][None, :, None, :]
+    dist = np.sqrt(dx ** 2 + dy ** 2 + 1e-10)
+    dist[:, :, np.arange(nv), np.arange(nv)] = np.inf
+    L = np.floor(eta / dist)
+    dF = -L * (2 * L + 1) * (L + 1) / 3 + L * (L + 1) * eta / dist
+    rep = np.zeros((2 * N, nv))
+    rep[:N] = W * (dF * dx).sum(axis=(1, 3))
+    rep[N:] = W * (dF * dy).sum(axis=(1, 3))
+    return rep
+
+
 def write_trajectory(filename, X0, frames):
     """Trajectory bytes as the drivers write them: header and initial shapes
     (driver_confined.py:204-206), then one (time, shapes) record per step

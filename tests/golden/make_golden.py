@@ -412,8 +412,23 @@ def job_io(promote):
     return out
 
 
+def job_repulsion(promote):
+    """capsules.repulsionForce (capsules.py:209-252) on a packed cluster."""
+    import ref_shim
+    R = ref_shim.load(promote=promote)
+    torch = R.torch
+    out = {}
+    for tag, (nv, N, gap, W, eta) in {"tight": (6, 16, 0.02, 1e5, 1.0 / 16), "wide": (5, 32, 0.05, 900.0, 0.4)}.items():
+        X = small_cluster(nv=nv, N=N, seed=7, gap=gap)
+        ves = R.capsules.capsules(torch.tensor(X), None, None, 1.0, 1.0)
+        rep = ves.repulsionForce(torch.tensor(X), W, eta)
+        out.update({f"X_{tag}": X, f"rep_{tag}": _np(rep), f"W_{tag}": W, f"eta_{tag}": eta})
+    return out
+
+
 JOBS = {
     'io_fp64': (job_io, True, ()),
+    'repulsion_fp64': (job_repulsion, True, ()),
     'mlarm_fp64': (job_mlarm, 'fp64', ()),
     'mlarm_mixed': (job_mlarm, 'mixed', ()),
     'nets_fp64': (job_nets, 'fp64', ()),

@@ -75,3 +75,13 @@ def test_init_ves2d_defaults():
     assert prams["viscCont"] == [2.0, 2.0, 2.0]
     options, prams = initVes2D({"confined": True}, {"Nbd": 32, "nvbd": 2})
     assert prams["Nbd"] == 32 and prams["nvbd"] == 2 and prams["viscCont"] == [1]
+
+
+def test_oracle_repulsion_matches_reference(golden):
+    """capsules.repulsionForce (capsules.py:209-252) restated."""
+    g = golden("repulsion_fp64")
+    for tag in ("tight", "wide"):
+        ref = g[f"rep_{tag}"]
+        got = O.repulsion_force(g[f"X_{tag}"], float(g[f"W_{tag}"]), float(g[f"eta_{tag}"]))
+        assert np.abs(ref).max() > 0
+        assert np.abs(got - ref).max() < 1e-12 * np.abs(ref).max(), tag

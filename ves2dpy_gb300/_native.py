@@ -202,6 +202,8 @@ SIGNATURES = {
     "ves_ctx_set_timing": (_I, [_P, _I]),
     "ves_ctx_stats": (_I, [_P, ctypes.POINTER(Stats), _I]),
     "ves_probe_sfu_peak": (_I, [ctypes.POINTER(ctypes.c_double), _P]),
+    "ves_repulsion_force_workspace": (_SZ, [_I]),
+    "ves_repulsion_force": (_I, [_I, _I, _P, _D, _D, _P, _P, _SZ, _P]),
     "ves_traj_create": (_I, [ctypes.c_char_p, _I, _I, _P, _I, _I, ctypes.POINTER(_P)]),
     "ves_traj_append": (_I, [_P, _D, _P, _I, _P]),
     "ves_traj_flush": (_I, [_P, ctypes.POINTER(_LL)]),

@@ -94,6 +94,21 @@ class capsules:  # noqa: N801 - the reference class name
                                          nat.stream_ptr(dev)), "computeDerivs")
         return mats_from_vm(Ben), mats_from_vm(Ten), mats_from_vm(Div)
 
+    def repulsionForce(self, X, W, eta):
+        """Penalty-layer repulsion between vesicles (capsules.py:209-252):
+        for each point, W * sum over the points of the other vesicles of
+        dF(d) (x - y) with L = floor(eta / d) layers, d = sqrt(|x - y|^2 + 1e-10).
+        Returns [2N, nv]."""
+        X = as_device_f64(X)
+        N, nv = X.shape[0] // 2, X.shape[1]
+        Xv = to_vm(X)
+        out = torch.empty_like(Xv)
+        lib = nat.load_library()
+        ws = torch.empty(lib.ves_repulsion_force_workspace(nv), dtype=torch.uint8, device=X.device)
+        nat.check(lib.ves_repulsion_force(N, nv, Xv.data_ptr(), float(W), float(eta), out.data_ptr(), ws.data_ptr(),
+                                          ws.numel(), nat.stream_ptr(X.device)), "repulsionForce")
+        return from_vm(out)
+
     def getZone(self, vesicle2=None, relate=1):
         """Near zone of every vesicle w.r.t. every other, MATLAB getZone semantics
         (matlab/capsules_py.m:194-467, relate == 1; absent from the Python

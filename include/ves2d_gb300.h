@@ -60,6 +60,7 @@ extern "C" {
 #define VES_NEAR_NONE 0            /* plain upsampled trapezoid rule, no exclusion */
 #define VES_NEAR_PY_HH 1           /* mytorch/poten.py:466-600 + biem_support.py:520-613 */
 #define VES_NEAR_MATLAB 2          /* matlab/poten_py.m:495-692 + capsules_py.m:194-643   */
+#define VES_NEAR_PY_RBF 3          /* mytorch/poten.py:643-894 (nearSingInt_rbf), py_hh lists */
 
 /* background flows (mytorch/tstep_biem.py:849-952) */
 #define VES_FLOW_RELAXATION 0
@@ -181,9 +182,11 @@ VES_API int ves_density(int nv, int ns, const double* f, const double* sa, doubl
 /* nearSingInt_hh (poten.py:466-600) / nearSingInt (poten_py.m:495-692):
  * LP[nv][2][N] = far field of f over Nup-upsampled sources with the near
  * pairs removed, plus the near correction built from vself = G f.
- * scheme: VES_NEAR_PY_HH or VES_NEAR_MATLAB (lists from the matching
- * ves_near_zone_*), VES_NEAR_NONE (nl ignored).  near_only (or NULL)
- * receives the correction alone (the reference's second return value). */
+ * scheme: VES_NEAR_PY_HH, VES_NEAR_PY_RBF (both with the lists of
+ * ves_near_zone_py) or VES_NEAR_MATLAB (lists of ves_near_zone_matlab),
+ * VES_NEAR_NONE (nl ignored).  near_only (or NULL) receives the correction
+ * alone (the reference's second return value; zero for VES_NEAR_PY_RBF, whose
+ * reference returns LP only). */
 VES_API int ves_near_sing_int(ves_ctx* ctx, int scheme, int precision, int nv, const double* X,
                       const double* sa_up, const double* Xup, const double* f,
                       const double* vself, const ves_near_lists* nl, double h, double* LP,

@@ -108,6 +108,83 @@ def ellipse(N: int, ra: float):
     return X0
 
 
+RBF_LAYERS = 3
+
+
+def rbf_width(N: int) -> float:
+    """Gaussian width of the near-field fit (poten.py:715-726, 853-863, upsample -1)."""
+    return 0.672 if N == 32 else 0.0132
+
+
+def rbf_layers(X, f, vself):
+    """Layer points and self velocities of each vesicle for the RBF near-field
+    fit (poten.py:728-752, exactStokesSL_onlyself biem_support.py:468-516):
+    layer 0 is the boundary with the self velocity ``vself``; layers 1, 2 lie
+    at distances 1/(2N), 1/N along the outward normal (ty, -tx) of the coarse
+    curve and carry the vesicle's own single layer evaluated from the curve
+    and density upsampled to N*2*ceil(sqrt(2N)) points.  Returns points and
+    velocities of shape (N, 3, 2, nv)."""
+    N, nv = X.shape[0] // 2, X.shape[1]
+    M = N * (RBF_LAYERS - 1) * math.ceil(math.sqrt((RBF_LAYERS - 1) * N))
+    Xf, ff = interpft_vec(X, M), interpft_vec(f, M)
+    Dxf, Dyf = get_dxy(Xf)
+    saf = np.sqrt(Dxf ** 2 + Dyf ** 2)
+    den = ff * np.vstack((saf, saf)) * 2 * np.pi / M
+    Dx, Dy = get_dxy(X)
+    jac = np.sqrt(Dx ** 2 + Dy ** 2)
+    nx, ny = Dy / jac, -Dx / jac
+    dl = np.linspace(0, 1 / N, RBF_LAYERS)[1:]
+    pts = np.zeros((N, RBF_LAYERS, 2, nv))
+    vel = np.zeros((N, RBF_LAYERS, 2, nv))
+    pts[:, 0, 0], pts[:, 0, 1] = X[:N], X[N:]
+    vel[:, 0, 0], vel[:, 0, 1] = vself[:N], vself[N:]
+    for l, d in enumerate(dl, start=1):
+        pts[:, l, 0] = X[:N] + nx * d
+        pts[:, l, 1] = X[N:] + ny * d
+    for v in range(nv):
+        xs, ys = Xf[:M, v], Xf[M:, v]
+        dx_, dy_ = den[:M, v], den[M:, v]
+        for l in range(1, RBF_LAYERS):
+            rx = pts[:, l, 0, v][:, None] - xs[None, :]
+            ry = pts[:, l, 1, v][:, None] - ys[None, :]
+            r2 = rx ** 2 + ry ** 2
+            lg = 0.5 * np.log(r2)
+            c = (rx * dx_ + ry * dy_) / r2
+            vel[:, l, 0, v] = (-(lg * dx_).sum(1) + (c * rx).sum(1)) / (4 * np.pi)
+            vel[:, l, 1, v] = (-(lg * dy_).sum(1) + (c * ry).sum(1)) / (4 * np.pi)
+    return pts, vel
+
+
+def near_sing_int_rbf(X, f, vself, far, id1, id2):
+    """nearSingInt_rbf (poten.py:643-785) + nearFieldCorrectionUP_SOLVE
+    (:788-894): far field (already without the near pairs) plus, for every
+    near (target point, source vesicle) pair, the source vesicle's Gaussian
+    RBF fit of its self velocity on three layers, evaluated at the target
+    point.  ``id1`` = k*N + i (target point i of vesicle k), ``id2`` = source."""
+    N, nv = X.shape[0] // 2, X.shape[1]
+    LP = np.array(far, dtype=np.float64, copy=True)
+    if nv == 1 or len(id1) == 0:
+        return LP
+    w = rbf_width(N)
+    pts, vel = rbf_layers(X, f, vself)
+    n = N * RBF_LAYERS
+    coeffs = np.zeros((nv, n, 2))
+    P = pts.reshape(n, 2, nv) / w        # index i * 3 + l, as the reference's reshape
+    V = vel.reshape(n, 2, nv)
+    for v in range(nv):
+        d2 = ((P[:, None, :, v] - P[None, :, :, v]) ** 2).sum(-1)
+        A = np.exp(-d2) + 1e-6 * np.eye(n)
+        coeffs[v] = np.linalg.solve(A, V[:, :, v])
+    for p, v in zip(np.asarray(id1), np.asarray(id2)):
+        k, i = p // N, p % N
+        q = np.array([X[i, k], X[N + i, k]]) / w
+        g = np.exp(-((P[:, :, v] - q[None, :]) ** 2).sum(-1))
+        corr = g @ coeffs[v]
+        LP[i, k] += corr[0]
+        LP[N + i, k] += corr[1]
+    return LP
+
+
 def repulsion_force(X, W, eta):
     """Penalty-layer repulsion (capsules.py:209-252), dense over all
     (point, point, vesicle, vesicle) pairs as in the reference."""

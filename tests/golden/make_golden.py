@@ -426,8 +426,89 @@ def job_repulsion(promote):
     return out
 
 
+def job_rbf(promote):
+    """nearSingInt_rbf (poten.py:643-785) with nearFieldCorrectionUP_SOLVE
+    (:788-894) and exactStokesSL_onlyself (biem_support.py:468-516), called as
+    the newtorch BIEM matvec does (tstep_biem.py:431): self term G f, far field
+    with the near-zone exclusions, near pairs corrected by the RBF fit."""
+    import ref_shim
+    R = ref_shim.load(promote=promote)
+    torch = R.torch
+    out = {}
+    cases = {"n32": (small_cluster_sized(4, 32, seed=11, scale=1.0, gap=0.01), 32),
+             "n128": (mlarm_suspension(), 128)}
+    for tag, (X, N) in cases.items():
+        Xt = torch.tensor(X)
+        nv = X.shape[1]
+        ves = R.capsules.capsules(Xt, None, None, 1.0, torch.ones(nv))
+        op = R.poten.Poten(N)
+        G = op.stokesSLmatrix(ves)
+        Xup = R.filter.interpft_vec(Xt, op.Nup)
+        near = R.biem_support.naiveNearZoneInfo(Xt, Xup)
+        rng = np.random.default_rng(12)
+        f = torch.tensor(rng.normal(size=(2 * N, nv)))
+        SLP = lambda F: op.exactStokesSLdiag(ves, G, F)  # noqa: E731
+        far = R.biem_support.wrapper_allExactStokesSLTarget_compare2(
+            Xup, R.capsules.capsules(Xup, None, None, 1.0, torch.ones(nv)).sa, R.filter.interpft_vec(f, op.Nup),
+            Xt, near[-1])
+        LP = op.nearSingInt_rbf(ves, f, SLP, near, R.biem_support.wrapper_allExactStokesSLTarget_compare2, ves, True)
+        out.update({f"X_{tag}": X, f"f_{tag}": _np(f), f"G_{tag}": _np(G), f"vself_{tag}": _np(SLP(f)),
+                    f"far_{tag}": _np(far), f"LP_{tag}": _np(LP), f"id1_{tag}": _np(near[2][0]),
+                    f"id2_{tag}": _np(near[2][1])})
+    return out
+
+
+def small_cluster_sized(nv, N, seed, scale, gap):
+    """A row of nv vesicles of area pi*scale^2, each placed so that its leftmost
+    point faces the previous vesicle's rightmost point at distance ``gap``."""
+    from ves2dpy_gb300.suspension import vesicle_shape
+    rng = np.random.default_rng(seed)
+    X = np.zeros((2 * N, nv))
+    prev = None
+    for k in range(nv):
+        x, y = vesicle_shape(N, rng, 0.8, area=np.pi * scale ** 2)
+        x, y = x - x.mean(), y - y.mean()
+        if prev is not None:
+            px, py = prev
+            i, j = int(np.argmax(px)), int(np.argmin(x))
+            x = x + (px[i] - x[j]) + gap
+            y = y + (py[i] - y[j])
+        X[:N, k], X[N:, k] = x, y
+        prev = (x, y)
+    return X
+
+
+def job_step_rbf(promote):
+    """One BIEM step of the mytorch stepper with its matvec near field by
+    nearSingInt_rbf -- the alternative written (commented) at
+    mytorch/tstep_biem.py:494 and used by the newtorch stepper
+    (newtorch/tstep_biem.py:431) -- on the packed near cluster.  (The newtorch
+    stepper also drops the 1e-7 regularisation of mytorch's stokesSLmatrix,
+    newtorch/poten.py:71, so its steps differ from these in G as well.)"""
+    import ref_shim
+    R = ref_shim.load(promote=promote)
+    torch = R.torch
+    op_cls = R.poten.Poten
+
+    def hh_as_rbf(self, vesicleSou, f, selfMat, NearV2V, kernelDirect, vesicleTar, tEqualS):
+        LP = self.nearSingInt_rbf(vesicleSou, f, selfMat, NearV2V, kernelDirect, vesicleTar, tEqualS)
+        return LP, torch.zeros_like(LP)
+
+    op_cls.nearSingInt_hh = hh_as_rbf
+    X = small_cluster(nv=4, N=16, seed=1)
+    N, nv = X.shape[0] // 2, X.shape[1]
+    Xt = torch.tensor(X)
+    prams, options = make_prams(R, N, nv, 1e-4, 2.0)
+    tt = R.tstep_biem.TStepBiem(Xt, None, options, prams)
+    Xn, sig, _, _, it, iflag = tt.time_step(Xt, torch.zeros(N, nv), None, None)
+    return dict(X0=X, dt=1e-4, speed=2.0, X1=_np(Xn).astype(np.float64), sig1=_np(sig).astype(np.float64),
+                iter1=int(it), iflag1=bool(iflag))
+
+
 JOBS = {
     'io_fp64': (job_io, True, ()),
+    'step_near_rbf_fp64': (job_step_rbf, True, ()),
+    'rbf_fp64': (job_rbf, True, ()),
     'repulsion_fp64': (job_repulsion, True, ()),
     'mlarm_fp64': (job_mlarm, 'fp64', ()),
     'mlarm_mixed': (job_mlarm, 'mixed', ()),

@@ -210,3 +210,36 @@ def test_post_step_conditioning(golden, tag):
     assert rel(oc.alignCenterAngle(T(X), T(g[f"redist5_{tag}"])), g[f"align_{tag}"]) < FP64_TOL
     Xc = oc.correctAreaAndLengthAugLag(T(g[f"pert_{tag}"]), T(g[f"a0_{tag}"]), T(g[f"l0_{tag}"]))
     assert rel(Xc, g[f"corrected_{tag}"]) < 1e-9
+
+
+def test_near_sing_int_rbf_matches_reference(golden):
+    """nearSingInt_rbf on the device against the reference (golden rbf_fp64):
+    FP64 all-pairs sums, FP64 RBF fits of the vesicles that have near pairs."""
+    from ves2dpy_gb300.biem_support import naiveNearZoneInfo
+    from ves2dpy_gb300.capsules import capsules
+    from ves2dpy_gb300.filter import interpft_vec
+    from ves2dpy_gb300.poten import Poten
+    g = golden("rbf_fp64")
+    for tag, N in (("n32", 32), ("n128", 128)):
+        X = T(g[f"X_{tag}"])
+        nv = X.shape[1]
+        ves = capsules(X, None, None, 1.0, torch.ones(nv))
+        op = Poten(N)
+        G = op.stokesSLmatrix(ves, "fp64")
+        near = naiveNearZoneInfo(X, interpft_vec(X, op.Nup))
+        SLP = lambda F: op.exactStokesSLdiag(ves, G, F)  # noqa: E731
+        LP = op.nearSingInt_rbf(ves, T(g[f"f_{tag}"]), SLP, near, None, ves, True, precision="fp64")
+        assert rel(LP, g[f"LP_{tag}"]) < 1e-10, (tag, rel(LP, g[f"LP_{tag}"]))
+        # the correction is a large part of the result on these packed clusters
+        assert rel(g[f"far_{tag}"], g[f"LP_{tag}"]) > 1e-2
+
+
+def test_time_step_near_rbf_fp64(golden):
+    """The BIEM step with the matvec near field by nearSingInt_rbf (the
+    alternative at mytorch/tstep_biem.py:494, the newtorch stepper's choice)
+    on the packed near cluster."""
+    g = golden("step_near_rbf_fp64")
+    Xn, sn, _, _, it, iflag = _step(g["X0"], float(g["dt"]), float(g["speed"]), near="py_rbf")
+    assert not iflag and it == int(g["iter1"])
+    assert rel(Xn, g["X1"]) < FP64_TOL, rel(Xn, g["X1"])
+    assert rel(sn, g["sig1"]) < 1e-8, rel(sn, g["sig1"])

@@ -85,3 +85,16 @@ def test_oracle_repulsion_matches_reference(golden):
         got = O.repulsion_force(g[f"X_{tag}"], float(g[f"W_{tag}"]), float(g[f"eta_{tag}"]))
         assert np.abs(ref).max() > 0
         assert np.abs(got - ref).max() < 1e-12 * np.abs(ref).max(), tag
+
+
+def test_oracle_rbf_near_field_matches_reference(golden):
+    """nearSingInt_rbf (poten.py:643-894) restated: layer velocities, Gaussian
+    fits (LU instead of the reference's Cholesky) and the near-pair
+    correction."""
+    g = golden("rbf_fp64")
+    for tag in ("n32", "n128"):
+        ref = g[f"LP_{tag}"]
+        got = O.near_sing_int_rbf(g[f"X_{tag}"], g[f"f_{tag}"], g[f"vself_{tag}"], g[f"far_{tag}"],
+                                  g[f"id1_{tag}"], g[f"id2_{tag}"])
+        assert len(g[f"id1_{tag}"]) > 0
+        assert np.abs(got - ref).max() < 1e-10 * np.abs(ref).max(), tag

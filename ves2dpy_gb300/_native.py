@@ -28,7 +28,7 @@ VES_ERR_SINGULAR = 8
 VES_ERR_WORKSPACE = 9
 
 PREC = {"fp64": 0, "fp32c": 1, "fp32m": 2}
-NEAR = {"none": 0, "py_hh": 1, "matlab": 2}
+NEAR = {"none": 0, "py_hh": 1, "matlab": 2, "py_rbf": 3}
 FLOW = {"relaxation": 0, "extensional": 1, "parabolic": 2, "taylorGreen": 3, "shear": 4, "vortex": 5}
 
 

@@ -166,7 +166,8 @@ extern "C" int ves_density(int nv, int ns, const double* f, const double* sa, do
 extern "C" size_t ves_near_sing_int_workspace(ves_ctx* c, int precision, int nv) {
   if (!c) return 0;
   WsCarver w(nullptr, 0);
-  near_sing_int_run(c, VES_NEAR_PY_HH, precision, nv, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0,
+  // the largest scheme: the RBF fits add their buffers to the all-pairs scratch
+  near_sing_int_run(c, VES_NEAR_PY_RBF, precision, nv, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, 0,
                     nullptr, nullptr, w, 0);
   return w.off + 256;
 }

@@ -154,6 +154,10 @@ int near_sing_int_run(ves_ctx* c, int scheme, int precision, int nv, const doubl
                       const ves_near_lists* nl, double h, double* LP, double* near_only, WsCarver& ws,
                       cudaStream_t s);
 
+// RBF near-field fits (nearSingInt_rbf): adds the fits of the near pairs to LP
+int rbf_near_correct(ves_ctx* c, int nv, const double* X, const double* f, const double* vself,
+                     const ves_near_lists* nl, double* LP, WsCarver& ws, cudaStream_t s);
+
 // post-step conditioning
 int post_redistribute(ves_ctx* c, int nv, const double* X, double* Xout, int* flags, WsCarver& ws,
                       cudaStream_t s);

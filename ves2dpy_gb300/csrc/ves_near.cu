@@ -460,12 +460,16 @@ int near_sing_int_run(ves_ctx* c, int scheme, int precision, int nv, const doubl
   double* den = ws.take<double>((size_t)nv * 2 * Nup);
   int* selfidx = ws.take<int>((size_t)nv);
   const ves_near_lists* excl = (scheme == VES_NEAR_NONE) ? nullptr : nl;
-  if (ws.sizing) return farfield_run(c, precision, nv, Nup, Xup, den, nv, N, X, selfidx, excl, LP, ws, s);
+  if (ws.sizing) {
+    farfield_run(c, precision, nv, Nup, Xup, den, nv, N, X, selfidx, excl, LP, ws, s);
+    if (scheme == VES_NEAR_PY_RBF) rbf_near_correct(c, nv, X, f, vself, nl, LP, ws, s);
+    return VES_OK;
+  }
   if (!ws.ok()) {
     ves_record_error(VES_ERR_WORKSPACE, "near_sing_int: workspace too small");
     return VES_ERR_WORKSPACE;
   }
-  if (scheme != VES_NEAR_NONE && scheme != VES_NEAR_PY_HH && scheme != VES_NEAR_MATLAB) {
+  if (scheme != VES_NEAR_NONE && scheme != VES_NEAR_PY_HH && scheme != VES_NEAR_MATLAB && scheme != VES_NEAR_PY_RBF) {
     ves_record_error(VES_ERR_ARG, "near_sing_int: bad scheme %d", scheme);
     return VES_ERR_ARG;
   }
@@ -487,7 +491,10 @@ int near_sing_int_run(ves_ctx* c, int scheme, int precision, int nv, const doubl
   identity_index_kernel<<<ceil_div(nv, 256), 256, 0, s>>>(nv, selfidx);
   int rc = farfield_run(c, precision, nv, Nup, Xup, den, nv, N, X, selfidx, excl, LP, ws, s);
   if (rc) return rc;
-  if (scheme == VES_NEAR_PY_HH) {
+  if (scheme == VES_NEAR_PY_RBF) {
+    // nearSingInt_rbf: the far field above plus the fits of the near pairs
+    if ((rc = rbf_near_correct(c, nv, X, f, vself, nl, LP, ws, s))) return rc;
+  } else if (scheme == VES_NEAR_PY_HH) {
     const long long warps = (long long)nv * nl->maxc;
     ves_count_launch();
     hh_apply_kernel<<<ceil_div(warps * 32, 256), 256, 0, s>>>(nv, N, Nup, nl->maxc, X, Xup, nl->cand_count,

@@ -442,7 +442,8 @@ static int biem_step_impl(ves_ctx* c, const ves_step_params* prm, int nv, const 
     ves_record_error(VES_ERR_ARG, "biem_step: bad arguments");
     return VES_ERR_ARG;
   }
-  if (prm->near_scheme != VES_NEAR_NONE && prm->near_scheme != VES_NEAR_PY_HH && prm->near_scheme != VES_NEAR_MATLAB) {
+  if (prm->near_scheme != VES_NEAR_NONE && prm->near_scheme != VES_NEAR_PY_HH && prm->near_scheme != VES_NEAR_MATLAB &&
+      prm->near_scheme != VES_NEAR_PY_RBF) {
     ves_record_error(VES_ERR_ARG, "biem_step: bad near scheme");
     return VES_ERR_ARG;
   }
@@ -472,7 +473,7 @@ static int biem_step_impl(ves_ctx* c, const ves_step_params* prm, int nv, const 
       goto done;
     if ((rc = ves_cuda_status(cudaStreamSynchronize(s), "len sync"))) goto done;
     S.h = *std::min_element(hl.begin(), hl.end()) / N;
-  } else if (prm->near_scheme == VES_NEAR_PY_HH) {
+  } else if (prm->near_scheme == VES_NEAR_PY_HH || prm->near_scheme == VES_NEAR_PY_RBF) {
     WsCarver sub(S.scratch, S.scratch_bytes);
     if ((rc = near_zone_py(c, nv, X, S.Xup, 0.0, &S.nl, sub, s))) goto done;
   }

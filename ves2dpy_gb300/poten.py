@@ -108,6 +108,22 @@ class Poten:
             raise TypeError("NearV2V must come from naiveNearZoneInfo")
         return self._near_common("py_hh", vesicleSou, f, selfMat, NearV2V, precision)
 
+    def nearSingInt_rbf(self, vesicleSou, f, selfMat, NearV2V, kernelDirect=None, vesicleTar=None, tEqualS=True,
+                        precision: str = "fp64"):
+        """poten.py:643-894: far field over upsampled sources with the near pairs
+        of ``NearV2V`` removed, plus, for each near pair, the source vesicle's
+        Gaussian RBF fit of its self velocity on three layers (the boundary
+        with ``selfMat(f)`` and two normal offsets with its own single layer)
+        evaluated at the target point.  Returns LP.  ``kernelDirect`` is
+        replaced by the device all-pairs kernel."""
+        if not tEqualS or (vesicleTar is not None and vesicleTar is not vesicleSou):
+            raise NotImplementedError("nearSingInt_rbf: only sources == targets (tEqualS)")
+        if vesicleSou.nv == 1:
+            return torch.zeros_like(as_device_f64(vesicleSou.X))
+        if not isinstance(NearV2V, NearZone) or NearV2V.scheme != "py_hh":
+            raise TypeError("NearV2V must come from naiveNearZoneInfo")
+        return self._near_common("py_rbf", vesicleSou, f, selfMat, NearV2V, precision)[0]
+
     def nearSingInt(self, vesicleSou, f, selfMat, NearStruct, kernelDirect=None, vesicleTar=None, tEqualS=True,
                     precision: str = "fp64"):
         """MATLAB nearSingInt (matlab/poten_py.m:495-692) with NearStruct from

@@ -19,7 +19,8 @@ class TStepBiem:
     """tstep_biem.py:25-153.
 
     Extra keyword options select the device arithmetic:
-    ``near`` ("py_hh" = the reference's nearSingInt_hh, "matlab" = the MATLAB
+    ``near`` ("py_hh" = the reference's nearSingInt_hh, "py_rbf" = its
+    nearSingInt_rbf as in the newtorch step, "matlab" = the MATLAB
     near-singular scheme, "none"), ``farfield_precision`` and ``sl_precision``
     ("fp64" or "fp32c").
     """

@@ -208,6 +208,10 @@ typedef struct ves_step_params {
   int sl_precision;      /* VES_PREC_* for the Alpert matrix build */
   int maxc;              /* candidate capacity per vesicle (0 = default 64) */
   int max_entries;       /* MATLAB near entries capacity (0 = default) */
+  int repulsion;         /* add the penalty-layer repulsion (tstep_biem.py:250-264);
+                            needs near_scheme VES_NEAR_PY_HH or VES_NEAR_PY_RBF */
+  double rep_strength;   /* W (prams['repStrength']) */
+  double min_dist;       /* eta (prams['minDist']) */
 } ves_step_params;
 
 typedef struct ves_step_result {

@@ -505,8 +505,32 @@ def job_step_rbf(promote):
                 iter1=int(it), iflag1=bool(iflag))
 
 
+def job_step_rep(promote):
+    """One BIEM step with repulsion (tstep_biem.py:250-264: repulsionForce,
+    then G rep + nearSingInt_rbf(rep) on the right-hand side) on the packed
+    near cluster, mytorch stepper (matvec near field nearSingInt_hh)."""
+    import ref_shim
+    R = ref_shim.load(promote=promote)
+    patch_exact_stokes_sl(R)
+    torch = R.torch
+    X = small_cluster(nv=4, N=16, seed=1)
+    N, nv = X.shape[0] // 2, X.shape[1]
+    Xt = torch.tensor(X)
+    prams, options = make_prams(R, N, nv, 1e-4, 2.0)
+    options['repulsion'] = True
+    prams['repStrength'] = 2e3
+    prams['minDist'] = 0.06
+    tt = R.tstep_biem.TStepBiem(Xt, None, options, prams)
+    ves = R.capsules.capsules(Xt, None, None, 1.0, torch.ones(nv))
+    rep = ves.repulsionForce(Xt, prams['repStrength'], prams['minDist'])
+    Xn, sig, _, _, it, iflag = tt.time_step(Xt, torch.zeros(N, nv), None, None)
+    return dict(X0=X, dt=1e-4, speed=2.0, W=prams['repStrength'], eta=prams['minDist'], rep=_np(rep),
+                X1=_np(Xn).astype(np.float64), sig1=_np(sig).astype(np.float64), iter1=int(it), iflag1=bool(iflag))
+
+
 JOBS = {
     'io_fp64': (job_io, True, ()),
+    'step_rep_fp64': (job_step_rep, True, ()),
     'step_near_rbf_fp64': (job_step_rbf, True, ()),
     'rbf_fp64': (job_rbf, True, ()),
     'repulsion_fp64': (job_repulsion, True, ()),

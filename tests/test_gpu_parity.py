@@ -243,3 +243,21 @@ def test_time_step_near_rbf_fp64(golden):
     assert not iflag and it == int(g["iter1"])
     assert rel(Xn, g["X1"]) < FP64_TOL, rel(Xn, g["X1"])
     assert rel(sn, g["sig1"]) < 1e-8, rel(sn, g["sig1"])
+
+
+def test_time_step_with_repulsion_fp64(golden):
+    """The BIEM step with repulsion (tstep_biem.py:250-264): penalty force on
+    the current shapes, G rep + nearSingInt_rbf(rep) added to the position
+    right-hand side; matvec near field nearSingInt_hh."""
+    from ves2dpy_gb300.tstep_biem import TStepBiem
+    g = golden("step_rep_fp64")
+    X = g["X0"]
+    N, nv = X.shape[0] // 2, X.shape[1]
+    prams = dict(dt=float(g["dt"]), kappa=1.0, gmresTol=1e-10, gmresMaxIter=200, farFieldSpeed=float(g["speed"]),
+                 viscCont=[1.0] * nv, repStrength=float(g["W"]), minDist=float(g["eta"]))
+    options = dict(farField="shear", usePreco=True, repulsion=True)
+    tt = TStepBiem(T(X), None, options, prams, near="py_hh", farfield_precision="fp64", sl_precision="fp64")
+    Xn, sn, _, _, it, iflag = tt.time_step(T(X), torch.zeros(N, nv, dtype=torch.float64, device=dev()))
+    assert not iflag and it == int(g["iter1"])
+    assert rel(Xn, g["X1"]) < FP64_TOL, rel(Xn, g["X1"])
+    assert rel(sn, g["sig1"]) < 1e-8, rel(sn, g["sig1"])

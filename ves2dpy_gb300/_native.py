@@ -80,6 +80,9 @@ class StepParams(ctypes.Structure):
         ("sl_precision", ctypes.c_int),
         ("maxc", ctypes.c_int),
         ("max_entries", ctypes.c_int),
+        ("repulsion", ctypes.c_int),
+        ("rep_strength", ctypes.c_double),
+        ("min_dist", ctypes.c_double),
     ]
 
 

@@ -82,10 +82,16 @@ __global__ void pack_kernel(int nv, int N, const double* __restrict__ A2, const 
   out[idx] = (r < 2 * N) ? A2[k * 2 * N + r] : B1[k * N + (r - 2 * N)];
 }
 
+// out = (X + dt * (frepG + frepN)) + dt * v, the repulsion terms when present
+// (tstep_biem.py:257-270: Frepulsion = G rep + nearSingInt_rbf(rep), then vInf)
 __global__ void rhs_pos_kernel(long long n, double dt, const double* __restrict__ X, const double* __restrict__ v,
+                               const double* __restrict__ frepG, const double* __restrict__ frepN,
                                double* __restrict__ out) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = X[i] + dt * v[i];
+  if (i >= n) return;
+  double r = X[i];
+  if (frepG) r = r + dt * (frepG[i] + frepN[i]);
+  out[i] = r + dt * v[i];
 }
 
 __global__ void unpack_kernel(int nv, int N, const double* __restrict__ x, double* __restrict__ X,
@@ -431,6 +437,14 @@ static int biem_step_impl(ves_ctx* c, const ves_step_params* prm, int nv, const 
                       nullptr, 0, nullptr, nullptr, w, s);
     scratch = std::max(scratch, w.off);
   }
+  if (prm->repulsion) {  // force, G force, its near-field integral (RBF), the force's scratch
+    WsCarver w(nullptr, 0);
+    w.take<double>((size_t)3 * nv * 2 * N);
+    w.take<char>(ves_repulsion_force_workspace(nv));
+    near_sing_int_run(c, VES_NEAR_PY_RBF, prm->farfield_precision, nv, nullptr, nullptr, nullptr, nullptr, nullptr,
+                      nullptr, 0, nullptr, nullptr, w, s);
+    scratch = std::max(scratch, w.off);
+  }
   S.scratch = ws.take<char>(scratch + 1024);
   S.scratch_bytes = scratch + 1024;
   if (ws.sizing) return VES_OK;
@@ -445,6 +459,10 @@ static int biem_step_impl(ves_ctx* c, const ves_step_params* prm, int nv, const 
   if (prm->near_scheme != VES_NEAR_NONE && prm->near_scheme != VES_NEAR_PY_HH && prm->near_scheme != VES_NEAR_MATLAB &&
       prm->near_scheme != VES_NEAR_PY_RBF) {
     ves_record_error(VES_ERR_ARG, "biem_step: bad near scheme");
+    return VES_ERR_ARG;
+  }
+  if (prm->repulsion && prm->near_scheme != VES_NEAR_PY_HH && prm->near_scheme != VES_NEAR_PY_RBF) {
+    ves_record_error(VES_ERR_ARG, "biem_step: repulsion needs the naiveNearZoneInfo lists (near py_hh or py_rbf)");
     return VES_ERR_ARG;
   }
   int rc = ves_reset_status(c, s);
@@ -479,8 +497,27 @@ static int biem_step_impl(ves_ctx* c, const ves_step_params* prm, int nv, const 
   }
   // right-hand side [X + dt*vinf; surfaceDiv(X)]
   launch_bg_flow(nv, N, prm->flow, prm->speed, prm->chan_width, prm->vortex_size, X, vinf, s);
-  ves_count_launch();
-  rhs_pos_kernel<<<ceil_div((long long)nv * 2 * N, 256), 256, 0, s>>>((long long)nv * 2 * N, prm->dt, X, vinf, vinf);
+  if (prm->repulsion && nv > 1) {
+    // repulsion on the current shapes: G rep + nearSingInt_rbf(rep) (tstep_biem.py:250-264)
+    WsCarver sub(S.scratch, S.scratch_bytes);
+    double* rp = sub.take<double>((size_t)nv * 2 * N);
+    double* rG = sub.take<double>((size_t)nv * 2 * N);
+    double* rN = sub.take<double>((size_t)nv * 2 * N);
+    const size_t rws = ves_repulsion_force_workspace(nv);
+    char* rw = sub.take<char>(rws);
+    if ((rc = ves_repulsion_force(N, nv, X, prm->rep_strength, prm->min_dist, rp, rw, rws, s))) goto done;
+    launch_bgemv_f64(nv, 2 * N, 2 * N, S.G, rp, 2LL * N, rG, 2LL * N, s);
+    if ((rc = near_sing_int_run(c, VES_NEAR_PY_RBF, prm->farfield_precision, nv, X, S.sa_up, S.Xup, rp, rG, &S.nl,
+                                S.h, rN, nullptr, sub, s)))
+      goto done;
+    ves_count_launch();
+    rhs_pos_kernel<<<ceil_div((long long)nv * 2 * N, 256), 256, 0, s>>>((long long)nv * 2 * N, prm->dt, X, vinf, rG, rN,
+                                                                        vinf);
+  } else {
+    ves_count_launch();
+    rhs_pos_kernel<<<ceil_div((long long)nv * 2 * N, 256), 256, 0, s>>>((long long)nv * 2 * N, prm->dt, X, vinf,
+                                                                        nullptr, nullptr, vinf);
+  }
   launch_surface_div(c, nv, S.isa, S.tang, X, 2LL * N, rhs2, N, s);
   ves_count_launch();
   pack_kernel<<<ceil_div(n, 256), 256, 0, s>>>(nv, N, vinf, rhs2, B.b);

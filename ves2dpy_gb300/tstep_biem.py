@@ -29,8 +29,6 @@ class TStepBiem:
                  sl_precision: str = "fp32c", device=None):
         if Xwalls is not None:
             raise NotImplementedError("confined flows (walls) are not supported by the device stepper")
-        if options.get("repulsion", False):
-            raise NotImplementedError("repulsion is not supported by the device stepper")
         visc = torch.as_tensor(prams.get("viscCont", 1.0), dtype=torch.float64)
         if torch.any(visc != 1):
             raise NotImplementedError("viscosity contrast != 1 is not supported by the device stepper")
@@ -50,6 +48,12 @@ class TStepBiem:
         self.options = dict(options)
         self.usePreco = bool(options.get("usePreco", True))
         self.confined = False
+        # repulsion (tstep_biem.py:75-83), off for a single vesicle
+        self.repulsion = bool(options.get("repulsion", False)) and X.shape[1] > 1
+        self.repStrength = float(prams.get("repStrength", 900))
+        self.minDist = float(prams.get("minDist", 0.4))
+        if self.repulsion and near not in ("py_hh", "py_rbf"):
+            raise NotImplementedError("repulsion needs near='py_hh' or 'py_rbf' (naiveNearZoneInfo lists)")
         self.near = near
         self.farfield_precision = farfield_precision
         self.sl_precision = sl_precision
@@ -80,6 +84,9 @@ class TStepBiem:
         p.sl_precision = nat.PREC[self.sl_precision]
         p.maxc = 64
         p.max_entries = 0
+        p.repulsion = 1 if self.repulsion else 0
+        p.rep_strength = self.repStrength
+        p.min_dist = self.minDist
         return p
 
     def workspace_bytes(self) -> int:

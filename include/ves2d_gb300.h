@@ -193,6 +193,41 @@ VES_API int ves_near_sing_int(ves_ctx* ctx, int scheme, int precision, int nv, c
                       double* near_only, void* ws, size_t ws_bytes, void* stream);
 VES_API size_t ves_near_sing_int_workspace(ves_ctx* ctx, int precision, int nv);
 
+/* ---- double layer (viscosity contrast) ------------------------------------ */
+/* Geometry of capsules(interpft(X, Nup)): Xup[nv][2][Nup], sa[nv][Nup],
+ * tang[nv][2][Nup], cur[nv][Nup] (any output may be NULL), from the first and
+ * second derivatives of the trig interpolant at the Nup grid. */
+VES_API int ves_upsample_geometry(ves_ctx* ctx, int nv, const double* X, double* Xup, double* sa, double* tang,
+                                  double* cur, void* stream);
+/* stokesDLmatrix (poten.py:102-175): D[nv][2N][2N] on the Nup-upsampled
+ * curve restricted to N points; visc[nv] device viscosity contrasts (D = 0
+ * where visc == 1).  precision: VES_PREC_FP64 or VES_PREC_FP32C (kernel
+ * values in FP64, the R Dup P products in FP32, as the single-layer build). */
+VES_API int ves_stokes_dl_matrix(ves_ctx* ctx, int nv, const double* X, const double* visc, int precision,
+                                 double* D, void* ws, size_t ws_bytes, void* stream);
+VES_API size_t ves_stokes_dl_matrix_workspace(ves_ctx* ctx, int nv, int precision);
+/* den[nv][2][ns] = f * sa * 2*pi/ns * (1 - visc)  (poten.py:411; visc NULL: all 1) */
+VES_API int ves_dl_density(int nv, int ns, const double* f, const double* sa, const double* visc, double* den,
+                           void* stream);
+/* Direct double-layer sum, exactStokesDL (poten.py:399-441):
+ *   u(x) = 1/pi sum_src ((r.n)(r.den)/|r|^4) r,  r = x - y,  n = (ty, -tx),
+ * sources Xsrc[nsrc][2][ns] with unit tangents tang[nsrc][2][ns] and den from
+ * ves_dl_density; targets Xtar[nt][2][ntp] (ntp <= 1024); self_idx and nl as
+ * ves_farfield.  FP64. */
+VES_API int ves_farfield_dl(ves_ctx* ctx, int nsrc, int ns, const double* Xsrc, const double* tang,
+                            const double* den, int nt, int ntp, const double* Xtar, const int* self_idx,
+                            const ves_near_lists* nl, double* out, void* stream);
+/* nearSingInt with kernelDirect = exactStokesDL (tstep_biem.py:236,501;
+ * poten_py.m:495-692): double-layer far field over the Nup-upsampled sources
+ * (Xup, tang_up, sa_up of the upsampled curve) with the near pairs removed,
+ * plus the near correction from vself = jump f + D f.  scheme:
+ * VES_NEAR_NONE, VES_NEAR_PY_HH or VES_NEAR_MATLAB. */
+VES_API int ves_near_sing_int_dl(ves_ctx* ctx, int scheme, int nv, const double* X, const double* Xup,
+                                 const double* tang_up, const double* sa_up, const double* visc, const double* f,
+                                 const double* vself, const ves_near_lists* nl, double h, double* LP,
+                                 double* near_only, void* ws, size_t ws_bytes, void* stream);
+VES_API size_t ves_near_sing_int_dl_workspace(ves_ctx* ctx, int nv);
+
 /* ---- the implicit BIEM step (tstep_biem.py:181-428) ------------------------ */
 typedef struct ves_step_params {
   double dt;
@@ -212,6 +247,10 @@ typedef struct ves_step_params {
                             needs near_scheme VES_NEAR_PY_HH or VES_NEAR_PY_RBF */
   double rep_strength;   /* W (prams['repStrength']) */
   double min_dist;       /* eta (prams['minDist']) */
+  const double* visc_cont; /* device [nv] viscosity contrasts, or NULL when every
+                              vesicle has contrast 1 (no double-layer terms);
+                              with contrasts: D, Fdlp and alpha = (1 + visc)/2
+                              (tstep_biem.py:195-244, 486-501, 541-560) */
 } ves_step_params;
 
 typedef struct ves_step_result {
@@ -227,8 +266,9 @@ typedef struct ves_step_result {
 } ves_step_result;
 
 /* TStepBiem.time_step: X[nv][2][N], sigma[nv][N] -> Xout, sigma_out (may alias
- * the inputs).  Unconfined, viscosity contrast 1, no repulsion (the only
- * branches the benchmark configurations use). */
+ * the inputs).  Unconfined; optional repulsion and viscosity contrast.
+ * Without the preconditioner GMRES starts from zero, as the reference's
+ * gmres call without x0 (tstep_biem.py:383). */
 VES_API int ves_biem_step(ves_ctx* ctx, const ves_step_params* prm, int nv, const double* X,
                   const double* sigma, double* Xout, double* sigma_out, ves_step_result* res,
                   void* ws, size_t ws_bytes, void* stream);

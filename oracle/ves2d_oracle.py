@@ -729,6 +729,142 @@ def near_sing_int_matlab(X, f, vself, entries, h, tab: PotenTables):
 
 
 # --------------------------------------------------------------------------
+# Double layer of vesicles with a viscosity contrast (mytorch/poten.py:102-175,
+# 227-238, 399-441; matlab/poten_py.m:419-470, 495-692)
+# --------------------------------------------------------------------------
+
+
+def visc_vector(visc, nv):
+    v = np.asarray(1.0 if visc is None else visc, dtype=np.float64).reshape(-1)
+    return np.full(nv, float(v[0])) if v.size == 1 else v
+
+
+def stokes_dl_matrix(X, visc, tab: PotenTables):
+    """Double-layer matrix D (2N, 2N, nv) (poten.py:102-175): trapezoid rule on
+    the Nup-upsampled curve, curvature limit on the diagonal, D = R Dup P
+    scaled by (1/pi)(2 pi/Nup); zero where visc == 1."""
+    N, nv = X.shape[0] // 2, X.shape[1]
+    Nup = tab.Nup
+    visc = visc_vector(visc, nv)
+    Xup = interpft_vec(X, Nup)
+    sa, tang, cur = diff_prop(Xup)
+    D = np.zeros((2 * N, 2 * N, nv))
+    ids = np.arange(Nup)
+    for k in range(nv):
+        if visc[k] == 1:
+            continue
+        c = -(1.0 - visc[k])
+        x, y = Xup[:Nup, k], Xup[Nup:, k]
+        tx, ty = tang[:Nup, k], tang[Nup:, k]
+        dx = x[None, :] - x[:, None]          # [a, b] = x_b - x_a (target a, source b)
+        dy = y[None, :] - y[:, None]
+        r2 = dx ** 2 + dy ** 2
+        r2[ids, ids] = 1.0
+        rho4 = 1.0 / r2 ** 2
+        rho4[ids, ids] = 0.0
+        K = c * ((dx * ty[None, :] - dy * tx[None, :]) * rho4 * sa[None, :, k])
+        D11, D12, D22 = K * dx ** 2, K * dx * dy, K * dy ** 2
+        fac = 0.5 * c * cur[:, k] * sa[:, k]
+        D11[ids, ids] = fac * tx ** 2
+        D12[ids, ids] = fac * tx * ty
+        D22[ids, ids] = fac * ty ** 2
+        w = (1.0 / np.pi) * (2 * np.pi / Nup)
+        D[:N, :N, k] = (tab.R @ D11 @ tab.P) * w
+        D[:N, N:, k] = (tab.R @ D12 @ tab.P) * w
+        D[N:, :N, k] = D[:N, N:, k]
+        D[N:, N:, k] = (tab.R @ D22 @ tab.P) * w
+    return D
+
+
+def exact_stokes_dl(Xsrc, tang_src, sa_src, f, visc_src, Xtar, K1=None, skip_self=False, keep=None):
+    """Direct double layer (poten.py:399-441): u(x) = 1/pi sum ((r.n)(r.den)/|r|^4) r,
+    r = x - y, n = (ty, -tx), den = f sa (2 pi / Ns) (1 - visc).
+
+    Sources: the vesicles K1 (all by default) of Xsrc; targets: every column
+    of Xtar.  ``skip_self`` drops source vesicle t for target column t (the
+    far-field loop of nearSingInt, poten_py.m:574-577); ``keep[s, i, t]``
+    (optional) drops the pair (source vesicle s, target point i of column t)."""
+    Ns, nvs = Xsrc.shape[0] // 2, Xsrc.shape[1]
+    Nt, nc = Xtar.shape[0] // 2, Xtar.shape[1]
+    K1 = list(range(nvs)) if K1 is None else list(K1)
+    visc_src = visc_vector(visc_src, nvs)
+    den = f * np.tile(sa_src, (2, 1)) * (2 * np.pi / Ns) * (1.0 - visc_src)[None, :]
+    out = np.zeros((2 * Nt, nc))
+    for t in range(nc):
+        xt, yt = Xtar[:Nt, t], Xtar[Nt:, t]
+        for s in K1:
+            if skip_self and s == t:
+                continue
+            dx = xt[None, :] - Xsrc[:Ns, s][:, None]          # (Ns, Nt)
+            dy = yt[None, :] - Xsrc[Ns:, s][:, None]
+            d2 = dx ** 2 + dy ** 2
+            nx, ny = tang_src[Ns:, s][:, None], -tang_src[:Ns, s][:, None]
+            c = ((dx * nx + dy * ny) / d2 ** 2) * (dx * den[:Ns, s][:, None] + dy * den[Ns:, s][:, None])
+            ux, uy = np.sum(c * dx, axis=0), np.sum(c * dy, axis=0)
+            if keep is not None:
+                ux = np.where(keep[s, :, t], ux, 0.0)
+                uy = np.where(keep[s, :, t], uy, 0.0)
+            out[:Nt, t] += ux
+            out[Nt:, t] += uy
+    return out / np.pi
+
+
+def near_sing_int_dl(X, f, vself, visc, tab: PotenTables, scheme="none", near=None, entries=None, h=None):
+    """nearSingInt with kernelDirect = exactStokesDL (tstep_biem.py:236,501).
+
+    Far field: the double layer of the Nup-upsampled sources of every other
+    vesicle with the near pairs removed.  Correction: ``scheme`` "py_hh"
+    (naiveNearZoneInfo lists ``near``): the nearSingInt_hh gather of vself
+    (poten.py:527-597); "matlab" (getZone ``entries``): the 7-point Lagrange
+    extrapolation of poten_py.m:595-688 with the double layer at the Lagrange
+    points; "none": far field only."""
+    N, nv = X.shape[0] // 2, X.shape[1]
+    if nv == 1:
+        return np.zeros_like(X)
+    Nup = tab.Nup
+    visc = visc_vector(visc, nv)
+    Xup = interpft_vec(X, Nup)
+    fup = interpft_vec(f, Nup)
+    sa_up, tang_up, _ = diff_prop(Xup)
+    keep = np.ones((nv, N, nv), dtype=bool)
+    if scheme == "py_hh":
+        ids0, ids1, ids2 = near[4]
+        oth = other_indices(nv)
+        for j, i, t in zip(ids0, ids1, ids2):
+            keep[oth[t][j], i, t] = False
+    elif scheme == "matlab":
+        for e in entries:
+            keep[e.k1, e.j, e.k2] = False
+    LP = exact_stokes_dl(Xup, tang_up, sa_up, fup, visc, X, skip_self=True, keep=keep)
+    if scheme == "py_hh":
+        for k1, k2, J, ic in hh_entries(near, N, nv):
+            pn0 = (ic - 3) % N
+            LP[J, k2] += vself[pn0, k1]
+            LP[J + N, k2] += vself[pn0 + N, k1]
+    elif scheme == "matlab":
+        interp = tab.interp
+        order = interp.shape[0]
+        p = (order + 2) // 2
+        beta = 1.1
+        for e in entries:
+            pn = np.mod(np.arange(e.icp - p + 1, e.icp - p + 1 + order), N)
+            velx = lagrange_eval(interp @ vself[pn, e.k1], e.theta)
+            vely = lagrange_eval(interp @ vself[pn + N, e.k1], e.theta)
+            tx, ty = X[e.j, e.k2], X[e.j + N, e.k2]
+            nx = (tx - e.nx) / e.dist
+            ny = (ty - e.ny) / e.dist
+            sl = beta * h * np.arange(1, order)
+            XLc = np.concatenate([e.nx + sl * nx, e.ny + sl * ny])[:, None]
+            lag = exact_stokes_dl(Xup, tang_up, sa_up, fup, visc, XLc, K1=[e.k1]).reshape(-1)
+            Px = interp @ np.concatenate([[velx], lag[:order - 1]])
+            Py = interp @ np.concatenate([[vely], lag[order - 1:]])
+            ds = e.dist / (beta * h * (order - 1))
+            LP[e.j, e.k2] += lagrange_eval(Px, ds)
+            LP[e.j + N, e.k2] += lagrange_eval(Py, ds)
+    return LP
+
+
+# --------------------------------------------------------------------------
 # Background flow (mytorch/tstep_biem.py:849-952)
 # --------------------------------------------------------------------------
 

@@ -528,7 +528,95 @@ def job_step_rep(promote):
                 X1=_np(Xn).astype(np.float64), sig1=_np(sig).astype(np.float64), iter1=int(it), iflag1=bool(iflag))
 
 
+def separated_row(nv, N, seed, spacing=2.5):
+    """nv vesicles of the default shape generator on a row, ``spacing`` apart
+    (no near pairs at the 1/N threshold)."""
+    from ves2dpy_gb300.suspension import vesicle_shape
+    rng = np.random.default_rng(seed)
+    X = np.zeros((2 * N, nv))
+    for k in range(nv):
+        x, y = vesicle_shape(N, rng, 0.7)
+        X[:N, k] = x - x.mean() + spacing * k
+        X[N:, k] = y - y.mean() + 0.3 * (k % 2)
+    return X
+
+
+def job_dl(promote):
+    """Double layer of vesicles with a viscosity contrast: stokesDLmatrix,
+    exactStokesDLdiag and exactStokesDL (mytorch/poten.py:102-175, 227-238,
+    399-441), the far-field loop of nearSingInt with kernelDirect =
+    exactStokesDL, and one BIEM step with contrasts.
+
+    The reference's viscosity-contrast step does not run as written: it calls
+    ``op.nearSingInt`` (tstep_biem.py:236, 501), which mytorch/poten.py does
+    not define, and its block preconditioner adds the 2N x N block G*Ten to a
+    2N x 2N one (tstep_biem.py:331-334, a shape error).  The step fixture
+    therefore runs with usePreco=False (scipy's removed ``tol`` keyword of
+    tstep_biem.py:383 passed as ``rtol``) on vesicles without near pairs, with
+    ``nearSingInt`` supplied as the far-field loop of matlab/poten_py.m:571-579
+    written with the reference's own interpft_vec, capsules and exactStokesDL
+    (with no near pairs that loop is the whole of nearSingInt)."""
+    import ref_shim
+    R = ref_shim.load(promote=promote)
+    torch = R.torch
+    out = {}
+
+    def far_loop(op):
+        def nearSingInt(vesicleSou, f, selfMat, NearStruct, kernelDirect, vesicleTar, tEqualS):
+            assert tEqualS and vesicleTar is vesicleSou
+            if NearStruct is not None:
+                assert len(NearStruct[4][0]) == 0 and len(NearStruct[3][0]) == 0, "near pairs present"
+            Xup = R.filter.interpft_vec(vesicleSou.X, op.Nup)
+            fup = R.filter.interpft_vec(f, op.Nup)
+            vup = R.capsules.capsules(Xup, None, None, vesicleSou.kappa, vesicleSou.viscCont)
+            nvs = vesicleSou.X.shape[1]
+            cols = [kernelDirect(vup, fup, vesicleTar.X[:, k:k + 1], [j for j in range(nvs) if j != k])
+                    for k in range(nvs)]
+            return torch.cat(cols, dim=1)
+        return nearSingInt
+
+    for tag, N, nv, seed, visc in (("n32", 32, 3, 41, [3.0, 1.0, 0.5]), ("n128", 128, 2, 42, [0.25, 4.0])):
+        X = separated_row(nv, N, seed)
+        Xt = torch.tensor(X)
+        vt = torch.tensor(visc)
+        ves = R.capsules.capsules(Xt, None, None, 1.0, vt)
+        op = R.poten.Poten(N)
+        D = op.stokesDLmatrix(ves)
+        rng = np.random.default_rng(seed + 100)
+        f = torch.tensor(rng.normal(size=(2 * N, nv)))
+        Xtar = Xt + torch.tensor([0.0] * N + [4.0] * N)[:, None]
+        dl = op.exactStokesDL(ves, f, Xtar, list(range(nv)))
+        near = R.biem_support.naiveNearZoneInfo(Xt, R.filter.interpft_vec(Xt, op.Nup))
+        assert len(near[4][0]) == 0
+        far = far_loop(op)(ves, f, None, near, op.exactStokesDL, ves, True)
+        out.update({f"X_{tag}": X, f"visc_{tag}": np.array(visc), f"f_{tag}": _np(f), f"D_{tag}": _np(D),
+                    f"DLdiag_{tag}": _np(op.exactStokesDLdiag(ves, D, f)), f"Xtar_{tag}": _np(Xtar),
+                    f"DL_{tag}": _np(dl), f"far_{tag}": _np(far)})
+
+    # one step, nv=3, N=32, contrasts 3, 1, 0.5
+    _gmres = R.tstep_biem.gmres
+
+    def gmres_rtol(A, b, tol=None, **kw):
+        return _gmres(A, b, rtol=tol, **kw)
+
+    R.tstep_biem.gmres = gmres_rtol
+    X = out["X_n32"]
+    N, nv = X.shape[0] // 2, X.shape[1]
+    Xt = torch.tensor(X)
+    prams, options = make_prams(R, N, nv, 1e-4, 2.0)
+    prams['viscCont'] = torch.tensor([3.0, 1.0, 0.5])
+    options['usePreco'] = False
+    tt = R.tstep_biem.TStepBiem(Xt, None, options, prams)
+    tt.op.nearSingInt = far_loop(tt.op)
+    Xn, sig, _, _, it, iflag = tt.time_step(Xt, torch.zeros(N, nv), None, None)
+    out.update(step_X0=X, step_visc=np.array([3.0, 1.0, 0.5]), step_dt=1e-4, step_speed=2.0,
+               step_X1=_np(Xn).astype(np.float64), step_sig1=_np(sig).astype(np.float64), step_iter1=int(it),
+               step_iflag1=bool(iflag))
+    return out
+
+
 JOBS = {
+    'dl_fp64': (job_dl, True, ()),
     'io_fp64': (job_io, True, ()),
     'step_rep_fp64': (job_step_rep, True, ()),
     'step_near_rbf_fp64': (job_step_rbf, True, ()),

@@ -83,6 +83,7 @@ class StepParams(ctypes.Structure):
         ("repulsion", ctypes.c_int),
         ("rep_strength", ctypes.c_double),
         ("min_dist", ctypes.c_double),
+        ("visc_cont", ctypes.c_void_p),
     ]
 
 
@@ -205,6 +206,14 @@ SIGNATURES = {
     "ves_ctx_set_timing": (_I, [_P, _I]),
     "ves_ctx_stats": (_I, [_P, ctypes.POINTER(Stats), _I]),
     "ves_probe_sfu_peak": (_I, [ctypes.POINTER(ctypes.c_double), _P]),
+    "ves_upsample_geometry": (_I, [_P, _I, _P, _P, _P, _P, _P, _P]),
+    "ves_stokes_dl_matrix": (_I, [_P, _I, _P, _P, _I, _P, _P, _SZ, _P]),
+    "ves_stokes_dl_matrix_workspace": (_SZ, [_P, _I, _I]),
+    "ves_dl_density": (_I, [_I, _I, _P, _P, _P, _P, _P]),
+    "ves_farfield_dl": (_I, [_P, _I, _I, _P, _P, _P, _I, _I, _P, _P, ctypes.POINTER(NearLists), _P, _P]),
+    "ves_near_sing_int_dl": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(NearLists), _D, _P, _P,
+                                  _P, _SZ, _P]),
+    "ves_near_sing_int_dl_workspace": (_SZ, [_P, _I]),
     "ves_repulsion_force_workspace": (_SZ, [_I]),
     "ves_repulsion_force": (_I, [_I, _I, _P, _D, _D, _P, _P, _SZ, _P]),
     "ves_traj_create": (_I, [ctypes.c_char_p, _I, _I, _P, _I, _I, ctypes.POINTER(_P)]),

@@ -186,6 +186,30 @@ extern "C" int ves_near_sing_int(ves_ctx* c, int scheme, int precision, int nv, 
   return finish(c, s, "ves_near_sing_int");
 }
 
+extern "C" size_t ves_near_sing_int_dl_workspace(ves_ctx* c, int nv) {
+  if (!c) return 0;
+  WsCarver w(nullptr, 0);
+  near_sing_int_dl_run(c, VES_NEAR_PY_HH, nv, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                       0, nullptr, nullptr, w, 0);
+  return w.off + 256;
+}
+
+extern "C" int ves_near_sing_int_dl(ves_ctx* c, int scheme, int nv, const double* X, const double* Xup,
+                                    const double* tang_up, const double* sa_up, const double* visc, const double* f,
+                                    const double* vself, const ves_near_lists* nl, double h, double* LP,
+                                    double* near_only, void* ws, size_t ws_bytes, void* stream) {
+  VES_REQUIRE(c && X && Xup && tang_up && sa_up && visc && f && LP && ws && nv >= 0,
+              "ves_near_sing_int_dl: bad arguments");
+  VES_REQUIRE(scheme == VES_NEAR_NONE || vself, "ves_near_sing_int_dl: vself required");
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = ves_reset_status(c, s);
+  if (rc) return rc;
+  WsCarver w(ws, ws_bytes);
+  rc = near_sing_int_dl_run(c, scheme, nv, X, Xup, tang_up, sa_up, visc, f, vself, nl, h, LP, near_only, w, s);
+  if (rc) return rc;
+  return finish(c, s, "ves_near_sing_int_dl");
+}
+
 extern "C" size_t ves_redistribute_arclength_workspace(ves_ctx* c, int nv) {
   if (!c) return 0;
   WsCarver w(nullptr, 0);

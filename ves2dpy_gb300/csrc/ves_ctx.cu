@@ -228,6 +228,12 @@ static double cardinal_deriv(int N, double t) {
   s -= 0.5 * N * sin(0.5 * N * t);
   return s / N;
 }
+static double cardinal_deriv2(int N, double t) {
+  double s = 0.0;
+  for (int k = 1; k < N / 2; ++k) s -= 2.0 * (double)k * k * cos(k * t);
+  s -= 0.25 * N * N * cos(0.5 * N * t);
+  return s / N;
+}
 // Entry (node at offset y, grid point r) of sinterpS_ (fft1.py:58-88).  Its
 // mode list puts frequency 0 in the Nyquist slot of the FFT, so the Nyquist
 // coefficient enters with weight exp(0) = 1: a (-1)^r / n term.
@@ -288,7 +294,7 @@ extern "C" int ves_ctx_create(int N, ves_ctx** out) {
     return rc;
   }
   // host tables
-  std::vector<double> d1N(N), d1Nup(Nup), pc(Nup), pcd(Nup), qw(c->nquad), cq(14 * Nup),
+  std::vector<double> d1N(N), d1Nup(Nup), pc(Nup), pcd(Nup), pcdd(Nup), qw(c->nquad), cq(14 * Nup),
       ad(14 * Nup), Rm((size_t)N * Nup), Pm((size_t)Nup * N), lag(49), c6(6 * N), c6d(6 * N), cos6(6 * N),
       sin6(6 * N), cosU(Nup), sinU(Nup);
   for (int r = 0; r < 6 * N; ++r) {
@@ -304,6 +310,7 @@ extern "C" int ves_ctx_create(int N, ves_ctx** out) {
     double t = 2.0 * VES_PI * r / Nup;
     pc[r] = cardinal(N, t);
     pcd[r] = cardinal_deriv(N, t);
+    pcdd[r] = cardinal_deriv2(N, t);
     cosU[r] = cos(t);
     sinU[r] = sin(t);
   }
@@ -332,7 +339,7 @@ extern "C" int ves_ctx_create(int N, ves_ctx** out) {
   for (int i = 0; i < 49; ++i) lag[i] = kLagrange[i];
 
   // one device buffer
-  size_t nd = d1N.size() + d1Nup.size() + pc.size() + pcd.size() + qw.size() + cq.size() + ad.size() +
+  size_t nd = d1N.size() + d1Nup.size() + pc.size() + pcd.size() + pcdd.size() + qw.size() + cq.size() + ad.size() +
               Rm.size() + Pm.size() + lag.size() + 4 * c6.size() + 2 * cosU.size();
   size_t nf = Rm.size() + Pm.size() + ad.size() + qw.size();
   size_t bytes = nd * sizeof(double) + nf * sizeof(float) + 1024;
@@ -352,6 +359,7 @@ extern "C" int ves_ctx_create(int N, ves_ctx** out) {
   c->d1Nup = put(d1Nup);
   c->pc = put(pc);
   c->pcd = put(pcd);
+  c->pcdd = put(pcdd);
   c->qw = put(qw);
   c->cq = put(cq);
   c->adense = put(ad);

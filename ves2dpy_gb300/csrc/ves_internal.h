@@ -19,6 +19,7 @@ struct ves_ctx {
   double* d1Nup;   // [Nup]  same on the Nup grid
   double* pc;      // [Nup]  N->Nup prolongation circulant: P[u][i] = pc[(u - m i) mod Nup]
   double* pcd;     // [Nup]  its derivative (d/dtheta of the interpolant)
+  double* pcdd;    // [Nup]  its second derivative
   double* qw;      // [nquad] Alpert weights (already / 4pi)
   double* cq;      // [14][Nup] coarse cardinal at the 14 off-grid Alpert nodes
   double* adense;  // [14][Nup] Nup-grid trig interpolation rows of the 14 off-grid nodes
@@ -93,6 +94,10 @@ void launch_upsample_deriv(const ves_ctx* c, int nv, const double* X, double* Xu
                            double* sa_up, cudaStream_t s);
 void launch_diff_prop(const ves_ctx* c, int grid, int nv, const double* X, double* sa, double* isa,
                       double* tang, double* cur, cudaStream_t s);
+// geometry of the Nup-upsampled curve (capsules(interpft(X, Nup))) from the
+// derivatives of the trig interpolant: Xup, sa, unit tangent, curvature (any may be null)
+void launch_upsample_geom(const ves_ctx* c, int nv, const double* X, double* Xup, double* sa, double* tang,
+                          double* cur, cudaStream_t s);
 void launch_geom_prop(const ves_ctx* c, int nv, const double* X, double* ra, double* area,
                       double* length, cudaStream_t s);
 void launch_trac_jump(const ves_ctx* c, int nv, double kappa, const double* isa, const double* tang,
@@ -103,9 +108,10 @@ void launch_surface_div(const ves_ctx* c, int nv, const double* isa, const doubl
 void launch_bg_flow(int nv, int N, int flow, double speed, double cw, double vs, const double* X,
                     double* v, cudaStream_t s);
 void launch_density(int nv, int ns, const double* f, const double* sa, double* den, cudaStream_t s);
+// Dm (or NULL): double-layer matrices [nv][2N][2N]; alpha (or NULL): (1 + visc)/2 per vesicle
 int derivs_and_precond(ves_ctx* c, int nv, const double* isa, const double* tang, const double* G,
                        double dt, double kappa, double* Ben, double* Ten, double* Div, double* M,
-                       WsCarver& ws, cudaStream_t s);
+                       WsCarver& ws, cudaStream_t s, const double* Dm = nullptr, const double* alpha = nullptr);
 
 // dense per-vesicle algebra
 void launch_bgemm_f64(int batch, int M, int N, int K, double alpha, const double* A, int lda,
@@ -153,6 +159,19 @@ int near_sing_int_run(ves_ctx* c, int scheme, int precision, int nv, const doubl
                       const double* sa_up, const double* Xup, const double* f, const double* vself,
                       const ves_near_lists* nl, double h, double* LP, double* near_only, WsCarver& ws,
                       cudaStream_t s);
+
+// double layer (viscosity contrast)
+int stokes_dl_matrix(ves_ctx* c, int nv, const double* X, const double* visc, int precision, double* D, WsCarver& ws,
+                     cudaStream_t s);
+void launch_dl_density(int nv, int ns, const double* f, const double* sa, const double* visc, double* den,
+                       cudaStream_t s);
+int farfield_dl_run(ves_ctx* c, int nsrc, int ns, const double* Xsrc, const double* tang, const double* den, int nt,
+                    int ntp, const double* Xtar, const int* self_idx, const ves_near_lists* nl, double* out,
+                    cudaStream_t s);
+int near_sing_int_dl_run(ves_ctx* c, int scheme, int nv, const double* X, const double* Xup, const double* tang_up,
+                         const double* sa_up, const double* visc, const double* f, const double* vself,
+                         const ves_near_lists* nl, double h, double* LP, double* near_only, WsCarver& ws,
+                         cudaStream_t s);
 
 // RBF near-field fits (nearSingInt_rbf): adds the fits of the near pairs to LP
 int rbf_near_correct(ves_ctx* c, int nv, const double* X, const double* f, const double* vself,

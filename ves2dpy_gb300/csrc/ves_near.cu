@@ -279,9 +279,14 @@ __global__ void __launch_bounds__(128) matlab_zone_kernel(int N, int maxc, doubl
   for (int i = threadIdx.x; i < wN; i += blockDim.x) em[i] = bits[i];
 }
 
-// MATLAB correction, one warp per entry
+// MATLAB correction, one warp per entry.  DL: the layer potential at the
+// Lagrange points is the double layer (kernelDirect = exactStokesDL,
+// tstep_biem.py:236,501), with normals (ty, -tx) of the upsampled source and
+// den already scaled by (1 - visc); otherwise the single layer.
+template <bool DL>
 __global__ void matlab_correct_kernel(int N, int Nup, double h, const double* __restrict__ X,
-                                      const double* __restrict__ Xup, const double* __restrict__ den,
+                                      const double* __restrict__ Xup, const double* __restrict__ tang_up,
+                                      const double* __restrict__ den,
                                       const double* __restrict__ vself, const double* __restrict__ lag,
                                       const int* __restrict__ n_entries, int max_entries,
                                       const int* __restrict__ ent_tsj, const int* __restrict__ ent_icp,
@@ -297,7 +302,7 @@ __global__ void matlab_correct_kernel(int N, int Nup, double h, const double* __
   const double beta = 1.1;
   const double xt = X[(long long)t * 2 * N + j], yt = X[(long long)t * 2 * N + N + j];
   const double ux = (xt - nxp) / dist, uy = (yt - nyp) / dist;
-  // single layer of source vesicle s at the 6 Lagrange points
+  // layer potential of source vesicle s at the 6 Lagrange points
   double ax[6], ay[6];
 #pragma unroll
   for (int m = 0; m < 6; ++m) ax[m] = ay[m] = 0.0;
@@ -305,15 +310,26 @@ __global__ void matlab_correct_kernel(int N, int Nup, double h, const double* __
   const double* ds = den + (long long)s * 2 * Nup;
   for (int u = lane; u < Nup; u += 32) {
     const double sxu = xs[u], syu = xs[Nup + u], dxu = ds[u], dyu = ds[Nup + u];
+    double nxu = 0.0, nyu = 0.0;
+    if (DL) {
+      nxu = tang_up[(long long)s * 2 * Nup + Nup + u];
+      nyu = -tang_up[(long long)s * 2 * Nup + u];
+    }
 #pragma unroll
     for (int m = 0; m < 6; ++m) {
       const double px = nxp + beta * h * ux * (m + 1), py = nyp + beta * h * uy * (m + 1);
       const double rx = px - sxu, ry = py - syu;
       const double r2 = rx * rx + ry * ry;
-      const double lg = 0.5 * log(r2);
-      const double cc = (rx * dxu + ry * dyu) / r2;
-      ax[m] += cc * rx - lg * dxu;
-      ay[m] += cc * ry - lg * dyu;
+      if (DL) {
+        const double cc = ((rx * nxu + ry * nyu) / (r2 * r2)) * (rx * dxu + ry * dyu);
+        ax[m] += cc * rx;
+        ay[m] += cc * ry;
+      } else {
+        const double lg = 0.5 * log(r2);
+        const double cc = (rx * dxu + ry * dyu) / r2;
+        ax[m] += cc * rx - lg * dxu;
+        ay[m] += cc * ry - lg * dyu;
+      }
     }
   }
 #pragma unroll
@@ -325,7 +341,7 @@ __global__ void matlab_correct_kernel(int N, int Nup, double h, const double* __
     }
   }
   if (lane != 0) return;
-  const double inv4pi = 1.0 / (4.0 * VES_PI);
+  const double kscale = DL ? 1.0 / VES_PI : 1.0 / (4.0 * VES_PI);
   double vals[2];
   for (int comp = 0; comp < 2; ++comp) {
     // on-curve value: Lagrange interpolant of vself around icp at theta
@@ -339,7 +355,7 @@ __global__ void matlab_correct_kernel(int N, int Nup, double h, const double* __
     const double vel = horner7(coef, th);
     double pts[7];
     pts[0] = vel;
-    for (int m = 0; m < 6; ++m) pts[m + 1] = (comp == 0 ? ax[m] : ay[m]) * inv4pi;
+    for (int m = 0; m < 6; ++m) pts[m + 1] = (comp == 0 ? ax[m] : ay[m]) * kscale;
     for (int r = 0; r < 7; ++r) {
       double a = 0;
       for (int q = 0; q < 7; ++q) a = fma(lag[r * 7 + q], pts[q], a);
@@ -503,9 +519,66 @@ int near_sing_int_run(ves_ctx* c, int scheme, int precision, int nv, const doubl
   } else if (scheme == VES_NEAR_MATLAB) {
     const long long warps = nl->max_entries;
     ves_count_launch();
-    matlab_correct_kernel<<<ceil_div(warps * 32, 256), 256, 0, s>>>(N, Nup, h, X, Xup, den, vself, c->lag,
+    matlab_correct_kernel<false><<<ceil_div(warps * 32, 256), 256, 0, s>>>(N, Nup, h, X, Xup, nullptr, den, vself, c->lag,
                                                                     nl->n_entries, nl->max_entries, nl->ent_tsj,
                                                                     nl->ent_icp, nl->ent_geo, LP, near_only);
   }
   return ves_launch_check("near_sing_int");
+}
+
+// nearSingInt with kernelDirect = exactStokesDL (tstep_biem.py:236,501;
+// matlab/poten_py.m:495-692): the double-layer far field over the Nup
+// upsampled sources (den = fup sa_up 2pi/Nup (1 - visc)) with the near pairs
+// removed, plus the correction from vself = jump f + D f: the py_hh rule
+// (which uses vself only) or the MATLAB Lagrange extrapolation with the
+// double layer at the Lagrange points.
+int near_sing_int_dl_run(ves_ctx* c, int scheme, int nv, const double* X, const double* Xup, const double* tang_up,
+                         const double* sa_up, const double* visc, const double* f, const double* vself,
+                         const ves_near_lists* nl, double h, double* LP, double* near_only, WsCarver& ws,
+                         cudaStream_t s) {
+  const int N = c->N, Nup = c->Nup;
+  double* fup = ws.take<double>((size_t)nv * 2 * Nup);
+  double* den = ws.take<double>((size_t)nv * 2 * Nup);
+  int* selfidx = ws.take<int>((size_t)nv);
+  if (ws.sizing) return VES_OK;
+  if (!ws.ok()) {
+    ves_record_error(VES_ERR_WORKSPACE, "near_sing_int_dl: workspace too small");
+    return VES_ERR_WORKSPACE;
+  }
+  if (scheme != VES_NEAR_NONE && scheme != VES_NEAR_PY_HH && scheme != VES_NEAR_MATLAB) {
+    ves_record_error(VES_ERR_ARG, "near_sing_int_dl: scheme %d (the double layer supports none, py_hh, matlab)",
+                     scheme);
+    return VES_ERR_ARG;
+  }
+  if (scheme != VES_NEAR_NONE && !nl) {
+    ves_record_error(VES_ERR_ARG, "near_sing_int_dl: near lists required");
+    return VES_ERR_ARG;
+  }
+  if (nv <= 0) return VES_OK;
+  if (near_only) {
+    int rc0 = ves_cuda_status(cudaMemsetAsync(near_only, 0, (size_t)nv * 2 * N * sizeof(double), s), "zero near");
+    if (rc0) return rc0;
+  }
+  if (nv == 1) return ves_cuda_status(cudaMemsetAsync(LP, 0, (size_t)2 * N * sizeof(double), s), "zero LP");
+  launch_upsample(c, nv, 2, f, 2LL * N, fup, s);
+  launch_dl_density(nv, Nup, fup, sa_up, visc, den, s);
+  ves_count_launch();
+  identity_index_kernel<<<ceil_div(nv, 256), 256, 0, s>>>(nv, selfidx);
+  int rc = farfield_dl_run(c, nv, Nup, Xup, tang_up, den, nv, N, X, selfidx, scheme == VES_NEAR_NONE ? nullptr : nl,
+                           LP, s);
+  if (rc) return rc;
+  if (scheme == VES_NEAR_PY_HH) {
+    const long long warps = (long long)nv * nl->maxc;
+    ves_count_launch();
+    hh_apply_kernel<<<ceil_div(warps * 32, 256), 256, 0, s>>>(nv, N, Nup, nl->maxc, X, Xup, nl->cand_count,
+                                                              nl->cand_src, nl->hh_mask, vself, LP, near_only,
+                                                              nullptr);
+  } else if (scheme == VES_NEAR_MATLAB) {
+    const long long warps = nl->max_entries;
+    ves_count_launch();
+    matlab_correct_kernel<true><<<ceil_div(warps * 32, 256), 256, 0, s>>>(
+        N, Nup, h, X, Xup, tang_up, den, vself, c->lag, nl->n_entries, nl->max_entries, nl->ent_tsj, nl->ent_icp,
+        nl->ent_geo, LP, near_only);
+  }
+  return ves_launch_check("near_sing_int_dl");
 }

@@ -93,6 +93,70 @@ __global__ void upsample_deriv_kernel(int N, int Nup, int m, const double* __res
   }
 }
 
+// Geometry of the upsampled curve from the first and second derivatives of
+// the trig interpolant at the Nup grid.  They equal the FFT derivatives of
+// interpft(X, Nup) on its own grid (diffProp of capsules(Xup),
+// curve_batch_compile.py:400-423) up to rounding, with an error that does not
+// grow with Nup as a fine-grid circulant derivative's does.
+__global__ void upsample_geom_kernel(int N, int Nup, int m, const double* __restrict__ pc,
+                                     const double* __restrict__ pcd, const double* __restrict__ pcdd,
+                                     const double* __restrict__ X, double* __restrict__ Xup,
+                                     double* __restrict__ sa, double* __restrict__ tang, double* __restrict__ cur) {
+  extern __shared__ double sh[];
+  double* x = sh;
+  double* y = x + N;
+  double* p = y + N;
+  double* pd = p + Nup;
+  double* pdd = pd + Nup;
+  const int k = blockIdx.x;
+  const double* Xk = X + (long long)k * 2 * N;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    x[i] = Xk[i];
+    y[i] = Xk[N + i];
+  }
+  for (int i = threadIdx.x; i < Nup; i += blockDim.x) {
+    p[i] = pc[i];
+    pd[i] = pcd[i];
+    pdd[i] = pcdd[i];
+  }
+  __syncthreads();
+  for (int u = threadIdx.x; u < Nup; u += blockDim.x) {
+    double sx = 0, sy = 0, dx = 0, dy = 0, ddx = 0, ddy = 0;
+    int r = u;
+    for (int i = 0; i < N; ++i) {
+      sx = fma(p[r], x[i], sx);
+      sy = fma(p[r], y[i], sy);
+      dx = fma(pd[r], x[i], dx);
+      dy = fma(pd[r], y[i], dy);
+      ddx = fma(pdd[r], x[i], ddx);
+      ddy = fma(pdd[r], y[i], ddy);
+      r -= m;
+      if (r < 0) r += Nup;
+    }
+    const long long o = (long long)k * 2 * Nup;
+    const double jac = sqrt(dx * dx + dy * dy);
+    if (Xup) {
+      Xup[o + u] = sx;
+      Xup[o + Nup + u] = sy;
+    }
+    if (sa) sa[(long long)k * Nup + u] = jac;
+    if (tang) {
+      tang[o + u] = dx / jac;
+      tang[o + Nup + u] = dy / jac;
+    }
+    if (cur) cur[(long long)k * Nup + u] = (dx * ddy - dy * ddx) / (jac * jac * jac);
+  }
+}
+
+void launch_upsample_geom(const ves_ctx* c, int nv, const double* X, double* Xup, double* sa, double* tang,
+                          double* cur, cudaStream_t s) {
+  if (nv <= 0) return;
+  const size_t sh = (size_t)(2 * c->N + 3 * c->Nup) * sizeof(double);
+  if (sh > 48 * 1024) cudaFuncSetAttribute(upsample_geom_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh);
+  ves_count_launch();
+  upsample_geom_kernel<<<nv, 256, sh, s>>>(c->N, c->Nup, c->m, c->pc, c->pcd, c->pcdd, X, Xup, sa, tang, cur);
+}
+
 void launch_upsample_deriv(const ves_ctx* c, int nv, const double* X, double* Xup, double* dXup,
                            double* sa_up, cudaStream_t s) {
   if (nv <= 0) return;
@@ -395,20 +459,30 @@ __global__ void assemble_ben_kernel(int N, const double* __restrict__ D4, double
   }
 }
 
-// M[k] (3N x 3N) from GB = G*Ben (2N x 2N), GT = G*Ten (2N x N), Div (N x 2N)
+// M[k] (3N x 3N) from GB = G*Ben (2N x 2N), GT = G*Ten (2N x N), Div (N x 2N).
+// With a viscosity contrast (Dm, alpha given) the position rows are the
+// self-interaction of the matvec, [I - D/alpha + dt*kappa*G*Ben/alpha,
+// -dt*G*Ten/alpha]; the reference's own assembly of that case
+// (tstep_biem.py:331-334) adds the 2N x N block G*Ten to the 2N x 2N one and
+// stops with a shape error.
 __global__ void assemble_precond_kernel(int N, double dt, double kappa, const double* __restrict__ GB,
                                         const double* __restrict__ GT, const double* __restrict__ Div,
+                                        const double* __restrict__ Dm, const double* __restrict__ alpha,
                                         double* __restrict__ M) {
   const int k = blockIdx.y;
   const int n3 = 3 * N, n2 = 2 * N;
+  const double ia = alpha ? 1.0 / alpha[k] : 1.0;
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n3 * n3; idx += gridDim.x * blockDim.x) {
     const int r = idx / n3, cc = idx % n3;
     double v;
     if (r < n2) {
-      if (cc < n2)
-        v = (r == cc ? 1.0 : 0.0) + dt * kappa * GB[(long long)k * n2 * n2 + (long long)r * n2 + cc];
-      else
-        v = -dt * GT[(long long)k * n2 * N + (long long)r * N + (cc - n2)];
+      if (cc < n2) {
+        v = (r == cc ? 1.0 : 0.0);
+        if (Dm) v -= Dm[(long long)k * n2 * n2 + (long long)r * n2 + cc] * ia;
+        v += (dt * kappa * GB[(long long)k * n2 * n2 + (long long)r * n2 + cc]) * ia;
+      } else {
+        v = (-dt * GT[(long long)k * n2 * N + (long long)r * N + (cc - n2)]) * ia;
+      }
     } else {
       v = (cc < n2) ? Div[(long long)k * N * n2 + (long long)(r - n2) * n2 + cc] : 0.0;
     }
@@ -420,7 +494,7 @@ __global__ void assemble_precond_kernel(int N, double dt, double kappa, const do
 // C = (Are Are - Aim Aim) + i (Are Aim + Aim Are); D4 = Cr Cr - Ci Ci.
 int derivs_and_precond(ves_ctx* c, int nv, const double* isa, const double* tang, const double* G,
                        double dt, double kappa, double* Ben, double* Ten, double* Div, double* M,
-                       WsCarver& ws, cudaStream_t s) {
+                       WsCarver& ws, cudaStream_t s, const double* Dm, const double* alpha) {
   const int N = c->N;
   const size_t NN = (size_t)N * N;
   double* Are = ws.take<double>(NN * nv);
@@ -465,7 +539,7 @@ int derivs_and_precond(ves_ctx* c, int nv, const double* isa, const double* tang
     launch_bgemm_f64(nv, 2 * N, N, 2 * N, 1.0, G, 2 * N, sG, Ten, N, 2 * sN, 0.0, GT, N, 2 * sN, s);
     dim3 g3(ceil_div(9 * NN, 256), nv);
     ves_count_launch();
-    assemble_precond_kernel<<<g3, 256, 0, s>>>(N, dt, kappa, GB, GT, Div, M);
+    assemble_precond_kernel<<<g3, 256, 0, s>>>(N, dt, kappa, GB, GT, Div, Dm, alpha, M);
   }
   return ves_launch_check("derivs_and_precond");
 }

@@ -82,16 +82,43 @@ __global__ void pack_kernel(int nv, int N, const double* __restrict__ A2, const 
   out[idx] = (r < 2 * N) ? A2[k * 2 * N + r] : B1[k * N + (r - 2 * N)];
 }
 
-// out = (X + dt * (frepG + frepN)) + dt * v, the repulsion terms when present
-// (tstep_biem.py:257-270: Frepulsion = G rep + nearSingInt_rbf(rep), then vInf)
-__global__ void rhs_pos_kernel(long long n, double dt, const double* __restrict__ X, const double* __restrict__ v,
-                               const double* __restrict__ frepG, const double* __restrict__ frepN,
+// rhs1 in the reference's order (tstep_biem.py:242-270), each term scaled by
+// 1/alpha (alpha = (1 + visc)/2, 1 without a contrast):
+//   X - (Fdlp + D X) / alpha + dt (G rep + nearSingInt_rbf(rep)) / alpha + dt vInf / alpha
+__global__ void rhs_pos_kernel(long long n, int N, double dt, const double* __restrict__ X,
+                               const double* __restrict__ v, const double* __restrict__ frepG,
+                               const double* __restrict__ frepN, const double* __restrict__ fdl,
+                               const double* __restrict__ dx, const double* __restrict__ alpha,
                                double* __restrict__ out) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const double ia = alpha ? 1.0 / alpha[i / (2 * N)] : 1.0;
   double r = X[i];
-  if (frepG) r = r + dt * (frepG[i] + frepN[i]);
-  out[i] = r + dt * v[i];
+  if (fdl) r = r - (fdl[i] + dx[i]) * ia;
+  if (frepG) r = r + (dt * (frepG[i] + frepN[i])) * ia;
+  out[i] = r + (dt * v[i]) * ia;
+}
+
+// alpha = (1 + visc) / 2 (tstep_biem.py:195)
+__global__ void alpha_kernel(int nv, const double* __restrict__ visc, double* __restrict__ alpha) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nv) alpha[k] = (1.0 + visc[k]) / 2;
+}
+
+// vself of the double layer: X jump + D X, jump = (1 - visc)/2 (tstep_biem.py:233-234)
+__global__ void dl_self_kernel(long long n, int N, const double* __restrict__ visc, const double* __restrict__ X,
+                               long long xs, const double* __restrict__ DX, double* __restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const long long k = i / (2 * N), r = i % (2 * N);
+  out[i] = X[k * xs + r] * (0.5 * (1 - visc[k])) + DX[i];
+}
+
+// [nv][3][N] -> [nv][2][N] (the positions of a GMRES vector)
+__global__ void take_pos_kernel(long long n, int N, const double* __restrict__ v, double* __restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = v[(i / (2 * N)) * 3 * N + i % (2 * N)];
 }
 
 __global__ void unpack_kernel(int nv, int N, const double* __restrict__ x, double* __restrict__ X,
@@ -105,15 +132,26 @@ __global__ void unpack_kernel(int nv, int N, const double* __restrict__ x, doubl
     sig[k * N + (r - 2 * N)] = x[idx];
 }
 
-// valPos = ((-(dt*Gf)) - dt*LP) + Xm  (tstep_biem.py:541-576, alpha = 1)
+// valPos = -(dt Gf)/alpha - D Xm/alpha - (dt LP)/alpha - Fdlp/alpha + Xm
+// (tstep_biem.py:541-576; alpha = 1 and no double-layer terms without a contrast)
 __global__ void combine_pos_kernel(int nv, int N, double dt, const double* __restrict__ v,
                                    const double* __restrict__ Gf, const double* __restrict__ LP,
-                                   double* __restrict__ out) {
+                                   const double* __restrict__ alpha, const double* __restrict__ DX,
+                                   const double* __restrict__ Fdl, double* __restrict__ out) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long long)nv * 2 * N) return;
   const long long k = idx / (2 * N), r = idx % (2 * N);
-  double val = -(dt * Gf[idx]);
-  val -= dt * LP[idx];
+  double val;
+  if (alpha) {
+    const double a = alpha[k];
+    val = -((dt * Gf[idx]) / a);
+    val -= DX[idx] / a;
+    val -= (dt * LP[idx]) / a;
+    val -= Fdl[idx] / a;
+  } else {
+    val = -(dt * Gf[idx]);
+    val -= dt * LP[idx];
+  }
   val += v[k * 3 * N + r];
   out[k * 3 * N + r] = val;
 }
@@ -153,6 +191,9 @@ struct StepState {
   // geometry of the step
   double *sa, *isa, *tang, *Xup, *sa_up, *G, *LU;
   int* piv;
+  // viscosity contrast (null without one): contrasts, alpha, D, upsampled tangents
+  const double* visc;
+  double *alpha, *D, *tang_up, *Xm, *DX, *vdl, *Fdl;
   ves_near_lists nl;
   double h;
   // matvec temporaries
@@ -160,6 +201,7 @@ struct StepState {
   char* scratch;
   size_t scratch_bytes;
   int matvecs;
+  int dl_scheme;  // near scheme of the double layer: py_hh for the py lists, else the step's
 };
 
 // out = A v (time_matvec, tstep_biem.py:430-610), v and out in [nv][3][N]
@@ -173,8 +215,22 @@ int matvec(StepState& S, const double* v, double* out) {
   int rc = near_sing_int_run(c, S.prm->near_scheme, S.prm->farfield_precision, nv, S.X, S.sa_up, S.Xup, S.f, S.Gf,
                              &S.nl, S.h, S.LP, nullptr, sub, S.s);
   if (rc) return rc;
+  if (S.visc) {
+    // D Xm and the double layer of Xm (tstep_biem.py:489, 497-501)
+    const long long n2 = (long long)nv * 2 * N;
+    ves_count_launch();
+    take_pos_kernel<<<ceil_div(n2, 256), 256, 0, S.s>>>(n2, N, v, S.Xm);
+    launch_bgemv_f64(nv, 2 * N, 2 * N, S.D, S.Xm, 2LL * N, S.DX, 2LL * N, S.s);
+    ves_count_launch();
+    dl_self_kernel<<<ceil_div(n2, 256), 256, 0, S.s>>>(n2, N, S.visc, S.Xm, 2LL * N, S.DX, S.vdl);
+    WsCarver sub2(S.scratch, S.scratch_bytes);
+    if ((rc = near_sing_int_dl_run(c, S.dl_scheme, nv, S.X, S.Xup, S.tang_up, S.sa_up, S.visc, S.Xm, S.vdl, &S.nl,
+                                   S.h, S.Fdl, nullptr, sub2, S.s)))
+      return rc;
+  }
   ves_count_launch();
-  combine_pos_kernel<<<ceil_div((long long)nv * 2 * N, 256), 256, 0, S.s>>>(nv, N, S.prm->dt, v, S.Gf, S.LP, out);
+  combine_pos_kernel<<<ceil_div((long long)nv * 2 * N, 256), 256, 0, S.s>>>(nv, N, S.prm->dt, v, S.Gf, S.LP, S.alpha,
+                                                                            S.DX, S.Fdl, out);
   launch_surface_div(c, nv, S.isa, S.tang, v, 3LL * N, out + 2 * N, 3LL * N, S.s);
   return ves_launch_check("matvec");
 }
@@ -396,6 +452,20 @@ static int biem_step_impl(ves_ctx* c, const ves_step_params* prm, int nv, const 
   S.nl.ent_tsj = ws.take<int>((size_t)maxe * 3);
   S.nl.ent_icp = ws.take<int>((size_t)maxe);
   S.nl.ent_geo = ws.take<double>((size_t)maxe * 4);
+  const bool vc = prm && prm->visc_cont != nullptr;  // viscosity contrast: double-layer terms
+  S.visc = vc ? prm->visc_cont : nullptr;
+  if (vc) {
+    S.alpha = ws.take<double>(nv);
+    S.D = ws.take<double>((size_t)nv * 4 * N * N);
+    S.tang_up = ws.take<double>((size_t)nv * 2 * Nup);
+    S.Xm = ws.take<double>((size_t)nv * 2 * N);
+    S.DX = ws.take<double>((size_t)nv * 2 * N);
+    S.vdl = ws.take<double>((size_t)nv * 2 * N);
+    S.Fdl = ws.take<double>((size_t)nv * 2 * N);
+  }
+  S.dl_scheme = (prm && (prm->near_scheme == VES_NEAR_PY_HH || prm->near_scheme == VES_NEAR_PY_RBF))
+                    ? VES_NEAR_PY_HH
+                    : (prm ? prm->near_scheme : VES_NEAR_NONE);
   GmresBufs B;
   B.V = ws.take<double>((size_t)(restart + 1) * n);
   B.w = ws.take<double>(n);
@@ -436,6 +506,15 @@ static int biem_step_impl(ves_ctx* c, const ves_step_params* prm, int nv, const 
     near_sing_int_run(c, prm->near_scheme, prm->farfield_precision, nv, nullptr, nullptr, nullptr, nullptr, nullptr,
                       nullptr, 0, nullptr, nullptr, w, s);
     scratch = std::max(scratch, w.off);
+  }
+  if (vc) {
+    WsCarver w(nullptr, 0);
+    stokes_dl_matrix(c, nv, nullptr, nullptr, prm->sl_precision, nullptr, w, s);
+    scratch = std::max(scratch, w.off);
+    WsCarver w2(nullptr, 0);
+    near_sing_int_dl_run(c, S.dl_scheme, nv, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                         0, nullptr, nullptr, w2, s);
+    scratch = std::max(scratch, w2.off);
   }
   if (prm->repulsion) {  // force, G force, its near-field integral (RBF), the force's scratch
     WsCarver w(nullptr, 0);
@@ -479,6 +558,14 @@ static int biem_step_impl(ves_ctx* c, const ves_step_params* prm, int nv, const 
     WsCarver sub(S.scratch, S.scratch_bytes);
     if ((rc = alpert_sl_matrix(c, nv, X, prm->sl_precision, S.G, sub, s))) goto done;
   }
+  if (vc) {
+    // alpha, the upsampled tangents and poten.stokesDLmatrix (tstep_biem.py:195, 203-205)
+    ves_count_launch();
+    alpha_kernel<<<ceil_div(nv, 256), 256, 0, s>>>(nv, S.visc, S.alpha);
+    launch_upsample_geom(c, nv, X, nullptr, nullptr, S.tang_up, nullptr, s);
+    WsCarver sub(S.scratch, S.scratch_bytes);
+    if ((rc = stokes_dl_matrix(c, nv, X, S.visc, prm->sl_precision, S.D, sub, s))) goto done;
+  }
   S.h = 0.0;
   if (prm->near_scheme == VES_NEAR_MATLAB) {
     WsCarver sub(S.scratch, S.scratch_bytes);
@@ -495,8 +582,19 @@ static int biem_step_impl(ves_ctx* c, const ves_step_params* prm, int nv, const 
     WsCarver sub(S.scratch, S.scratch_bytes);
     if ((rc = near_zone_py(c, nv, X, S.Xup, 0.0, &S.nl, sub, s))) goto done;
   }
-  // right-hand side [X + dt*vinf; surfaceDiv(X)]
+  // right-hand side [X + dt*vinf; surfaceDiv(X)], with the double layer of X
+  // (Fdlp + D X, tstep_biem.py:231-244) and the repulsion when present
   launch_bg_flow(nv, N, prm->flow, prm->speed, prm->chan_width, prm->vortex_size, X, vinf, s);
+  if (vc) {
+    const long long n2 = (long long)nv * 2 * N;
+    launch_bgemv_f64(nv, 2 * N, 2 * N, S.D, X, 2LL * N, S.DX, 2LL * N, s);
+    ves_count_launch();
+    dl_self_kernel<<<ceil_div(n2, 256), 256, 0, s>>>(n2, N, S.visc, X, 2LL * N, S.DX, S.vdl);
+    WsCarver sub(S.scratch, S.scratch_bytes);
+    if ((rc = near_sing_int_dl_run(c, S.dl_scheme, nv, X, S.Xup, S.tang_up, S.sa_up, S.visc, X, S.vdl, &S.nl, S.h,
+                                   S.Fdl, nullptr, sub, s)))
+      goto done;
+  }
   if (prm->repulsion && nv > 1) {
     // repulsion on the current shapes: G rep + nearSingInt_rbf(rep) (tstep_biem.py:250-264)
     WsCarver sub(S.scratch, S.scratch_bytes);
@@ -511,25 +609,31 @@ static int biem_step_impl(ves_ctx* c, const ves_step_params* prm, int nv, const 
                                 S.h, rN, nullptr, sub, s)))
       goto done;
     ves_count_launch();
-    rhs_pos_kernel<<<ceil_div((long long)nv * 2 * N, 256), 256, 0, s>>>((long long)nv * 2 * N, prm->dt, X, vinf, rG, rN,
-                                                                        vinf);
+    rhs_pos_kernel<<<ceil_div((long long)nv * 2 * N, 256), 256, 0, s>>>(
+        (long long)nv * 2 * N, N, prm->dt, X, vinf, rG, rN, vc ? S.Fdl : nullptr, S.DX, S.alpha, vinf);
   } else {
     ves_count_launch();
-    rhs_pos_kernel<<<ceil_div((long long)nv * 2 * N, 256), 256, 0, s>>>((long long)nv * 2 * N, prm->dt, X, vinf,
-                                                                        nullptr, nullptr, vinf);
+    rhs_pos_kernel<<<ceil_div((long long)nv * 2 * N, 256), 256, 0, s>>>(
+        (long long)nv * 2 * N, N, prm->dt, X, vinf, nullptr, nullptr, vc ? S.Fdl : nullptr, S.DX, S.alpha, vinf);
   }
   launch_surface_div(c, nv, S.isa, S.tang, X, 2LL * N, rhs2, N, s);
   ves_count_launch();
   pack_kernel<<<ceil_div(n, 256), 256, 0, s>>>(nv, N, vinf, rhs2, B.b);
-  ves_count_launch();
-  pack_kernel<<<ceil_div(n, 256), 256, 0, s>>>(nv, N, X, sigma, B.x);
+  if (prm->use_preco) {
+    ves_count_launch();
+    pack_kernel<<<ceil_div(n, 256), 256, 0, s>>>(nv, N, X, sigma, B.x);
+  } else {
+    // without the preconditioner the reference calls gmres without x0 (tstep_biem.py:383)
+    if ((rc = ves_cuda_status(cudaMemsetAsync(B.x, 0, n * sizeof(double), s), "x0"))) goto done;
+  }
   // preconditioner
   if (prm->use_preco) {
     WsCarver sub(S.scratch, S.scratch_bytes);
     double* Ben = nullptr;
     double* Ten = sub.take<double>((size_t)nv * 2 * N * N);
     double* Div = sub.take<double>((size_t)nv * 2 * N * N);
-    if ((rc = derivs_and_precond(c, nv, S.isa, S.tang, S.G, prm->dt, prm->kappa, Ben, Ten, Div, S.LU, sub, s)))
+    if ((rc = derivs_and_precond(c, nv, S.isa, S.tang, S.G, prm->dt, prm->kappa, Ben, Ten, Div, S.LU, sub, s,
+                                 vc ? S.D : nullptr, vc ? S.alpha : nullptr)))
       goto done;
     if ((rc = launch_lu_factor(c, nv, 3 * N, S.LU, S.piv, s))) goto done;
   }

@@ -20,6 +20,22 @@ LAGRANGE_INTERP = [
     [1.00, 0.00, 0.00, 0.00, 0.00, 0.00, 0.00]]
 
 
+def visc_tensor(viscCont, nv, device):
+    """Viscosity contrasts as a device float64 vector of nv entries."""
+    v = torch.as_tensor(1.0 if viscCont is None else viscCont, dtype=torch.float64)
+    if v.dim() == 0:
+        v = v.repeat(nv)
+    v = v.reshape(-1)
+    if v.numel() != nv:
+        raise ValueError(f"viscCont has {v.numel()} entries for {nv} vesicles")
+    return v.to(device).contiguous()
+
+
+def _is_double_layer(kernel) -> bool:
+    f = getattr(kernel, "__func__", kernel)
+    return f is Poten.exactStokesDL or getattr(f, "__name__", "") == "exactStokesDL"
+
+
 class Poten:
     """Poten(N) (poten.py:14-37): the quadrature tables live in the device
     context of the C library, created once per (N, device)."""
@@ -54,7 +70,78 @@ class Poten:
                                                  nat.stream_ptr(fv.device)), "exactStokesSLdiag")
         return from_vm(out)
 
+    def stokesDLmatrix(self, vesicle, precision: str = "fp64"):
+        """Double-layer matrix D (2N, 2N, nv) (poten.py:102-175): trapezoid rule
+        on the Nup-upsampled curve with the curvature limit on the diagonal,
+        restricted to N points; zero for vesicles without a viscosity
+        contrast.  ``precision`` "fp32c" does the restriction products in FP32."""
+        ctx, nv = self._ctx, vesicle.nv
+        Xv = to_vm(as_device_f64(vesicle.X))
+        visc = visc_tensor(vesicle.viscCont, nv, Xv.device)
+        D = torch.empty(nv, 2 * self.N, 2 * self.N, dtype=torch.float64, device=Xv.device)
+        prec = nat.PREC[precision]
+        ws = ctx.workspace(ctx.lib.ves_stokes_dl_matrix_workspace(ctx.handle, nv, prec))
+        nat.check(ctx.lib.ves_stokes_dl_matrix(ctx.handle, nv, Xv.data_ptr(), visc.data_ptr(), prec, D.data_ptr(),
+                                               ws.data_ptr(), ws.numel(), nat.stream_ptr(Xv.device)),
+                  "stokesDLmatrix")
+        return mats_from_vm(D)
+
+    def exactStokesDLdiag(self, vesicle, D, f):
+        """Per-vesicle D[:, :, k] @ f[:, k] (poten.py:227-238)."""
+        return self.exactStokesSLdiag(vesicle, D, f)
+
     # -- between vesicles ------------------------------------------------------
+    def exactStokesDL(self, vesicle, f, Xtar=None, K1=None):
+        """Double layer of vesicles K1 (density f, scaled by 1 - viscCont) at
+        every column of Xtar (poten.py:399-441), in FP64."""
+        Xtar = as_device_f64(Xtar)
+        if Xtar.dim() == 1:
+            Xtar = Xtar.unsqueeze(1)
+        K1 = list(range(vesicle.nv)) if K1 is None else [int(k) for k in K1]
+        N, ntp, ncol = vesicle.N, Xtar.shape[0] // 2, Xtar.shape[1]
+        dev = Xtar.device
+        idx = torch.tensor(K1, dtype=torch.long, device=dev)
+        Xs = to_vm(as_device_f64(vesicle.X).index_select(1, idx))
+        ts = to_vm(as_device_f64(vesicle.xt).index_select(1, idx))
+        fs = to_vm(as_device_f64(f).index_select(1, idx))
+        sas = to_vm(as_device_f64(vesicle.sa).index_select(1, idx))
+        visc = visc_tensor(vesicle.viscCont, vesicle.nv, dev).index_select(0, idx).contiguous()
+        lib, st = nat.load_library(), nat.stream_ptr(dev)
+        den = torch.empty_like(fs)
+        nat.check(lib.ves_dl_density(len(K1), N, fs.data_ptr(), sas.data_ptr(), visc.data_ptr(), den.data_ptr(), st),
+                  "exactStokesDL density")
+        Xt = to_vm(Xtar)
+        out = torch.empty(ncol, 2 * ntp, dtype=torch.float64, device=dev)
+        nat.check(lib.ves_farfield_dl(self._ctx.handle, len(K1), N, Xs.data_ptr(), ts.data_ptr(), den.data_ptr(),
+                                      ncol, ntp, Xt.data_ptr(), None, None, out.data_ptr(), st), "exactStokesDL")
+        return from_vm(out)
+
+    def _near_dl(self, scheme, vesicleSou, f, selfMat, Near):
+        """nearSingInt with kernelDirect = exactStokesDL on the device."""
+        X = as_device_f64(vesicleSou.X)
+        N, nv = X.shape[0] // 2, X.shape[1]
+        ctx = self._ctx
+        Xv = to_vm(X)
+        st = nat.stream_ptr(X.device)
+        Xup = torch.empty(nv, 2 * self.Nup, dtype=torch.float64, device=X.device)
+        sa_up = torch.empty(nv, self.Nup, dtype=torch.float64, device=X.device)
+        tang_up = torch.empty(nv, 2 * self.Nup, dtype=torch.float64, device=X.device)
+        nat.check(ctx.lib.ves_upsample_geometry(ctx.handle, nv, Xv.data_ptr(), Xup.data_ptr(), sa_up.data_ptr(),
+                                                tang_up.data_ptr(), None, st), "upsample geometry")
+        visc = visc_tensor(vesicleSou.viscCont, nv, X.device)
+        fv = to_vm(as_device_f64(f))
+        vself = to_vm(as_device_f64(selfMat(f))) if selfMat is not None else None
+        LP = torch.empty(nv, 2 * N, dtype=torch.float64, device=X.device)
+        ws = ctx.workspace(ctx.lib.ves_near_sing_int_dl_workspace(ctx.handle, nv))
+        stc = Near.struct() if Near is not None else None
+        h = Near.h if Near is not None else 0.0
+        nat.check(ctx.lib.ves_near_sing_int_dl(ctx.handle, nat.NEAR[scheme], nv, Xv.data_ptr(), Xup.data_ptr(),
+                                               tang_up.data_ptr(), sa_up.data_ptr(), visc.data_ptr(), fv.data_ptr(),
+                                               nat.ptr(vself), ctypes.byref(stc) if stc is not None else None,
+                                               float(h), LP.data_ptr(), None, ws.data_ptr(), ws.numel(), st),
+                  "nearSingInt (double layer)")
+        return from_vm(LP)
+
     def exactStokesSL(self, vesicle, f, Xtar=None, K1=None, precision: str = "fp64"):
         """Single layer of vesicles K1 at the single target column Xtar (poten.py:280-336)."""
         Xtar = as_device_f64(Xtar)
@@ -106,6 +193,8 @@ class Poten:
             return z, z
         if not isinstance(NearV2V, NearZone) or NearV2V.scheme != "py_hh":
             raise TypeError("NearV2V must come from naiveNearZoneInfo")
+        if _is_double_layer(kernelDirect):
+            return self._near_dl("py_hh", vesicleSou, f, selfMat, NearV2V), None
         return self._near_common("py_hh", vesicleSou, f, selfMat, NearV2V, precision)
 
     def nearSingInt_rbf(self, vesicleSou, f, selfMat, NearV2V, kernelDirect=None, vesicleTar=None, tEqualS=True,
@@ -128,11 +217,23 @@ class Poten:
                     precision: str = "fp64"):
         """MATLAB nearSingInt (matlab/poten_py.m:495-692) with NearStruct from
         capsules.getZone: trapezoid contribution of the near source removed and
-        replaced by the 7-point Lagrange extrapolation along the normal."""
+        replaced by the 7-point Lagrange extrapolation along the normal.
+
+        With ``kernelDirect = exactStokesDL`` (the viscosity-contrast calls at
+        tstep_biem.py:236,501) the layer potential is the double layer; the
+        near lists may then also come from naiveNearZoneInfo (the step's
+        ``NearV2V``), whose near pairs get the nearSingInt_hh correction."""
         if not tEqualS or (vesicleTar is not None and vesicleTar is not vesicleSou):
             raise NotImplementedError("nearSingInt: only sources == targets (tEqualS)")
         if vesicleSou.nv == 1:
             return torch.zeros_like(as_device_f64(vesicleSou.X))
+        if _is_double_layer(kernelDirect):
+            if NearStruct is None:
+                return self._near_dl("none", vesicleSou, f, None, None)
+            if not isinstance(NearStruct, NearZone):
+                raise TypeError("NearStruct must come from capsules.getZone or naiveNearZoneInfo")
+            return self._near_dl("matlab" if NearStruct.scheme == "matlab" else "py_hh", vesicleSou, f, selfMat,
+                                 NearStruct)
         if NearStruct is None:
             return self._near_common("none", vesicleSou, f, None, None, precision)[0]
         if not isinstance(NearStruct, NearZone) or NearStruct.scheme != "matlab":

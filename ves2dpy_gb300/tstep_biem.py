@@ -18,6 +18,11 @@ from .layout import as_device_f64, from_vm, to_vm
 class TStepBiem:
     """tstep_biem.py:25-153.
 
+    With a viscosity contrast (``prams['viscCont'] != 1``) the step adds the
+    double-layer terms of the reference (D, Fdlp, alpha = (1 + visc)/2); the
+    double layer's near pairs use the py_hh rule with the naiveNearZoneInfo
+    lists ("py_hh", "py_rbf") or the MATLAB rule ("matlab").
+
     Extra keyword options select the device arithmetic:
     ``near`` ("py_hh" = the reference's nearSingInt_hh, "py_rbf" = its
     nearSingInt_rbf as in the newtorch step, "matlab" = the MATLAB
@@ -29,9 +34,6 @@ class TStepBiem:
                  sl_precision: str = "fp32c", device=None):
         if Xwalls is not None:
             raise NotImplementedError("confined flows (walls) are not supported by the device stepper")
-        visc = torch.as_tensor(prams.get("viscCont", 1.0), dtype=torch.float64)
-        if torch.any(visc != 1):
-            raise NotImplementedError("viscosity contrast != 1 is not supported by the device stepper")
         X = as_device_f64(X, device)
         self.device = X.device
         self.N = X.shape[0] // 2
@@ -40,6 +42,10 @@ class TStepBiem:
         self.dt = float(prams["dt"])
         self.kappa = float(prams["kappa"])
         self.viscCont = prams.get("viscCont")
+        # viscosity contrast (tstep_biem.py:195-244): double-layer terms when any vesicle has visc != 1
+        from .poten import visc_tensor
+        visc = visc_tensor(self.viscCont, self.nv, self.device)
+        self._visc = visc if bool(torch.any(visc != 1)) else None
         self.gmresTol = float(prams["gmresTol"])
         self.gmresMaxIter = int(prams["gmresMaxIter"])
         self.farFieldSpeed = float(prams.get("farFieldSpeed", 1.0))
@@ -87,6 +93,7 @@ class TStepBiem:
         p.repulsion = 1 if self.repulsion else 0
         p.rep_strength = self.repStrength
         p.min_dist = self.minDist
+        p.visc_cont = None if self._visc is None else self._visc.data_ptr()
         return p
 
     def workspace_bytes(self) -> int:

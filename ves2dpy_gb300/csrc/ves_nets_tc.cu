@@ -29,6 +29,7 @@
 // each CTA walks a contiguous range of (group, vesicle) items, loading a
 // group's weight image into shared memory once per group it meets.
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -312,13 +313,15 @@ __device__ __forceinline__ Seg next_seg(long long lo, long long hi, int nv) {
 
 // KC1 / KCD: compile-time K chunk counts of the two conv pairs' outputs (0:
 // read them from the geometry); fixed counts let every epilogue and issue
-// loop unroll.
-template <int KC1, int KCD>
-__global__ void __launch_bounds__(kThreads, 1) down_kernel(KArgs a) {
+// loop unroll.  NG: warp groups per CTA, each running its own items (2: 256
+// TMEM columns each; 3: 128 columns each, when N1 + N2 <= 128 and three
+// groups' arrays fit in shared memory).
+template <int KC1, int KCD, int NG>
+__global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
   extern __shared__ __align__(128) unsigned char sm[];
-  __shared__ uint64_t bar[2], xbar[2];  // per warp group: MMA completion, input arrival
+  __shared__ uint64_t bar[NG], xbar[NG];  // per warp group: MMA completion, input arrival
   __shared__ uint32_t tbase;
-  __shared__ int fail[2];
+  __shared__ int fail[NG];
   const Geo& g = a.g;
   const int kc1 = KC1 ? KC1 : kc1, kcd = KCD ? KCD : kcd;
   const int L = g.L, L2 = L / 2, L4 = L / 4;
@@ -327,23 +330,23 @@ __global__ void __launch_bounds__(kThreads, 1) down_kernel(KArgs a) {
   const int qd = warp & 3;                                       // TMEM lane quarter = position block
   const Range rg = my_items(a.items);
   if (rg.lo >= rg.hi) return;
-  const uint32_t ncols = 512;  // 256 columns per warp group (one CTA per SM)
+  const uint32_t ncols = 512;  // all of TMEM (one CTA per SM)
   if (tid == 0) {
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < NG; ++k) {
       tc_mbar_init(&bar[k], 1);
       tc_mbar_init(&xbar[k], 1);
+      fail[k] = 0;
     }
     tc_mbar_fence_init();
-    fail[0] = fail[1] = 0;
   }
   if (warp == 0) tc_tmem_alloc(&tbase, ncols);
-  zero16(sm + g.dxs, g.dsmem - g.dxs);  // K padding of the activation arrays stays zero
+  zero16(sm + g.dxs, NG * g.dgrp + 128 * 16);  // K padding of the activation arrays stays zero
   tc_fence_async_smem();
   tc_fence_before_sync();
   __syncthreads();
   tc_fence_after_sync();
   const int N1 = kc1 * 8, N2 = kcd * 8;
-  const uint32_t tcol = tbase + 256 * wg;
+  const uint32_t tcol = tbase + (NG == 2 ? 256 : 128) * wg;
   const uint32_t d1 = tcol, d2 = tcol + N1;
   const uint32_t sbase = tc_smem_u32(sm);
   const int goff = wg * g.dgrp;
@@ -403,7 +406,7 @@ __global__ void __launch_bounds__(kThreads, 1) down_kernel(KArgs a) {
     tc_fence_async_smem();  // weights (and the zeroed padding) -> tensor core, for both groups
     __syncthreads();
     if (sg.lo + wg < sg.hi) fetch_x(sg.lo + wg);
-    for (long long it = sg.lo + wg; it < sg.hi; it += 2) {
+    for (long long it = sg.lo + wg; it < sg.hi; it += NG) {
       const long long v = it % a.nv;
       if (!group_wait(&xbar[wg], xphase, a.st, 20, wg, &fail[wg])) {
         failed = true;
@@ -413,7 +416,7 @@ __global__ void __launch_bounds__(kThreads, 1) down_kernel(KArgs a) {
       xpend = false;
       convert_x();
       group_sync_for_mma(wg);  // xs complete; xf fully read
-      if (it + 2 < sg.hi) fetch_x(it + 2);
+      if (it + NG < sg.hi) fetch_x(it + NG);
       // conv pair 1: D1[p][o], p < L/2 on the lanes, o < n1 in the columns
       if (gt == 0) {
         const uint32_t idesc = tc_idesc_bf16(128, N1);
@@ -870,6 +873,17 @@ int tcnet_pack(const ves_net_block& b, int G, int L, const float* const* p, std:
   return VES_OK;
 }
 
+// Warp groups allowed in the down kernel (VES_TC_DOWN_GROUPS=2 forces two;
+// read once).
+static int tcnet_down_groups_max() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = getenv("VES_TC_DOWN_GROUPS");
+    v = (e && atoi(e) == 2) ? 2 : 3;
+  }
+  return v;
+}
+
 int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_down, const unsigned char* d_up,
                     const float* x, float* out, unsigned char* mid, VesDeviceStatus* st, cudaStream_t s) {
   using namespace tcnet;
@@ -890,19 +904,25 @@ int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_dow
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  // compiled chunk-count variants; others run the generic kernels
-  void (*dk)(KArgs) = down_kernel<0, 0>;
-  void (*uk)(KArgs) = up_kernel<0>;
+  // compiled chunk-count variants; others run the generic kernels.  Three
+  // warp groups in the down kernel when their TMEM columns and arrays fit.
   const int kc1 = a.g.kc1, kcd = a.g.kcd;
-  if (kc1 == 4 && kcd == 6) dk = down_kernel<4, 6>;
-  if (kc1 == 6 && kcd == 6) dk = down_kernel<6, 6>;
-  if (kc1 == 6 && kcd == 8) dk = down_kernel<6, 8>;
-  if (kc1 == 8 && kcd == 8) dk = down_kernel<8, 8>;
+  const int dsm3 = a.g.dxs + 3 * a.g.dgrp + 128 * 16;
+  const bool three = (kc1 + kcd) * 8 <= 128 && dsm3 <= kMaxSmem && tcnet_down_groups_max() >= 3;
+  void (*dk)(KArgs) = three ? down_kernel<0, 0, 3> : down_kernel<0, 0, 2>;
+  void (*uk)(KArgs) = up_kernel<0>;
+#define VES_DK(A, B) dk = three ? down_kernel<A, B, 3> : down_kernel<A, B, 2>
+  if (kc1 == 4 && kcd == 6) VES_DK(4, 6);
+  if (kc1 == 6 && kcd == 6) VES_DK(6, 6);
+  if (kc1 == 6 && kcd == 8) VES_DK(6, 8);
+  if (kc1 == 8 && kcd == 8) VES_DK(8, 8);
+#undef VES_DK
   if (kcd == 6) uk = up_kernel<6>;
   if (kcd == 8) uk = up_kernel<8>;
+  const int ngd = three ? 3 : 2;
   // one CTA per SM (it allocates all 512 TMEM columns): at least 117 KB of
   // shared memory per CTA keeps a second one off the SM
-  const int dsm = std::max(tb.dsmem, kMinSmem), usm = std::max(tb.usmem, kMinSmem);
+  const int dsm = std::max(three ? dsm3 : tb.dsmem, kMinSmem), usm = std::max(tb.usmem, kMinSmem);
   int rc = ves_cuda_status(cudaFuncSetAttribute(dk, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm), "tc down smem");
   if (rc) return rc;
   rc = ves_cuda_status(cudaFuncSetAttribute(uk, cudaFuncAttributeMaxDynamicSharedMemorySize, usm), "tc up smem");
@@ -910,7 +930,7 @@ int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_dow
   const int grid = (int)std::min<long long>(a.items, (long long)nsm);
   a.img = d_down;
   ves_count_launch(2);
-  dk<<<grid, kThreads, dsm, s>>>(a);
+  dk<<<grid, ngd * kGroupThreads, dsm, s>>>(a);
   a.img = d_up;
   uk<<<grid, kThreads, usm, s>>>(a);
   return ves_launch_check("tc net block");

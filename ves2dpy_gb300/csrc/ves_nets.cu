@@ -295,7 +295,7 @@ int net_forward_t(const ves_net* net, int nv, const Real* in, Real* out, WsCarve
     int rc;
     if (tc) {
       const TcBlock& tb = net->tcb[bi];
-      rc = tcnet_run_block(tb, net->groups, nv, net->d_tc + tb.down_off, net->d_tc + tb.up_off,
+      rc = tcnet_run_block(tb, net->groups, nv, net->d_tc + tb.down_off, net->d_tc + tb.up1_off, net->d_tc + tb.up2_off,
                            reinterpret_cast<const float*>(src), reinterpret_cast<float*>(dst), mid,
                            st ? st : net->d_status, s);
     } else {
@@ -401,10 +401,10 @@ extern "C" int ves_net_create(int precision, int groups, int length, int nblocks
     return rc0;
   }
   if (tc) {
-    std::vector<unsigned char> img, down, up;
+    std::vector<unsigned char> img, down, up1, up2;
     for (int i = 0; i < nblocks; ++i) {
       TcBlock tb;
-      if (tcnet_pack(blocks[i], groups, length, params + (size_t)i * 30, down, up, tb)) {
+      if (tcnet_pack(blocks[i], groups, length, params + (size_t)i * 30, down, up1, up2, tb)) {
         ves_record_error(VES_ERR_ARG, "net_create: block %d does not fit the tensor-core kernels", i);
         cudaFree(net->d_status);
         delete net;
@@ -412,8 +412,10 @@ extern "C" int ves_net_create(int precision, int groups, int length, int nblocks
       }
       tb.down_off = img.size();
       img.insert(img.end(), down.begin(), down.end());
-      tb.up_off = img.size();
-      img.insert(img.end(), up.begin(), up.end());
+      tb.up1_off = img.size();
+      img.insert(img.end(), up1.begin(), up1.end());
+      tb.up2_off = img.size();
+      img.insert(img.end(), up2.begin(), up2.end());
       net->mid_max = std::max(net->mid_max, tb.mid_bytes);
       net->tcb.push_back(tb);
     }

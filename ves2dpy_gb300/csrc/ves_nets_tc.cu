@@ -22,12 +22,16 @@
 // follows in shared memory, and those rows are never read back.  Output
 // channels are N, rounded up to 16.
 //
-// Two kernels per block: "down" (conv pair 1, conv pair 2) and "up"
-// (transposed convs, mix, residual and pass-through).  The block input and
-// output stay FP32 in global memory ([nv][groups*channels][L]); the down ->
-// up intermediate is BF16 in the K-major layout.  Kernels are persistent:
-// each CTA walks a contiguous range of (group, vesicle) items, loading a
-// group's weight image into shared memory once per group it meets.
+// Three kernels per block: "down" (conv pair 1, conv pair 2), "up1"
+// (transposed conv 1) and "up2" (transposed conv 2, mix, residual and
+// pass-through).  The block input and output stay FP32 in global memory
+// ([nv][groups*channels][L]); the intermediates between the kernels are BF16
+// in the K-major layout.  Kernels are persistent: each CTA walks a contiguous
+// range of (group, vesicle) items, loading a group's weight image into shared
+// memory once per group it meets, and runs several warp groups, each on its
+// own items (3, 4 and 3 when TMEM and shared memory allow): while one waits
+// for its MMAs the others run their epilogues.  Splitting the transposed
+// convs over two kernels keeps each weight image small enough for that.
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -58,29 +62,35 @@ struct Geo {
   int kcin, kc1, kcd;    // 8-channel K chunks of the three GEMM inputs (even)
   // down image: W1 [11][kcin][n1][16B], W2 [11][kc1][d][16B], consts [6][128] f32
   int dw1, dw2, dcst, dsize;
-  // down arrays of warp group 0 (group 1 at + dgrp): xs [2][kcin][L/2+6][16B],
+  // down arrays of warp group 0 (group k at + k*dgrp): xs [2][kcin][L/2+6][16B],
   // as [2][kc1][L/4+6][16B], stage [kcd][L/4][16B], xf [cin][L] f32 (the
-  // block input as it arrives by bulk copy); then a tail
-  int dxs, das, dstage, dxf, dgrp, dsmem;
-  // up image: D1, D2 (transposed convs), M [3][kcd][cmix][16B], consts [7][128] f32.
-  // D layout: umerge = 1: [5][kcd][2*kcd*8][16B], both output parities in one
-  // operand of N = 2*kcd*8 rows (parity r at row r*kcd*8); umerge = 0 (when the
-  // padded image does not fit): [2][5][kcd][d][16B]
-  int umerge, uw1, uw2, uwm, ucst, usize;
-  // up arrays of warp group 0 (group 1 at + ugrp): bs [kcd][L/4+4][16B],
-  // cs [kcd][L/2+4][16B], ds [kcd][L+2][16B] (at least cin*L*4 bytes: it
-  // first receives the block input); then a tail
-  int ubs, ucs, uds, ugrp, usmem;
-  int mid_bytes;         // down -> up intermediate per (vesicle, group): [kcd][L/4][16B]
+  // block input as it arrives by bulk copy); a tail of 2 KB follows the groups
+  int dxs, das, dstage, dxf, dgrp;
+  // up1 image (transposed conv 1): W [2][5][kcd][d][16B] (output parity r, tap u),
+  // consts [7][128] f32; arrays of warp group 0: bs [kcd][L/4+4][16B]
+  int u1w, u1cst, u1size, u1bs, u1grp;
+  // up2 image (transposed conv 2 and mix): W (u2merge = 1: [5][kcd][2*kcd*8][16B],
+  // both output parities in one operand of N = 2*kcd*8 rows, parity r at row
+  // r*kcd*8; u2merge = 0: as up1), M [3][kcd][cmix][16B], consts [7][128] f32;
+  // arrays of warp group 0: cs [kcd][L/2+4][16B], ds [kcd][L+2][16B] (at least
+  // cin*L*4 bytes: it first receives the block input)
+  int u2merge, u2w, u2wm, u2cst, u2size, u2cs, u2ds, u2grp;
+  // per (vesicle, group) item in the workspace: down -> up1 [kcd][L/4][16B],
+  // then up1 -> up2 [kcd][L/2][16B]
+  int mid_bytes, mid2_bytes, mid_stride;
 };
 
 constexpr int kMaxSmem = 227 * 1024 - 256;  // dynamic shared memory available next to the static part
+constexpr int kTail = 128 * 16;             // after the groups' arrays: rows an MMA reads past the last one
 
-// byte offset of row o of K chunk kc of tap u, output parity r, in transposed conv `layer`
-__host__ __device__ inline int up_w_off(const Geo& g, int layer, int r, int u, int kc, int o) {
-  const int base = layer ? g.uw2 : g.uw1;
-  if (g.umerge) return base + ((u * g.kcd + kc) * 2 * g.kcd * 8 + r * g.kcd * 8 + o) * 16;
+// byte offset of row o of K chunk kc of tap u, output parity r, in the
+// unmerged layout [2][5][kcd][d][16B] (base = start of the weights)
+__host__ __device__ inline int dec_w_off(const Geo& g, int base, int r, int u, int kc, int o) {
   return base + (((r * 5 + u) * g.kcd + kc) * g.d + o) * 16;
+}
+// same in the merged layout [5][kcd][2*kcd*8][16B]
+__host__ __device__ inline int dec_w_off_merged(const Geo& g, int base, int r, int u, int kc, int o) {
+  return base + ((u * g.kcd + kc) * 2 * g.kcd * 8 + r * g.kcd * 8 + o) * 16;
 }
 
 inline Geo make_geo(const ves_net_block& b, int L) {
@@ -116,30 +126,30 @@ inline Geo make_geo(const ves_net_block& b, int L) {
   g.dxf = o;
   o += rup(g.cin * L * 4, 16);
   g.dgrp = o - g.dxs;
-  g.dsmem = g.dxs + 2 * g.dgrp + 128 * 16;
-  // ds doubles as the landing area of the block input x (FP32 [cin][L]) from
-  // the start of an item until the first transposed conv's epilogue
-  g.ugrp = g.kcd * (L / 4 + 4) * 16 + g.kcd * (L / 2 + 4) * 16 + std::max(g.kcd * (L + 2) * 16, rup(g.cin * L * 4, 16));
-  for (g.umerge = 1; g.umerge >= 0; --g.umerge) {
-    o = 0;
-    const int dbytes = g.umerge ? 5 * g.kcd * 2 * g.kcd * 8 * 16 : 10 * g.kcd * g.d * 16;
-    g.uw1 = o;
-    o += dbytes;
-    g.uw2 = o;
-    o += dbytes;
-    g.uwm = o;
-    o += 3 * g.kcd * g.cmix * 16;
-    g.ucst = o;
-    o += 7 * 128 * 4;
-    g.usize = o;
-    g.usmem = g.usize + 2 * g.ugrp + 128 * 16;
-    if (g.usmem <= kMaxSmem) break;
+  const int dec_unmerged = 10 * g.kcd * g.d * 16;
+  // up1: always M-split (2 * L/4 <= 128), so the smaller unmerged layout
+  g.u1w = 0;
+  g.u1cst = dec_unmerged;
+  g.u1size = g.u1cst + 7 * 128 * 4;
+  g.u1bs = g.u1size;
+  g.u1grp = g.kcd * (L / 4 + 4) * 16;
+  // up2: merged (one MMA of N = 2*Nd per tap) when the conv is not M-split
+  // and the image still leaves room for three warp groups
+  g.u2grp = g.kcd * (L / 2 + 4) * 16 + std::max(g.kcd * (L + 2) * 16, rup(g.cin * L * 4, 16));
+  for (g.u2merge = (2 * (L / 2) > 128) ? 1 : 0; g.u2merge >= 0; --g.u2merge) {
+    const int dbytes = g.u2merge ? 5 * g.kcd * 2 * g.kcd * 8 * 16 : dec_unmerged;
+    g.u2w = 0;
+    g.u2wm = dbytes;
+    g.u2cst = g.u2wm + 3 * g.kcd * g.cmix * 16;
+    g.u2size = g.u2cst + 7 * 128 * 4;
+    if (g.u2size + 3 * g.u2grp + kTail <= kMaxSmem) break;
   }
-  if (g.umerge < 0) g.umerge = 0;
-  g.ubs = g.usize;
-  g.ucs = g.ubs + g.kcd * (L / 4 + 4) * 16;
-  g.uds = g.ucs + g.kcd * (L / 2 + 4) * 16;
+  if (g.u2merge < 0) g.u2merge = 0;
+  g.u2cs = g.u2size;
+  g.u2ds = g.u2cs + g.kcd * (L / 2 + 4) * 16;
   g.mid_bytes = g.kcd * (L / 4) * 16;
+  g.mid2_bytes = g.kcd * (L / 2) * 16;
+  g.mid_stride = g.mid_bytes + g.mid2_bytes;
   return g;
 }
 
@@ -323,7 +333,7 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
   __shared__ uint32_t tbase;
   __shared__ int fail[NG];
   const Geo& g = a.g;
-  const int kc1 = KC1 ? KC1 : kc1, kcd = KCD ? KCD : kcd;
+  const int kc1 = KC1 ? KC1 : g.kc1, kcd = KCD ? KCD : g.kcd;
   const int L = g.L, L2 = L / 2, L4 = L / 4;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int wg = tid / kGroupThreads, gt = tid % kGroupThreads;  // warp group, thread within it
@@ -482,8 +492,8 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
       }
       tc_fence_before_sync();
       group_sync(wg);
-      copy16_g(a.mid + ((size_t)v * a.G + sg.grp) * g.mid_bytes, reinterpret_cast<unsigned char*>(stage), g.mid_bytes,
-               gt);
+      copy16_g(a.mid + ((size_t)v * a.G + sg.grp) * g.mid_stride, reinterpret_cast<unsigned char*>(stage),
+               g.mid_bytes, gt);
     }
     lo = sg.hi;
     failed = __syncthreads_or(failed ? 1 : 0) != 0;  // every thread takes part
@@ -497,15 +507,88 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// KCD: compile-time K chunk count of the transposed convs (0: from the geometry)
+// ---------------------------------------------------------------------------
+// The transposed convolutions, split in two kernels so that their weight
+// images and per-group arrays are small enough for more warp groups per SM:
+//   up1: transposed conv 1 (intermediate [kcd][L/4] -> [kcd][L/2], BF16 rows
+//        to global memory);
+//   up2: transposed conv 2, mix, residual and pass-through channels.
+// Both M-split a transposed conv when its two output parities fit in 128
+// lanes (2*npos <= 128): parity r's operand starts r*npos rows early, so its
+// valid rows land on lanes [r*npos, (r+1)*npos) and every warp has epilogue
+// work; otherwise both parities share one MMA of N = 2*Nd (merged image) or
+// run as two MMAs on the same lanes.  Parity r accumulates in TMEM columns
+// [r*Nd, (r+1)*Nd) either way.
+
+// Issue one transposed conv (thread 0 of the group).  w0/w1: byte offsets of
+// parity 0/1 weights (tap 0, chunk 0, row 0), bTap: tap stride (16-byte
+// units), lboB: K-chunk stride of B in bytes, merged: both parities in one
+// operand of N = 2*Nd rows at w0.
 template <int KCD>
-__global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
+__device__ __forceinline__ void deconv_issue(uint32_t dt, uint32_t sbase, uint32_t a_off, uint32_t lboA, int npos,
+                                             int Nd, int kcd, bool merged, uint32_t w0, uint32_t w1, uint32_t bTap,
+                                             uint32_t lboB) {
+  const bool msplit = 2 * npos <= 128;
+  const uint32_t stepA = (2 * lboA) >> 4;
+  if (merged && !msplit) {
+    const uint32_t idesc = tc_idesc_bf16(128, 2 * Nd);
+    const uint64_t a0 = tc_desc(sbase + a_off, lboA, 128), b0 = tc_desc(sbase + w0, lboB, 128);
+#define VES_DEC(NK) issue_deconv<NK>(dt, a0, b0, bTap, stepA, (2 * lboB) >> 4, idesc)
+    VES_TC_NK_SWITCH(kcd / 2, VES_DEC)
+#undef VES_DEC
+  } else {
+    const uint32_t idesc = tc_idesc_bf16(128, Nd);
+    for (int r = 0; r < 2; ++r) {
+      const int lift = msplit ? r * npos * 16 : 0;
+      const uint64_t a0 = tc_desc(sbase + a_off - lift, lboA, 128);
+      const uint64_t b0 = tc_desc(sbase + (r ? w1 : w0), lboB, 128);
+#define VES_DEC(NK) issue_deconv<NK>(dt + r * Nd, a0, b0, bTap, stepA, (2 * lboB) >> 4, idesc)
+      VES_TC_NK_SWITCH(kcd / 2, VES_DEC)
+#undef VES_DEC
+    }
+  }
+}
+
+// Epilogue of a transposed conv over npos input rows: 8 channels of output
+// position 2q + r for this thread's lane go to dst[kc * pitch + 2q + r + row0].
+template <int KCD>
+__device__ __forceinline__ void deconv_epilogue(uint32_t dt, int qd, int lane, int npos, int Nd, int kcd, int nreal,
+                                                const float* cst, int ob, int os, int ot, uint4* dst, int pitch,
+                                                int row0) {
+  const bool msplit = 2 * npos <= 128;
+  const int lane0 = 32 * qd;
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    int q;
+    if (msplit) {
+      if (lane0 < r * npos || lane0 >= (r + 1) * npos) continue;  // uniform per warp
+      q = lane0 + lane - r * npos;
+    } else {
+      if (lane0 >= npos) continue;
+      q = lane0 + lane;
+    }
+#pragma unroll
+    for (int k0 = 0; k0 < (KCD ? KCD : 8); k0 += 4) {
+      if (k0 >= kcd) break;
+      float vv[32];
+      tc_ld32(dt + ((uint32_t)lane0 << 16) + r * Nd + 8 * k0, vv);
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (k0 + k < kcd) dst[(size_t)(k0 + k) * pitch + 2 * q + r + row0] = act8(vv + 8 * k, cst, k0 + k, nreal, ob, os, ot);
+    }
+  }
+}
+
+// up1: KCD compile-time K chunk count (0: from the geometry); NG warp groups
+// (TMEM columns [128*wg, 128*wg + 2*Nd) each).
+template <int KCD, int NG>
+__global__ void __launch_bounds__(NG * kGroupThreads, 1) up1_kernel(KArgs a) {
   extern __shared__ __align__(128) unsigned char sm[];
-  __shared__ uint64_t bar[2], mbar[2], rbar[2];  // per warp group: MMA completion, intermediate, block input
+  __shared__ uint64_t bar[NG], mbar[NG];  // per warp group: MMA completion, intermediate arrival
   __shared__ uint32_t tbase;
-  __shared__ int fail[2];
+  __shared__ int fail[NG];
   const Geo& g = a.g;
-  const int kcd = KCD ? KCD : kcd;
+  const int kcd = KCD ? KCD : g.kcd;
   const int L = g.L, L2 = L / 2, L4 = L / 4;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int wg = tid / kGroupThreads, gt = tid % kGroupThreads;
@@ -514,114 +597,156 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
   if (rg.lo >= rg.hi) return;
   const uint32_t ncols = 512;
   if (tid == 0) {
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < NG; ++k) {
       tc_mbar_init(&bar[k], 1);
       tc_mbar_init(&mbar[k], 1);
-      tc_mbar_init(&rbar[k], 1);
+      fail[k] = 0;
     }
     tc_mbar_fence_init();
-    fail[0] = fail[1] = 0;
   }
   if (warp == 0) tc_tmem_alloc(&tbase, ncols);
-  zero16(sm + g.ubs, g.usmem - g.ubs);  // halos and K padding stay zero
+  zero16(sm + g.u1bs, NG * g.u1grp + 128 * 16);  // halos and K padding stay zero
   tc_fence_async_smem();
   tc_fence_before_sync();
   __syncthreads();
   tc_fence_after_sync();
-  const uint32_t dt = tbase + 256 * wg;
+  const uint32_t dt = tbase + 128 * wg;
   const uint32_t sbase = tc_smem_u32(sm);
-  const int goff = wg * g.ugrp;
-  const float* cst = reinterpret_cast<const float*>(sm + g.ucst);
-  const int PB = L4 + 4, PC = L2 + 4, PD = L + 2;
-  const int Nd = kcd * 8, Nm = rup(g.cmix, 16);
-  const int cout = g.cmix + g.npass;
-  const int nh = L / 128;      // 128-position halves of the mix
-  const int mcol = 2 * Nd;     // first TMEM column of the mix accumulators (after the transposed convs')
-  uint4* bs = reinterpret_cast<uint4*>(sm + g.ubs + goff);
-  uint4* cs = reinterpret_cast<uint4*>(sm + g.ucs + goff);
-  uint4* ds = reinterpret_cast<uint4*>(sm + g.uds + goff);
-  const float* xf = reinterpret_cast<const float*>(ds);  // block input while it sits in ds
-  const bool need_x = g.residual || g.npass > 0;
-  const uint32_t xbytes = (uint32_t)(g.cin * L * 4);
-  unsigned phase = 0, mphase = 0, rphase = 0;
-  bool mpend = false, rpend = false;  // bulk copies into bs / ds in flight
+  const float* cst = reinterpret_cast<const float*>(sm + g.u1cst);
+  const int PB = L4 + 4;
+  const int Nd = kcd * 8;
+  uint4* bs = reinterpret_cast<uint4*>(sm + g.u1bs + wg * g.u1grp);
+  const uint32_t bTap = (uint32_t)(kcd * g.d * 16) >> 4;
+  const uint32_t w1 = (uint32_t)(g.u1w + 5 * kcd * g.d * 16);
+  unsigned phase = 0, mphase = 0;
+  bool mpend = false;  // a bulk copy into bs is in flight
   // intermediate [kcd][L/4][16B] of an item -> bs rows 2 .. L/4+1 of each chunk
   auto fetch_mid = [&](long long item) {
     if (gt == 0) {
       const int grp = (int)(item / a.nv);
       const long long v = item % a.nv;
-      const unsigned char* src = a.mid + ((size_t)v * a.G + grp) * g.mid_bytes;
+      const unsigned char* src = a.mid + ((size_t)v * a.G + grp) * g.mid_stride;
       tc_expect_tx(&mbar[wg], (uint32_t)g.mid_bytes);
       for (int kc = 0; kc < kcd; ++kc) tc_bulk_g2s(bs + kc * PB + 2, src + kc * L4 * 16, L4 * 16, &mbar[wg]);
     }
     mpend = true;
   };
-  // One transposed conv over npos input rows: output parity r in TMEM columns
-  // [r*Nd, (r+1)*Nd).  When both parities fit in 128 lanes (2*npos <= 128)
-  // parity r's operand starts r*npos rows early, so its valid rows land on
-  // lanes [r*npos, (r+1)*npos) and twice as many warps share the epilogue;
-  // otherwise both parities share one MMA of N = 2*Nd (merged image) or run
-  // as two MMAs on the same lanes.
-  auto deconv_mma = [&](int layer, uint32_t a_off, uint32_t lboA, int npos) {
-    const bool msplit = 2 * npos <= 128;
-    const uint32_t bTap = (uint32_t)(up_w_off(g, layer, 0, 1, 0, 0) - up_w_off(g, layer, 0, 0, 0, 0)) >> 4;
-    const uint32_t stepA = (2 * lboA) >> 4;
-    if (g.umerge && !msplit) {
-      const uint32_t idesc = tc_idesc_bf16(128, 2 * Nd);
-      const uint32_t lboB = 2 * Nd * 16;
-      const uint64_t a0 = tc_desc(sbase + a_off, lboA, 128), b0 = tc_desc(sbase + up_w_off(g, layer, 0, 0, 0, 0), lboB, 128);
-#define VES_DEC(NK) issue_deconv<NK>(dt, a0, b0, bTap, stepA, (2 * lboB) >> 4, idesc)
-      VES_TC_NK_SWITCH(kcd / 2, VES_DEC)
-#undef VES_DEC
-    } else {
-      const uint32_t idesc = tc_idesc_bf16(128, Nd);
-      const uint32_t lboB = (g.umerge ? 2 * Nd : g.d) * 16;
-      for (int r = 0; r < 2; ++r) {
-        const int lift = msplit ? r * npos * 16 : 0;
-        const uint64_t a0 = tc_desc(sbase + a_off - lift, lboA, 128);
-        const uint64_t b0 = tc_desc(sbase + up_w_off(g, layer, r, 0, 0, 0), lboB, 128);
-#define VES_DEC(NK) issue_deconv<NK>(dt + r * Nd, a0, b0, bTap, stepA, (2 * lboB) >> 4, idesc)
-        VES_TC_NK_SWITCH(kcd / 2, VES_DEC)
-#undef VES_DEC
+  bool failed = false, stuck = false;
+  for (long long lo = rg.lo; lo < rg.hi && !failed;) {
+    const Seg sg = next_seg(lo, rg.hi, a.nv);
+    __syncthreads();
+    copy16(sm, a.img + (size_t)sg.grp * g.u1size, g.u1size);
+    tc_fence_async_smem();
+    __syncthreads();
+    if (sg.lo + wg < sg.hi) fetch_mid(sg.lo + wg);
+    for (long long it = sg.lo + wg; it < sg.hi; it += NG) {
+      const long long v = it % a.nv;
+      if (!group_wait(&mbar[wg], mphase, a.st, 26, wg, &fail[wg])) {
+        failed = true;
+        break;
       }
+      mphase ^= 1;
+      mpend = false;
+      tc_fence_after_sync();
+      if (gt == 0) {
+        deconv_issue<KCD>(dt, sbase, g.u1bs + wg * g.u1grp, PB * 16, L4, Nd, kcd, false, g.u1w, w1, bTap,
+                          g.d * 16);
+        tc_commit(&bar[wg]);
+      }
+      if (!group_wait_one(&bar[wg], phase, a.st, 23, wg, gt, &fail[wg])) {
+        failed = stuck = true;
+        break;
+      }
+      phase ^= 1;
+      tc_fence_after_sync();
+      // bs is free once the MMAs have completed: this group's next item
+      if (it + NG < sg.hi) fetch_mid(it + NG);
+      uint4* dst = reinterpret_cast<uint4*>(a.mid + ((size_t)v * a.G + sg.grp) * g.mid_stride + g.mid_bytes);
+      deconv_epilogue<KCD>(dt, qd, lane, L4, Nd, kcd, g.d, cst, 0, 128, 256, dst, L2, 0);
+      tc_fence_before_sync();
+      group_sync(wg);  // every TMEM read done before the next item's MMAs
     }
-    tc_commit(&bar[wg]);
-  };
-  // epilogue of a transposed conv: out(8 channels, position 2q + r) for this
-  // thread's lane; `dst` rows are 2q + r + row0, chunk stride `pitch`
-  auto deconv_epi = [&](int npos, uint4* dst, int pitch, int row0, int ob, int os, int ot) {
-    const bool msplit = 2 * npos <= 128;
-    const int lane0 = 32 * qd;
-#pragma unroll
-    for (int r = 0; r < 2; ++r) {
-      int q;
-      if (msplit) {
-        if (lane0 < r * npos || lane0 >= (r + 1) * npos) continue;  // uniform per warp
-        q = lane0 + lane - r * npos;
-      } else {
-        if (lane0 >= npos) continue;
-        q = lane0 + lane;
-      }
-#pragma unroll
-      for (int k0 = 0; k0 < kcd; k0 += 4) {
-        float vv[32];
-        tc_ld32(dt + ((uint32_t)lane0 << 16) + r * Nd + 8 * k0, vv);
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-          if (k0 + k < kcd)
-            dst[(size_t)(k0 + k) * pitch + 2 * q + r + row0] = act8(vv + 8 * k, cst, k0 + k, g.d, ob, os, ot);
-      }
+    lo = sg.hi;
+    failed = __syncthreads_or(failed ? 1 : 0) != 0;  // every thread takes part
+  }
+  if (stuck) tc_mbar_wait(&bar[wg], phase, nullptr, 0);
+  if (mpend) tc_mbar_wait(&mbar[wg], mphase, nullptr, 0);
+  tc_fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc_tmem_dealloc(tbase, ncols);
+}
+
+// up2: transposed conv 2, mix, residual and pass-through.  NG warp groups,
+// TMEM columns [cstride*wg, cstride*wg + 2*Nd + nh*Nm) each.
+template <int KCD, int NG>
+__global__ void __launch_bounds__(NG * kGroupThreads, 1) up2_kernel(KArgs a) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  __shared__ uint64_t bar[NG], mbar[NG], rbar[NG];  // per warp group: MMA completion, intermediate, block input
+  __shared__ uint32_t tbase;
+  __shared__ int fail[NG];
+  const Geo& g = a.g;
+  const int kcd = KCD ? KCD : g.kcd;
+  const int L = g.L, L2 = L / 2;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int wg = tid / kGroupThreads, gt = tid % kGroupThreads;
+  const int qd = warp & 3;
+  const Range rg = my_items(a.items);
+  if (rg.lo >= rg.hi) return;
+  const uint32_t ncols = 512;
+  if (tid == 0) {
+    for (int k = 0; k < NG; ++k) {
+      tc_mbar_init(&bar[k], 1);
+      tc_mbar_init(&mbar[k], 1);
+      tc_mbar_init(&rbar[k], 1);
+      fail[k] = 0;
     }
+    tc_mbar_fence_init();
+  }
+  if (warp == 0) tc_tmem_alloc(&tbase, ncols);
+  zero16(sm + g.u2cs, NG * g.u2grp + 128 * 16);  // halos and K padding stay zero
+  tc_fence_async_smem();
+  tc_fence_before_sync();
+  __syncthreads();
+  tc_fence_after_sync();
+  const uint32_t dt = tbase + (NG == 2 ? 256 : 160) * wg;
+  const uint32_t sbase = tc_smem_u32(sm);
+  const int goff = wg * g.u2grp;
+  const float* cst = reinterpret_cast<const float*>(sm + g.u2cst);
+  const int PC = L2 + 4, PD = L + 2;
+  const int Nd = kcd * 8, Nm = rup(g.cmix, 16);
+  const int cout = g.cmix + g.npass;
+  const int nh = L / 128;   // 128-position halves of the mix
+  const int mcol = 2 * Nd;  // first TMEM column of the mix accumulators (after the transposed conv's)
+  uint4* cs = reinterpret_cast<uint4*>(sm + g.u2cs + goff);
+  uint4* ds = reinterpret_cast<uint4*>(sm + g.u2ds + goff);
+  const float* xf = reinterpret_cast<const float*>(ds);  // block input while it sits in ds
+  const bool need_x = g.residual || g.npass > 0;
+  const uint32_t xbytes = (uint32_t)(g.cin * L * 4);
+  const uint32_t bTap = (uint32_t)((g.u2merge ? 2 * Nd : g.d) * kcd * 16) >> 4;
+  const uint32_t lboB = (uint32_t)((g.u2merge ? 2 * Nd : g.d) * 16);
+  const uint32_t w1 = g.u2merge ? (uint32_t)(g.u2w + Nd * 16) : (uint32_t)(g.u2w + 5 * kcd * g.d * 16);
+  unsigned phase = 0, mphase = 0, rphase = 0;
+  bool mpend = false, rpend = false;  // bulk copies into cs / ds in flight
+  // up1 output [kcd][L/2][16B] of an item -> cs rows 2 .. L/2+1 of each chunk
+  auto fetch_mid = [&](long long item) {
+    if (gt == 0) {
+      const int grp = (int)(item / a.nv);
+      const long long v = item % a.nv;
+      const unsigned char* src = a.mid + ((size_t)v * a.G + grp) * g.mid_stride + g.mid_bytes;
+      tc_expect_tx(&mbar[wg], (uint32_t)g.mid2_bytes);
+      for (int kc = 0; kc < kcd; ++kc) tc_bulk_g2s(cs + kc * PC + 2, src + kc * L2 * 16, L2 * 16, &mbar[wg]);
+    }
+    mpend = true;
   };
   bool failed = false, stuck = false;
   for (long long lo = rg.lo; lo < rg.hi && !failed;) {
     const Seg sg = next_seg(lo, rg.hi, a.nv);
     __syncthreads();
-    copy16(sm, a.img + (size_t)sg.grp * g.usize, g.usize);
+    copy16(sm, a.img + (size_t)sg.grp * g.u2size, g.u2size);
     tc_fence_async_smem();
     __syncthreads();
     if (sg.lo + wg < sg.hi) fetch_mid(sg.lo + wg);
-    for (long long it = sg.lo + wg; it < sg.hi; it += 2) {
+    for (long long it = sg.lo + wg; it < sg.hi; it += NG) {
       const long long v = it % a.nv;
       const float* __restrict__ xin = a.x + ((long long)v * a.G + sg.grp) * (long long)g.cin * L;
       float* __restrict__ op = a.out + ((long long)v * a.G + sg.grp) * (long long)cout * L;
@@ -633,24 +758,6 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
         }
         rpend = true;
       }
-      if (!group_wait(&mbar[wg], mphase, a.st, 26, wg, &fail[wg])) {
-        failed = true;
-        break;
-      }
-      mphase ^= 1;
-      mpend = false;
-      tc_fence_after_sync();
-      // transposed conv 1: rows q < L/4
-      if (gt == 0) deconv_mma(0, g.ubs + goff, PB * 16, L4);
-      if (!group_wait_one(&bar[wg], phase, a.st, 23, wg, gt, &fail[wg])) {
-        failed = stuck = true;
-        break;
-      }
-      phase ^= 1;
-      tc_fence_after_sync();
-      // bs is free once the first transposed conv has completed: this group's next item
-      if (it + 2 < sg.hi) fetch_mid(it + 2);
-      deconv_epi(L4, cs, PC, 2, 0, 128, 256);
       if (need_x) {
         if (!group_wait(&rbar[wg], rphase, a.st, 27, wg, &fail[wg])) {
           failed = true;
@@ -665,39 +772,48 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
       }
       {
         // mix accumulators preset to residual + bias (columns [mcol, mcol + nh*Nm))
-        float r0[32], r1[32];
         const int p0 = 32 * qd + lane;
+        for (int h = 0; h < nh; ++h) {
+          float r0[32];
 #pragma unroll
-        for (int o = 0; o < 32; ++o) {
-          const bool on = o < g.cmix;
-          const float b = on ? cst[768 + o] : 0.f;
-          r0[o] = (on && g.residual ? xf[o * L + p0] : 0.f) + b;
-          r1[o] = (on && g.residual && nh > 1 ? xf[o * L + 128 + p0] : 0.f) + b;
+          for (int o = 0; o < 32; ++o) {
+            const bool on = o < g.cmix;
+            r0[o] = (on && g.residual ? xf[o * L + 128 * h + p0] : 0.f) + (on ? cst[768 + o] : 0.f);
+          }
+          tc_st32(dt + ((uint32_t)(32 * qd) << 16) + mcol + h * Nm, r0);
         }
-        tc_st32(dt + ((uint32_t)(32 * qd) << 16) + mcol, r0);
-        if (nh > 1) tc_st32(dt + ((uint32_t)(32 * qd) << 16) + mcol + Nm, r1);
         tc_wait_st();
       }
+      if (!group_wait(&mbar[wg], mphase, a.st, 26, wg, &fail[wg])) {
+        failed = true;
+        break;
+      }
+      mphase ^= 1;
+      mpend = false;
       group_sync_for_mma(wg);  // also: every read of the block input in ds is done
-      // transposed conv 2: rows q < L/2
-      if (gt == 0) deconv_mma(1, g.ucs + goff, PC * 16, L2);
+      if (gt == 0) {
+        deconv_issue<KCD>(dt, sbase, g.u2cs + goff, PC * 16, L2, Nd, kcd, g.u2merge != 0, g.u2w, w1, bTap, lboB);
+        tc_commit(&bar[wg]);
+      }
       if (!group_wait_one(&bar[wg], phase, a.st, 24, wg, gt, &fail[wg])) {
         failed = stuck = true;
         break;
       }
       phase ^= 1;
       tc_fence_after_sync();
-      deconv_epi(L2, ds, PD, 1, 384, 512, 640);
+      // cs is free once the transposed conv has completed: this group's next item
+      if (it + NG < sg.hi) fetch_mid(it + NG);
+      deconv_epilogue<KCD>(dt, qd, lane, L2, Nd, kcd, g.d, cst, 384, 512, 640, ds, PD, 1);
       // the halo rows of ds (zero padding of the mix) held block input
       if (gt < 2 * kcd) ds[(gt >> 1) * PD + ((gt & 1) ? L + 1 : 0)] = make_uint4(0, 0, 0, 0);
       group_sync_for_mma(wg);
       // mix: D[p][o] = sum_t d[p + t - 1] M_t; positions in halves of 128 rows
       if (gt == 0) {
         const uint32_t idesc = tc_idesc_bf16(128, Nm);
-        const uint32_t lboA = PD * 16, lboB = g.cmix * 16;
-        const uint64_t a0 = tc_desc(sbase + g.uds + goff, lboA, 128), b0 = tc_desc(sbase + g.uwm, lboB, 128);
+        const uint32_t lboA = PD * 16, lboM = g.cmix * 16;
+        const uint64_t a0 = tc_desc(sbase + g.u2ds + goff, lboA, 128), b0 = tc_desc(sbase + g.u2wm, lboM, 128);
         for (int h = 0; h < nh; ++h) {  // onto residual + bias
-#define VES_MIX(NK) issue_mix<NK>(dt + mcol + h * Nm, a0 + (uint32_t)(128 * h), b0, (kcd * lboB) >> 4, (2 * lboA) >> 4, (2 * lboB) >> 4, idesc)
+#define VES_MIX(NK) issue_mix<NK>(dt + mcol + h * Nm, a0 + (uint32_t)(128 * h), b0, (kcd * lboM) >> 4, (2 * lboA) >> 4, (2 * lboM) >> 4, idesc)
           VES_TC_NK_SWITCH(kcd / 2, VES_MIX)
 #undef VES_MIX
         }
@@ -734,6 +850,7 @@ __global__ void __launch_bounds__(kThreads, 1) up_kernel(KArgs a) {
 
 }  // namespace tcnet
 
+
 // ---------------------------------------------------------------------------
 // host side
 #include "ves_nets_tc.h"
@@ -757,25 +874,28 @@ void put_row(unsigned char* img, size_t off, const float* vals8) {
 }  // namespace
 
 int tcnet_pack(const ves_net_block& b, int G, int L, const float* const* p, std::vector<unsigned char>& down,
-               std::vector<unsigned char>& up, TcBlock& out) {
+               std::vector<unsigned char>& up1, std::vector<unsigned char>& up2, TcBlock& out) {
   using namespace tcnet;
   const Geo g = make_geo(b, L);
+  static_assert(sizeof(Geo) <= sizeof(out.geo), "geometry record too large");
   out.geo_bytes = sizeof(Geo);
   memcpy(out.geo, &g, sizeof(Geo));
   out.dsize = g.dsize;
-  out.usize = g.usize;
-  out.dsmem = g.dsmem;
-  out.usmem = g.usmem;
-  out.mid_bytes = g.mid_bytes;
-  // TMEM per warp group: N1 + N2 (down) and 2 * N2 + the mix halves (up)
-  // columns of 256; the mix epilogue reads 32 columns; each lane quarter
-  // holds 32 whole positions
-  if (g.n1 > 128 || g.d > 128 || g.cmix > 32 || 2 * g.kcd * 8 + (L / 128) * rup(g.cmix, 16) > 256 || g.dsmem > kMaxSmem || g.usmem > kMaxSmem || L > 256 ||
-      (L / 4) % 32 != 0)
+  out.u1size = g.u1size;
+  out.u2size = g.u2size;
+  out.mid_bytes = g.mid_stride;
+  // TMEM per warp group with two groups (256 columns each): N1 + N2 (down),
+  // 2 * Nd (up1) and 2 * Nd + the mix halves (up2); the mix epilogue reads 32
+  // columns; each lane quarter holds 32 whole positions; every kernel fits
+  // two warp groups in shared memory
+  if (g.n1 > 128 || g.d > 128 || g.cmix > 32 || 2 * g.kcd * 8 + (L / 128) * rup(g.cmix, 16) > 256 ||
+      g.dxs + 2 * g.dgrp + kTail > kMaxSmem || g.u1size + 2 * g.u1grp + kTail > kMaxSmem ||
+      g.u2size + 2 * g.u2grp + kTail > kMaxSmem || L > 256 || (L / 4) % 32 != 0)
     return VES_ERR_ARG;
   const int c1 = b.c1, c2 = b.c2, d = g.d, cin = b.cin, cmix = b.cmix;
   down.assign((size_t)g.dsize * G, 0);
-  up.assign((size_t)g.usize * G, 0);
+  up1.assign((size_t)g.u1size * G, 0);
+  up2.assign((size_t)g.u2size * G, 0);
   auto bn = [&](int idx, int ch, float* s, float* t) {
     const float* w = p[14 + 4 * idx];
     const float* bb = p[15 + 4 * idx];
@@ -787,7 +907,8 @@ int tcnet_pack(const ves_net_block& b, int G, int L, const float* const* p, std:
   };
   for (int grp = 0; grp < G; ++grp) {
     unsigned char* D = down.data() + (size_t)grp * g.dsize;
-    unsigned char* U = up.data() + (size_t)grp * g.usize;
+    unsigned char* U1 = up1.data() + (size_t)grp * g.u1size;
+    unsigned char* U2 = up2.data() + (size_t)grp * g.u2size;
     float v8[8];
     // conv pair 1
     for (int oi = 0; oi < kOffsets; ++oi) {
@@ -849,7 +970,12 @@ int tcnet_pack(const ves_net_block& b, int G, int L, const float* const* p, std:
                 const int c = kc * 8 + e;
                 v8[e] = c < d ? W[((size_t)(grp * d + c) * d + o) * 10 + r + 2 * u] : 0.f;
               }
-              put_row(U, up_w_off(g, layer, r, u, kc, o), v8);
+              if (layer == 0)
+                put_row(U1, dec_w_off(g, g.u1w, r, u, kc, o), v8);
+              else if (g.u2merge)
+                put_row(U2, dec_w_off_merged(g, g.u2w, r, u, kc, o), v8);
+              else
+                put_row(U2, dec_w_off(g, g.u2w, r, u, kc, o), v8);
             }
     }
     for (int t = 0; t < 3; ++t)
@@ -859,9 +985,9 @@ int tcnet_pack(const ves_net_block& b, int G, int L, const float* const* p, std:
             const int c = kc * 8 + e;
             v8[e] = c < d ? p[12][((size_t)(grp * cmix + o) * d + c) * 3 + t] : 0.f;
           }
-          put_row(U, g.uwm + ((size_t)(t * g.kcd + kc) * cmix + o) * 16, v8);
+          put_row(U2, g.u2wm + ((size_t)(t * g.kcd + kc) * cmix + o) * 16, v8);
         }
-    float* uc = reinterpret_cast<float*>(U + g.ucst);
+    float* uc = reinterpret_cast<float*>(U1 + g.u1cst);
     for (int o = 0; o < d; ++o) {
       uc[o] = p[9][grp * d + o];
       bn(2, grp * d + o, &uc[128 + o], &uc[256 + o]);
@@ -869,6 +995,7 @@ int tcnet_pack(const ves_net_block& b, int G, int L, const float* const* p, std:
       bn(3, grp * d + o, &uc[512 + o], &uc[640 + o]);
     }
     for (int o = 0; o < cmix; ++o) uc[768 + o] = p[13][grp * cmix + o];
+    memcpy(U2 + g.u2cst, U1 + g.u1cst, 7 * 128 * 4);  // both up kernels carry the full constants block
   }
   return VES_OK;
 }
@@ -884,16 +1011,18 @@ static int tcnet_down_groups_max() {
   return v;
 }
 
-int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_down, const unsigned char* d_up,
-                    const float* x, float* out, unsigned char* mid, VesDeviceStatus* st, cudaStream_t s) {
+int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_down, const unsigned char* d_up1,
+                    const unsigned char* d_up2, const float* x, float* out, unsigned char* mid, VesDeviceStatus* st,
+                    cudaStream_t s) {
   using namespace tcnet;
-  // the block input and the intermediate are fetched by 16-byte bulk copies
+  // the block input and the intermediates are fetched by 16-byte bulk copies
   if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(mid)) & 15u) {
     ves_record_error(VES_ERR_ARG, "net_forward: input and workspace must be 16-byte aligned");
     return VES_ERR_ARG;
   }
   KArgs a;
   memcpy(&a.g, tb.geo, sizeof(Geo));
+  const Geo& g = a.g;
   a.G = G;
   a.nv = nv;
   a.items = (long long)G * nv;
@@ -904,34 +1033,48 @@ int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_dow
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  // compiled chunk-count variants; others run the generic kernels.  Three
-  // warp groups in the down kernel when their TMEM columns and arrays fit.
-  const int kc1 = a.g.kc1, kcd = a.g.kcd;
-  const int dsm3 = a.g.dxs + 3 * a.g.dgrp + 128 * 16;
-  const bool three = (kc1 + kcd) * 8 <= 128 && dsm3 <= kMaxSmem && tcnet_down_groups_max() >= 3;
-  void (*dk)(KArgs) = three ? down_kernel<0, 0, 3> : down_kernel<0, 0, 2>;
-  void (*uk)(KArgs) = up_kernel<0>;
-#define VES_DK(A, B) dk = three ? down_kernel<A, B, 3> : down_kernel<A, B, 2>
+  const int kc1 = g.kc1, kcd = g.kcd, Nd = kcd * 8;
+  // warp groups per CTA: as many as TMEM (512 columns) and shared memory allow
+  const int down3 = g.dxs + 3 * g.dgrp + kTail, up1_4 = g.u1size + 4 * g.u1grp + kTail,
+            up2_3 = g.u2size + 3 * g.u2grp + kTail;
+  const bool dn3 = (kc1 + kcd) * 8 <= 128 && down3 <= kMaxSmem && tcnet_down_groups_max() >= 3;
+  const bool u14 = 2 * Nd <= 128 && up1_4 <= kMaxSmem;
+  const bool u23 = 2 * Nd + (g.L / 128) * rup(g.cmix, 16) <= 160 && up2_3 <= kMaxSmem;
+  // compiled chunk-count variants; others run the generic kernels
+  void (*dk)(KArgs) = dn3 ? down_kernel<0, 0, 3> : down_kernel<0, 0, 2>;
+  void (*k1)(KArgs) = u14 ? up1_kernel<0, 4> : up1_kernel<0, 2>;
+  void (*k2)(KArgs) = u23 ? up2_kernel<0, 3> : up2_kernel<0, 2>;
+#define VES_DK(A, B) dk = dn3 ? down_kernel<A, B, 3> : down_kernel<A, B, 2>
   if (kc1 == 4 && kcd == 6) VES_DK(4, 6);
   if (kc1 == 6 && kcd == 6) VES_DK(6, 6);
   if (kc1 == 6 && kcd == 8) VES_DK(6, 8);
   if (kc1 == 8 && kcd == 8) VES_DK(8, 8);
 #undef VES_DK
-  if (kcd == 6) uk = up_kernel<6>;
-  if (kcd == 8) uk = up_kernel<8>;
-  const int ngd = three ? 3 : 2;
+  if (kcd == 6) {
+    k1 = u14 ? up1_kernel<6, 4> : up1_kernel<6, 2>;
+    k2 = u23 ? up2_kernel<6, 3> : up2_kernel<6, 2>;
+  }
+  if (kcd == 8) {
+    k1 = u14 ? up1_kernel<8, 4> : up1_kernel<8, 2>;
+    k2 = u23 ? up2_kernel<8, 3> : up2_kernel<8, 2>;
+  }
+  const int ng_d = dn3 ? 3 : 2, ng_1 = u14 ? 4 : 2, ng_2 = u23 ? 3 : 2;
   // one CTA per SM (it allocates all 512 TMEM columns): at least 117 KB of
   // shared memory per CTA keeps a second one off the SM
-  const int dsm = std::max(three ? dsm3 : tb.dsmem, kMinSmem), usm = std::max(tb.usmem, kMinSmem);
-  int rc = ves_cuda_status(cudaFuncSetAttribute(dk, cudaFuncAttributeMaxDynamicSharedMemorySize, dsm), "tc down smem");
-  if (rc) return rc;
-  rc = ves_cuda_status(cudaFuncSetAttribute(uk, cudaFuncAttributeMaxDynamicSharedMemorySize, usm), "tc up smem");
+  const int sm_d = std::max(g.dxs + ng_d * g.dgrp + kTail, kMinSmem);
+  const int sm_1 = std::max(g.u1size + ng_1 * g.u1grp + kTail, kMinSmem);
+  const int sm_2 = std::max(g.u2size + ng_2 * g.u2grp + kTail, kMinSmem);
+  int rc = ves_cuda_status(cudaFuncSetAttribute(dk, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_d), "tc down smem");
+  if (!rc) rc = ves_cuda_status(cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_1), "tc up1 smem");
+  if (!rc) rc = ves_cuda_status(cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_2), "tc up2 smem");
   if (rc) return rc;
   const int grid = (int)std::min<long long>(a.items, (long long)nsm);
+  ves_count_launch(3);
   a.img = d_down;
-  ves_count_launch(2);
-  dk<<<grid, ngd * kGroupThreads, dsm, s>>>(a);
-  a.img = d_up;
-  uk<<<grid, kThreads, usm, s>>>(a);
+  dk<<<grid, ng_d * kGroupThreads, sm_d, s>>>(a);
+  a.img = d_up1;
+  k1<<<grid, ng_1 * kGroupThreads, sm_1, s>>>(a);
+  a.img = d_up2;
+  k2<<<grid, ng_2 * kGroupThreads, sm_2, s>>>(a);
   return ves_launch_check("tc net block");
 }

@@ -8,16 +8,16 @@
 struct TcBlock {
   int geo[64];          // opaque block geometry (tcnet::Geo)
   int geo_bytes;
-  int dsize, usize;     // weight image bytes per group (down / up kernels)
-  int dsmem, usmem;     // dynamic shared memory of the two kernels
-  int mid_bytes;        // down -> up intermediate per (vesicle, group)
-  size_t down_off, up_off;  // byte offsets of the block's images in the device buffer
+  int dsize, u1size, u2size;  // weight image bytes per group (down / up1 / up2 kernels)
+  int mid_bytes;        // intermediates per (vesicle, group): down -> up1 -> up2
+  size_t down_off, up1_off, up2_off;  // byte offsets of the block's images in the device buffer
 };
 
 // Build the per-group weight images of one block (30 reference parameter
 // arrays, see ves_net_create) for sequence length L.
 int tcnet_pack(const ves_net_block& b, int G, int L, const float* const* params, std::vector<unsigned char>& down,
-               std::vector<unsigned char>& up, TcBlock& out);
+               std::vector<unsigned char>& up1, std::vector<unsigned char>& up2, TcBlock& out);
 // One block: x [nv][G*cin][L] -> out [nv][G*cout][L] (FP32), mid = scratch of nv*G*mid_bytes.
-int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_down, const unsigned char* d_up,
-                    const float* x, float* out, unsigned char* mid, VesDeviceStatus* st, cudaStream_t s);
+int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_down, const unsigned char* d_up1,
+                    const unsigned char* d_up2, const float* x, float* out, unsigned char* mid,
+                    VesDeviceStatus* st, cudaStream_t s);

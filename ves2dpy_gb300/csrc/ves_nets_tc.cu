@@ -45,7 +45,6 @@
 
 namespace tcnet {
 
-constexpr int kThreads = 256;  // two warp groups of four warps
 constexpr int kGroupThreads = 128;
 constexpr int kMinSmem = 117 * 1024;
 constexpr int kOffsets = 11;  // input shifts of a conv pair: -6..6 without +-5
@@ -297,12 +296,20 @@ __device__ __forceinline__ uint4 act8(const float* v, const float* cst, int kc, 
   *reinterpret_cast<float4*>(sh) = *reinterpret_cast<const float4*>(cst + ot + 8 * kc);
   *reinterpret_cast<float4*>(sh + 4) = *reinterpret_cast<const float4*>(cst + ot + 8 * kc + 4);
   float y[8];
-  if (8 * kc + 8 <= nreal) {  // uniform across the warp
+  // packed FP32x2 add and fma: per lane the same rounding as fadd / fmaf
 #pragma unroll
-    for (int e = 0; e < 8; ++e) y[e] = fmaf(fmaxf(v[e] + b[e], 0.f), sc[e], sh[e]);
-  } else {  // the chunk that holds the padding channels (TMEM columns past nreal are not defined)
+  for (int e = 0; e < 8; e += 2) {
+    float2 z = __fadd2_rn(make_float2(v[e], v[e + 1]), make_float2(b[e], b[e + 1]));
+    z.x = fmaxf(z.x, 0.f);
+    z.y = fmaxf(z.y, 0.f);
+    z = __ffma2_rn(z, make_float2(sc[e], sc[e + 1]), make_float2(sh[e], sh[e + 1]));
+    y[e] = z.x;
+    y[e + 1] = z.y;
+  }
+  if (8 * kc + 8 > nreal) {  // the chunk that holds the padding channels (TMEM columns past nreal are not defined)
 #pragma unroll
-    for (int e = 0; e < 8; ++e) y[e] = 8 * kc + e < nreal ? fmaf(fmaxf(v[e] + b[e], 0.f), sc[e], sh[e]) : 0.f;
+    for (int e = 0; e < 8; ++e)
+      if (8 * kc + e >= nreal) y[e] = 0.f;
   }
   return make_uint4(pack_bf2(y[0], y[1]), pack_bf2(y[2], y[3]), pack_bf2(y[4], y[5]), pack_bf2(y[6], y[7]));
 }
@@ -310,7 +317,7 @@ __device__ __forceinline__ uint4 act8(const float* v, const float* cst, int kc, 
 // ---------------------------------------------------------------------------
 // Segments: the CTA's contiguous item range split where the channel group
 // changes; the weight image is reloaded (whole CTA) at each segment start and
-// the two warp groups take the segment's items alternately.
+// the warp groups take the segment's items in turn.
 struct Seg {
   long long lo, hi;
   int grp;
@@ -641,7 +648,7 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) up1_kernel(KArgs a) {
     if (sg.lo + wg < sg.hi) fetch_mid(sg.lo + wg);
     for (long long it = sg.lo + wg; it < sg.hi; it += NG) {
       const long long v = it % a.nv;
-      if (!group_wait(&mbar[wg], mphase, a.st, 26, wg, &fail[wg])) {
+      if (!group_wait_one(&mbar[wg], mphase, a.st, 26, wg, gt, &fail[wg])) {
         failed = true;
         break;
       }
@@ -738,6 +745,17 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) up2_kernel(KArgs a) {
     }
     mpend = true;
   };
+  // block input x[v][grp*cin + c][pos] of an item -> ds (free once the
+  // group's previous mix has completed)
+  auto fetch_x = [&](long long item) {
+    if (gt == 0) {
+      const int grp = (int)(item / a.nv);
+      const long long v = item % a.nv;
+      tc_expect_tx(&rbar[wg], xbytes);
+      tc_bulk_g2s(ds, a.x + ((long long)v * a.G + grp) * (long long)g.cin * L, xbytes, &rbar[wg]);
+    }
+    rpend = true;
+  };
   bool failed = false, stuck = false;
   for (long long lo = rg.lo; lo < rg.hi && !failed;) {
     const Seg sg = next_seg(lo, rg.hi, a.nv);
@@ -745,21 +763,15 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) up2_kernel(KArgs a) {
     copy16(sm, a.img + (size_t)sg.grp * g.u2size, g.u2size);
     tc_fence_async_smem();
     __syncthreads();
-    if (sg.lo + wg < sg.hi) fetch_mid(sg.lo + wg);
+    if (sg.lo + wg < sg.hi) {
+      fetch_mid(sg.lo + wg);
+      if (need_x) fetch_x(sg.lo + wg);
+    }
     for (long long it = sg.lo + wg; it < sg.hi; it += NG) {
       const long long v = it % a.nv;
-      const float* __restrict__ xin = a.x + ((long long)v * a.G + sg.grp) * (long long)g.cin * L;
       float* __restrict__ op = a.out + ((long long)v * a.G + sg.grp) * (long long)cout * L;
-      // the block input lands in ds (free since the previous item's mix completed)
       if (need_x) {
-        if (gt == 0) {
-          tc_expect_tx(&rbar[wg], xbytes);
-          tc_bulk_g2s(ds, xin, xbytes, &rbar[wg]);
-        }
-        rpend = true;
-      }
-      if (need_x) {
-        if (!group_wait(&rbar[wg], rphase, a.st, 27, wg, &fail[wg])) {
+        if (!group_wait_one(&rbar[wg], rphase, a.st, 27, wg, gt, &fail[wg])) {
           failed = true;
           break;
         }
@@ -784,7 +796,7 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) up2_kernel(KArgs a) {
         }
         tc_wait_st();
       }
-      if (!group_wait(&mbar[wg], mphase, a.st, 26, wg, &fail[wg])) {
+      if (!group_wait_one(&mbar[wg], mphase, a.st, 26, wg, gt, &fail[wg])) {
         failed = true;
         break;
       }
@@ -825,6 +837,8 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) up2_kernel(KArgs a) {
       }
       phase ^= 1;
       tc_fence_after_sync();
+      // ds is free once the mix has completed: the block input of this group's next item
+      if (need_x && it + NG < sg.hi) fetch_x(it + NG);
       for (int h = 0; h < nh; ++h) {
         const int p = 128 * h + 32 * qd + lane;
         float vv[32];

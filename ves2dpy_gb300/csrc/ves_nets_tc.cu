@@ -190,17 +190,10 @@ __device__ __forceinline__ void copy16_g(unsigned char* dst, const unsigned char
   uint4* d = reinterpret_cast<uint4*>(dst);
   for (int i = t; i < bytes / 16; i += kGroupThreads) d[i] = s[i];
 }
-// Bounded waits of one warp group on an mbarrier; true when the phase
-// completed (the answer is uniform across the group).  group_wait: every
-// thread polls (data landed by bulk copy, normally already there);
-// group_wait_one: thread 0 of the group polls and the others sleep in the
-// group barrier (MMA completion, hundreds of cycles away).
-__device__ __forceinline__ bool group_wait(uint64_t* bar, unsigned phase, VesDeviceStatus* st, int site, int wg,
-                                           int* flag) {
-  if (!tc_mbar_wait(bar, phase, st, site)) atomicExch(flag, 1);
-  group_sync(wg);
-  return *(volatile int*)flag == 0;
-}
+// Bounded wait of one warp group on an mbarrier; true when the phase
+// completed (the answer is uniform across the group).  Thread 0 of the group
+// polls (sleeping between polls) and the others wait in the group barrier, so
+// a wait that is not yet satisfied takes no issue slots from the other groups.
 __device__ __forceinline__ bool group_wait_one(uint64_t* bar, unsigned phase, VesDeviceStatus* st, int site, int wg,
                                                int gt, int* flag) {
   if (gt == 0 && !tc_mbar_wait_sleep(bar, phase, st, site)) atomicExch(flag, 1);
@@ -425,7 +418,7 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
     if (sg.lo + wg < sg.hi) fetch_x(sg.lo + wg);
     for (long long it = sg.lo + wg; it < sg.hi; it += NG) {
       const long long v = it % a.nv;
-      if (!group_wait(&xbar[wg], xphase, a.st, 20, wg, &fail[wg])) {
+      if (!group_wait_one(&xbar[wg], xphase, a.st, 20, wg, gt, &fail[wg])) {
         failed = true;
         break;
       }

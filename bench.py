@@ -390,13 +390,14 @@ def run_gb300(a, rank, world):
     net_tflops = sum(flops.values()) / (net_total_ms * 1e-3) / 1e12 if net_total_ms > 0 else None
     # networks, timed live inside the timed MLARM steps (CUDA events around each forward pass)
     nl_tflops = (st.networks_flops / (st.networks_ms * 1e-3) / 1e12) if st.networks_ms > 0 else None
-    roof_net = {"bound": "tensor", "kernel": "tcnet::down_kernel / up_kernel (tcgen05.mma kind::f16, BF16)",
+    roof_net = {"bound": "tensor",
+                "kernel": "tcnet::down_kernel / up1_kernel / up2_kernel (tcgen05.mma kind::f16, BF16)",
                 "achieved": nl_tflops, "peak": bf16_peak, "unit": "TFLOP/s",
                 "frac": nl_tflops / bf16_peak if nl_tflops else None, "traffic": None,
-                "traffic_note": "ncu (profiles/tcnet_adv_block_nv64_full.md): one down+up launch pair of an "
-                                "advection-network block at nv=64 moves 215 + 383 MB of DRAM, the FP32 block input "
-                                "read twice, the output written once and the BF16 intermediate written and read "
-                                "(no re-reads); per launch it scales with nv",
+                "traffic_note": "ncu (profiles/tcnet_blocks_nv64_full.md): the down + up1 + up2 launches of one "
+                                "advection-network block at nv=64 move 25 + 99 + 250 MB of DRAM (the FP32 block "
+                                "input read by down and up2, the output written by up2, the BF16 intermediates "
+                                "written and read once; no re-reads), at most 20% of the DRAM peak",
                 "flops_per_step": st.networks_flops / a.steps, "ms_per_step": st.networks_ms / a.steps,
                 "passes_per_step": st.networks_launches / a.steps,
                 "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured",

@@ -209,20 +209,27 @@ VES_API size_t ves_stokes_dl_matrix_workspace(ves_ctx* ctx, int nv, int precisio
 /* den[nv][2][ns] = f * sa * 2*pi/ns * (1 - visc)  (poten.py:411; visc NULL: all 1) */
 VES_API int ves_dl_density(int nv, int ns, const double* f, const double* sa, const double* visc, double* den,
                            void* stream);
-/* Direct double-layer sum, exactStokesDL (poten.py:399-441):
+/* Double-layer sum, exactStokesDL (poten.py:399-441):
  *   u(x) = 1/pi sum_src ((r.n)(r.den)/|r|^4) r,  r = x - y,  n = (ty, -tx),
  * sources Xsrc[nsrc][2][ns] with unit tangents tang[nsrc][2][ns] and den from
- * ves_dl_density; targets Xtar[nt][2][ntp] (ntp <= 1024); self_idx and nl as
- * ves_farfield.  FP64. */
-VES_API int ves_farfield_dl(ves_ctx* ctx, int nsrc, int ns, const double* Xsrc, const double* tang,
-                            const double* den, int nt, int ntp, const double* Xtar, const int* self_idx,
-                            const ves_near_lists* nl, double* out, void* stream);
+ * ves_dl_density; targets Xtar[nt][2][ntp]; self_idx and nl as ves_farfield.
+ * precision VES_PREC_FP64: direct FP64 sum (ntp <= 1024, no workspace);
+ * VES_PREC_FP32M (or FP32C): multipole series of each source vesicle for the
+ * separated pairs, direct FP64 for the others (ntp <= 128; needs the source
+ * jacobian sa[nsrc][ns] and contrasts visc[nsrc] of the density, and the
+ * workspace of ves_farfield_dl_workspace). */
+VES_API int ves_farfield_dl(ves_ctx* ctx, int precision, int nsrc, int ns, const double* Xsrc, const double* tang,
+                            const double* den, const double* sa, const double* visc, int nt, int ntp,
+                            const double* Xtar, const int* self_idx, const ves_near_lists* nl, double* out,
+                            void* ws, size_t ws_bytes, void* stream);
+VES_API size_t ves_farfield_dl_workspace(int precision, int nsrc, int nt, int ntp);
 /* nearSingInt with kernelDirect = exactStokesDL (tstep_biem.py:236,501;
  * poten_py.m:495-692): double-layer far field over the Nup-upsampled sources
  * (Xup, tang_up, sa_up of the upsampled curve) with the near pairs removed,
  * plus the near correction from vself = jump f + D f.  scheme:
- * VES_NEAR_NONE, VES_NEAR_PY_HH or VES_NEAR_MATLAB. */
-VES_API int ves_near_sing_int_dl(ves_ctx* ctx, int scheme, int nv, const double* X, const double* Xup,
+ * VES_NEAR_NONE, VES_NEAR_PY_HH or VES_NEAR_MATLAB; precision as
+ * ves_farfield_dl. */
+VES_API int ves_near_sing_int_dl(ves_ctx* ctx, int scheme, int precision, int nv, const double* X, const double* Xup,
                                  const double* tang_up, const double* sa_up, const double* visc, const double* f,
                                  const double* vself, const ves_near_lists* nl, double h, double* LP,
                                  double* near_only, void* ws, size_t ws_bytes, void* stream);

@@ -143,3 +143,69 @@ def test_time_step_viscosity_contrast_preconditioned(golden):
     Xn, sn, _, _, it, iflag = _dl_step(g, True)
     assert not iflag and it < int(g["step_iter1"]) // 5, it
     assert rel(Xn, g["step_X1"]) < 1e-8, rel(Xn, g["step_X1"])
+
+
+UNIT_AREA = 0.65 / (4 * np.pi)  # reduced area 0.65 at unit length
+
+
+@pytest.mark.parametrize("nv,N,frac", [(256, 32, 0.2), (512, 128, 0.15)])
+def test_double_layer_multipole_vs_direct(nv, N, frac):
+    """exactStokesDL with the multipole series for separated pairs (FP32M)
+    against the FP64 direct sum, for a random density and for the positions
+    themselves (the density the step applies the operator to: a large mean
+    that the double layer of a closed curve cancels)."""
+    from ves2dpy_gb300.capsules import capsules
+    from ves2dpy_gb300.poten import Poten
+    from ves2dpy_gb300.suspension import random_suspension
+    X = random_suspension(nv, N, frac, min_gap=0.02, area=UNIT_AREA, seed=5)
+    rng = np.random.default_rng(9)
+    visc = rng.choice([0.5, 1.0, 3.0], size=nv)
+    ves = capsules(T(X), None, None, 1.0, torch.tensor(visc))
+    op = Poten(N)
+    for f in (T(rng.normal(size=(2 * N, nv))), T(X)):
+        # targets: 24 vesicles of the suspension, each against all the others
+        got, ref = [], []
+        for c in range(0, nv, nv // 24):
+            K = [j for j in range(nv) if j != c]
+            got.append(op.exactStokesDL(ves, f, ves.X[:, c:c + 1], K, precision="fp32m"))
+            ref.append(op.exactStokesDL(ves, f, ves.X[:, c:c + 1], K))
+        err = rel(torch.cat(got, 1), torch.cat(ref, 1).cpu().numpy())
+        assert err < 2e-6, err
+
+
+def test_near_sing_int_dl_multipole_with_near_pairs(golden):
+    """nearSingInt with the double layer, FP32M far field vs FP64, on the
+    packed cluster (near pairs: those pairs are summed directly in both)."""
+    from ves2dpy_gb300.biem_support import naiveNearZoneInfo
+    from ves2dpy_gb300.capsules import capsules
+    from ves2dpy_gb300.poten import Poten
+    X = golden("far_fp64")["X"]
+    N, nv = X.shape[0] // 2, X.shape[1]
+    visc = np.array([2.0, 1.0, 0.5, 3.0, 1.5, 0.8])[:nv]
+    ves = capsules(T(X), None, None, 1.0, torch.tensor(visc))
+    op = Poten(N)
+    D = op.stokesDLmatrix(ves)
+    jump = 0.5 * (1 - torch.tensor(visc, device=dev()))
+    DLP = lambda F: F * jump[None, :] + op.exactStokesDLdiag(ves, D, F)  # noqa: E731
+    near = naiveNearZoneInfo(T(X), None)
+    for f in (T(np.random.default_rng(4).normal(size=(2 * N, nv))), T(X)):
+        a = op.nearSingInt(ves, f, DLP, near, op.exactStokesDL, ves, True, precision="fp64")
+        b = op.nearSingInt(ves, f, DLP, near, op.exactStokesDL, ves, True, precision="fp32m")
+        assert rel(b, a.cpu().numpy()) < 1e-6, rel(b, a.cpu().numpy())
+
+
+def test_time_step_viscosity_contrast_multipole(golden):
+    """The contrast step with both far fields in FP32M (single layer and
+    double layer) and the FP32 Alpert build, preconditioned, GMRES to 1e-8:
+    positions within 1e-7 of the reference's FP64 step."""
+    from ves2dpy_gb300.tstep_biem import TStepBiem
+    g = golden("dl_fp64")
+    X = g["step_X0"]
+    N, nv = X.shape[0] // 2, X.shape[1]
+    prams = dict(dt=float(g["step_dt"]), kappa=1.0, gmresTol=1e-8, gmresMaxIter=200,
+                 farFieldSpeed=float(g["step_speed"]), viscCont=torch.tensor(g["step_visc"]))
+    options = dict(farField="shear", usePreco=True, repulsion=False)
+    tt = TStepBiem(T(X), None, options, prams, near="py_hh", farfield_precision="fp32m", sl_precision="fp32c")
+    Xn, sn, _, _, it, iflag = tt.time_step(T(X), torch.zeros(N, nv, dtype=torch.float64, device=dev()))
+    assert not iflag
+    assert rel(Xn, g["step_X1"]) < 1e-7, rel(Xn, g["step_X1"])

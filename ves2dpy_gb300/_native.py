@@ -210,9 +210,11 @@ SIGNATURES = {
     "ves_stokes_dl_matrix": (_I, [_P, _I, _P, _P, _I, _P, _P, _SZ, _P]),
     "ves_stokes_dl_matrix_workspace": (_SZ, [_P, _I, _I]),
     "ves_dl_density": (_I, [_I, _I, _P, _P, _P, _P, _P]),
-    "ves_farfield_dl": (_I, [_P, _I, _I, _P, _P, _P, _I, _I, _P, _P, ctypes.POINTER(NearLists), _P, _P]),
-    "ves_near_sing_int_dl": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(NearLists), _D, _P, _P,
-                                  _P, _SZ, _P]),
+    "ves_farfield_dl": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P, _I, _I, _P, _P, ctypes.POINTER(NearLists), _P,
+                             _P, _SZ, _P]),
+    "ves_farfield_dl_workspace": (_SZ, [_I, _I, _I, _I]),
+    "ves_near_sing_int_dl": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(NearLists), _D, _P,
+                                  _P, _P, _SZ, _P]),
     "ves_near_sing_int_dl_workspace": (_SZ, [_P, _I]),
     "ves_repulsion_force_workspace": (_SZ, [_I]),
     "ves_repulsion_force": (_I, [_I, _I, _P, _D, _D, _P, _P, _SZ, _P]),

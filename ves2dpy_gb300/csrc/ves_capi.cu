@@ -189,12 +189,12 @@ extern "C" int ves_near_sing_int(ves_ctx* c, int scheme, int precision, int nv, 
 extern "C" size_t ves_near_sing_int_dl_workspace(ves_ctx* c, int nv) {
   if (!c) return 0;
   WsCarver w(nullptr, 0);
-  near_sing_int_dl_run(c, VES_NEAR_PY_HH, nv, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
-                       0, nullptr, nullptr, w, 0);
+  near_sing_int_dl_run(c, VES_NEAR_PY_HH, VES_PREC_FP32M, nv, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                       nullptr, nullptr, 0, nullptr, nullptr, w, 0);
   return w.off + 256;
 }
 
-extern "C" int ves_near_sing_int_dl(ves_ctx* c, int scheme, int nv, const double* X, const double* Xup,
+extern "C" int ves_near_sing_int_dl(ves_ctx* c, int scheme, int precision, int nv, const double* X, const double* Xup,
                                     const double* tang_up, const double* sa_up, const double* visc, const double* f,
                                     const double* vself, const ves_near_lists* nl, double h, double* LP,
                                     double* near_only, void* ws, size_t ws_bytes, void* stream) {
@@ -205,7 +205,8 @@ extern "C" int ves_near_sing_int_dl(ves_ctx* c, int scheme, int nv, const double
   int rc = ves_reset_status(c, s);
   if (rc) return rc;
   WsCarver w(ws, ws_bytes);
-  rc = near_sing_int_dl_run(c, scheme, nv, X, Xup, tang_up, sa_up, visc, f, vself, nl, h, LP, near_only, w, s);
+  rc = near_sing_int_dl_run(c, scheme, precision, nv, X, Xup, tang_up, sa_up, visc, f, vself, nl, h, LP, near_only, w,
+                            s);
   if (rc) return rc;
   return finish(c, s, "ves_near_sing_int_dl");
 }

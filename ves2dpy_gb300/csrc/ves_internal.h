@@ -165,13 +165,15 @@ int stokes_dl_matrix(ves_ctx* c, int nv, const double* X, const double* visc, in
                      cudaStream_t s);
 void launch_dl_density(int nv, int ns, const double* f, const double* sa, const double* visc, double* den,
                        cudaStream_t s);
-int farfield_dl_run(ves_ctx* c, int nsrc, int ns, const double* Xsrc, const double* tang, const double* den, int nt,
-                    int ntp, const double* Xtar, const int* self_idx, const ves_near_lists* nl, double* out,
-                    cudaStream_t s);
-int near_sing_int_dl_run(ves_ctx* c, int scheme, int nv, const double* X, const double* Xup, const double* tang_up,
-                         const double* sa_up, const double* visc, const double* f, const double* vself,
-                         const ves_near_lists* nl, double h, double* LP, double* near_only, WsCarver& ws,
-                         cudaStream_t s);
+// precision VES_PREC_FP64: direct FP64 sum; FP32C / FP32M: multipole series for
+// separated pairs, direct FP64 for close ones (sa, visc of the sources required)
+int farfield_dl_run(ves_ctx* c, int precision, int nsrc, int ns, const double* Xsrc, const double* tang,
+                    const double* den, const double* sa, const double* visc, int nt, int ntp, const double* Xtar,
+                    const int* self_idx, const ves_near_lists* nl, double* out, WsCarver& ws, cudaStream_t s);
+int near_sing_int_dl_run(ves_ctx* c, int scheme, int precision, int nv, const double* X, const double* Xup,
+                         const double* tang_up, const double* sa_up, const double* visc, const double* f,
+                         const double* vself, const ves_near_lists* nl, double h, double* LP, double* near_only,
+                         WsCarver& ws, cudaStream_t s);
 
 // RBF near-field fits (nearSingInt_rbf): adds the fits of the near pairs to LP
 int rbf_near_correct(ves_ctx* c, int nv, const double* X, const double* f, const double* vself,

@@ -532,15 +532,19 @@ int near_sing_int_run(ves_ctx* c, int scheme, int precision, int nv, const doubl
 // removed, plus the correction from vself = jump f + D f: the py_hh rule
 // (which uses vself only) or the MATLAB Lagrange extrapolation with the
 // double layer at the Lagrange points.
-int near_sing_int_dl_run(ves_ctx* c, int scheme, int nv, const double* X, const double* Xup, const double* tang_up,
-                         const double* sa_up, const double* visc, const double* f, const double* vself,
-                         const ves_near_lists* nl, double h, double* LP, double* near_only, WsCarver& ws,
-                         cudaStream_t s) {
+int near_sing_int_dl_run(ves_ctx* c, int scheme, int precision, int nv, const double* X, const double* Xup,
+                         const double* tang_up, const double* sa_up, const double* visc, const double* f,
+                         const double* vself, const ves_near_lists* nl, double h, double* LP, double* near_only,
+                         WsCarver& ws, cudaStream_t s) {
   const int N = c->N, Nup = c->Nup;
   double* fup = ws.take<double>((size_t)nv * 2 * Nup);
   double* den = ws.take<double>((size_t)nv * 2 * Nup);
   int* selfidx = ws.take<int>((size_t)nv);
-  if (ws.sizing) return VES_OK;
+  const ves_near_lists* excl = (scheme == VES_NEAR_NONE) ? nullptr : nl;
+  if (ws.sizing) {
+    return farfield_dl_run(c, precision, nv, Nup, Xup, tang_up, den, sa_up, visc, nv, N, X, selfidx, excl, LP, ws,
+                           s);
+  }
   if (!ws.ok()) {
     ves_record_error(VES_ERR_WORKSPACE, "near_sing_int_dl: workspace too small");
     return VES_ERR_WORKSPACE;
@@ -564,8 +568,8 @@ int near_sing_int_dl_run(ves_ctx* c, int scheme, int nv, const double* X, const 
   launch_dl_density(nv, Nup, fup, sa_up, visc, den, s);
   ves_count_launch();
   identity_index_kernel<<<ceil_div(nv, 256), 256, 0, s>>>(nv, selfidx);
-  int rc = farfield_dl_run(c, nv, Nup, Xup, tang_up, den, nv, N, X, selfidx, scheme == VES_NEAR_NONE ? nullptr : nl,
-                           LP, s);
+  int rc = farfield_dl_run(c, precision, nv, Nup, Xup, tang_up, den, sa_up, visc, nv, N, X, selfidx, excl, LP, ws,
+                           s);
   if (rc) return rc;
   if (scheme == VES_NEAR_PY_HH) {
     const long long warps = (long long)nv * nl->maxc;

@@ -224,7 +224,8 @@ int matvec(StepState& S, const double* v, double* out) {
     ves_count_launch();
     dl_self_kernel<<<ceil_div(n2, 256), 256, 0, S.s>>>(n2, N, S.visc, S.Xm, 2LL * N, S.DX, S.vdl);
     WsCarver sub2(S.scratch, S.scratch_bytes);
-    if ((rc = near_sing_int_dl_run(c, S.dl_scheme, nv, S.X, S.Xup, S.tang_up, S.sa_up, S.visc, S.Xm, S.vdl, &S.nl,
+    if ((rc = near_sing_int_dl_run(c, S.dl_scheme, S.prm->farfield_precision, nv, S.X, S.Xup, S.tang_up, S.sa_up,
+                                   S.visc, S.Xm, S.vdl, &S.nl,
                                    S.h, S.Fdl, nullptr, sub2, S.s)))
       return rc;
   }
@@ -512,7 +513,8 @@ static int biem_step_impl(ves_ctx* c, const ves_step_params* prm, int nv, const 
     stokes_dl_matrix(c, nv, nullptr, nullptr, prm->sl_precision, nullptr, w, s);
     scratch = std::max(scratch, w.off);
     WsCarver w2(nullptr, 0);
-    near_sing_int_dl_run(c, S.dl_scheme, nv, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+    near_sing_int_dl_run(c, S.dl_scheme, prm->farfield_precision, nv, nullptr, nullptr, nullptr, nullptr, nullptr,
+                         nullptr, nullptr, nullptr,
                          0, nullptr, nullptr, w2, s);
     scratch = std::max(scratch, w2.off);
   }
@@ -591,7 +593,8 @@ static int biem_step_impl(ves_ctx* c, const ves_step_params* prm, int nv, const 
     ves_count_launch();
     dl_self_kernel<<<ceil_div(n2, 256), 256, 0, s>>>(n2, N, S.visc, X, 2LL * N, S.DX, S.vdl);
     WsCarver sub(S.scratch, S.scratch_bytes);
-    if ((rc = near_sing_int_dl_run(c, S.dl_scheme, nv, X, S.Xup, S.tang_up, S.sa_up, S.visc, X, S.vdl, &S.nl, S.h,
+    if ((rc = near_sing_int_dl_run(c, S.dl_scheme, prm->farfield_precision, nv, X, S.Xup, S.tang_up, S.sa_up, S.visc,
+                                   X, S.vdl, &S.nl, S.h,
                                    S.Fdl, nullptr, sub, s)))
       goto done;
   }

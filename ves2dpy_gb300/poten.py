@@ -91,9 +91,11 @@ class Poten:
         return self.exactStokesSLdiag(vesicle, D, f)
 
     # -- between vesicles ------------------------------------------------------
-    def exactStokesDL(self, vesicle, f, Xtar=None, K1=None):
+    def exactStokesDL(self, vesicle, f, Xtar=None, K1=None, precision: str = "fp64"):
         """Double layer of vesicles K1 (density f, scaled by 1 - viscCont) at
-        every column of Xtar (poten.py:399-441), in FP64."""
+        every column of Xtar (poten.py:399-441).  ``precision`` "fp64": direct
+        FP64 sum; "fp32m": multipole series for the separated vesicle-target
+        pairs (at most 128 points per target column), direct FP64 for the rest."""
         Xtar = as_device_f64(Xtar)
         if Xtar.dim() == 1:
             Xtar = Xtar.unsqueeze(1)
@@ -112,11 +114,14 @@ class Poten:
                   "exactStokesDL density")
         Xt = to_vm(Xtar)
         out = torch.empty(ncol, 2 * ntp, dtype=torch.float64, device=dev)
-        nat.check(lib.ves_farfield_dl(self._ctx.handle, len(K1), N, Xs.data_ptr(), ts.data_ptr(), den.data_ptr(),
-                                      ncol, ntp, Xt.data_ptr(), None, None, out.data_ptr(), st), "exactStokesDL")
+        prec = nat.PREC[precision]
+        ws = self._ctx.workspace(lib.ves_farfield_dl_workspace(prec, len(K1), ncol, ntp))
+        nat.check(lib.ves_farfield_dl(self._ctx.handle, prec, len(K1), N, Xs.data_ptr(), ts.data_ptr(), den.data_ptr(),
+                                      sas.data_ptr(), visc.data_ptr(), ncol, ntp, Xt.data_ptr(), None, None,
+                                      out.data_ptr(), ws.data_ptr(), ws.numel(), st), "exactStokesDL")
         return from_vm(out)
 
-    def _near_dl(self, scheme, vesicleSou, f, selfMat, Near):
+    def _near_dl(self, scheme, vesicleSou, f, selfMat, Near, precision="fp64"):
         """nearSingInt with kernelDirect = exactStokesDL on the device."""
         X = as_device_f64(vesicleSou.X)
         N, nv = X.shape[0] // 2, X.shape[1]
@@ -135,7 +140,8 @@ class Poten:
         ws = ctx.workspace(ctx.lib.ves_near_sing_int_dl_workspace(ctx.handle, nv))
         stc = Near.struct() if Near is not None else None
         h = Near.h if Near is not None else 0.0
-        nat.check(ctx.lib.ves_near_sing_int_dl(ctx.handle, nat.NEAR[scheme], nv, Xv.data_ptr(), Xup.data_ptr(),
+        nat.check(ctx.lib.ves_near_sing_int_dl(ctx.handle, nat.NEAR[scheme], nat.PREC[precision], nv, Xv.data_ptr(),
+                                               Xup.data_ptr(),
                                                tang_up.data_ptr(), sa_up.data_ptr(), visc.data_ptr(), fv.data_ptr(),
                                                nat.ptr(vself), ctypes.byref(stc) if stc is not None else None,
                                                float(h), LP.data_ptr(), None, ws.data_ptr(), ws.numel(), st),
@@ -194,7 +200,7 @@ class Poten:
         if not isinstance(NearV2V, NearZone) or NearV2V.scheme != "py_hh":
             raise TypeError("NearV2V must come from naiveNearZoneInfo")
         if _is_double_layer(kernelDirect):
-            return self._near_dl("py_hh", vesicleSou, f, selfMat, NearV2V), None
+            return self._near_dl("py_hh", vesicleSou, f, selfMat, NearV2V, precision), None
         return self._near_common("py_hh", vesicleSou, f, selfMat, NearV2V, precision)
 
     def nearSingInt_rbf(self, vesicleSou, f, selfMat, NearV2V, kernelDirect=None, vesicleTar=None, tEqualS=True,
@@ -229,11 +235,11 @@ class Poten:
             return torch.zeros_like(as_device_f64(vesicleSou.X))
         if _is_double_layer(kernelDirect):
             if NearStruct is None:
-                return self._near_dl("none", vesicleSou, f, None, None)
+                return self._near_dl("none", vesicleSou, f, None, None, precision)
             if not isinstance(NearStruct, NearZone):
                 raise TypeError("NearStruct must come from capsules.getZone or naiveNearZoneInfo")
             return self._near_dl("matlab" if NearStruct.scheme == "matlab" else "py_hh", vesicleSou, f, selfMat,
-                                 NearStruct)
+                                 NearStruct, precision)
         if NearStruct is None:
             return self._near_common("none", vesicleSou, f, None, None, precision)[0]
         if not isinstance(NearStruct, NearZone) or NearStruct.scheme != "matlab":

@@ -33,7 +33,14 @@
 //   trapezoid rule keeps that to rounding for separated targets, while the
 //   mean of a position-like density (the step applies the operator to X) would
 //   otherwise dominate the FP32 moments.  Close pairs and pairs on the near
-//   candidate list are summed directly in FP64 with the full density.
+//   candidate list are summed directly in FP32 over the upsampled points with
+//   the same mean-free density: a target more than 12 upsampled spacings from
+//   every source point sees the trapezoid rule of the constant density's
+//   double layer exact to rounding (its error decays like
+//   exp(-2 pi distance / spacing)), so dropping the mean changes the sum by
+//   rounding only; a target closer than that is summed again in FP64 with the
+//   full density (only without near lists: the near zone of the step, 1/N for
+//   unit length, is those 12 spacings, and its points are excluded).
 //   Sources without a contrast (visc == 1) have zero density and are skipped.
 #include "ves_internal.h"
 
@@ -324,7 +331,8 @@ struct __align__(16) DLSrc {
   float2 chi, clo;  // centre, high and low FP32 parts
   float R;          // bound on |y_j - c0|
   int skip;         // no contrast: zero density
-  float pad0, pad1;
+  float thr2;       // (12 upsampled spacings)^2: closer targets are summed in FP64
+  float pad1;
 };
 // one order k: C_k, E_k, (k+1) C_k, (k+1) G_k of the normalised moments
 struct __align__(16) DLMom {
@@ -342,7 +350,8 @@ __global__ void __launch_bounds__(256) dl_mp_prep_kernel(int ns, const double* _
                                                          const double* __restrict__ den,
                                                          const double* __restrict__ sa,
                                                          const double* __restrict__ visc, DLSrc* __restrict__ src,
-                                                         DLMom* __restrict__ mom) {
+                                                         DLMom* __restrict__ mom, float4* __restrict__ recA,
+                                                         float2* __restrict__ recB) {
   __shared__ double red[4][256];
   const int s = blockIdx.x, t = threadIdx.x;
   const double* x = X + (long long)s * 2 * ns;
@@ -366,16 +375,18 @@ __global__ void __launch_bounds__(256) dl_mp_prep_kernel(int ns, const double* _
       __syncthreads();
     }
   };
-  double sx = 0, sy = 0, sw = 0, sdx = 0, sdy = 0;
+  double sx = 0, sy = 0, sw = 0, sdx = 0, sdy = 0, sl = 0;
   for (int j = t; j < ns; j += 256) {
     sx += x[j];
     sy += x[ns + j];
     sw += js[j] * wscale;
     sdx += d[j];
     sdy += d[ns + j];
+    sl += js[j];
   }
-  block_sum4(sx, sy, sw, 0.0, false);
+  block_sum4(sx, sy, sw, sl, false);
   const double ccx = red[0][0] / ns, ccy = red[1][0] / ns, W = red[2][0];
+  const double hsp = red[3][0] * (2.0 * VES_PI / ns) / ns;  // mean spacing = length / ns
   __syncthreads();
   block_sum4(0.0, sdx, sdy, 0.0, false);
   const double fbx = (W != 0.0) ? red[1][0] / W : 0.0, fby = (W != 0.0) ? red[2][0] / W : 0.0;
@@ -384,6 +395,10 @@ __global__ void __launch_bounds__(256) dl_mp_prep_kernel(int ns, const double* _
   for (int j = t; j < ns; j += 256) {
     const double lx = x[j] - ccx, ly = x[ns + j] - ccy;
     r2 = fmax(r2, lx * lx + ly * ly);
+    // FP32 records of the direct rule: local position, normal, mean-free density
+    const double w = js[j] * wscale;
+    recA[(long long)s * ns + j] = make_float4((float)lx, (float)ly, (float)tg[ns + j], (float)(-tg[j]));
+    recB[(long long)s * ns + j] = make_float2((float)(d[j] - fbx * w), (float)(d[ns + j] - fby * w));
   }
   block_sum4(r2, 0.0, 0.0, 0.0, true);
   double R = sqrt(red[0][0]) * (1.0 + 1e-6);
@@ -394,7 +409,8 @@ __global__ void __launch_bounds__(256) dl_mp_prep_kernel(int ns, const double* _
     o.clo = make_float2((float)(ccx - (double)o.chi.x), (float)(ccy - (double)o.chi.y));
     o.R = (float)R;
     o.skip = (wscale == 0.0) ? 1 : 0;
-    o.pad0 = o.pad1 = 0.f;
+    o.thr2 = (float)(144.0 * hsp * hsp);
+    o.pad1 = 0.f;
     src[s] = o;
   }
   // moments: warp w takes orders k = w, w + 8, ... (<= kDLPMax); lanes split the points
@@ -486,12 +502,14 @@ __global__ void __launch_bounds__(256) dl_mp_targets_kernel(int ntp, const doubl
 
 struct DLMPArgs {
   int nsrc, ns, ntp;
-  const double* Xsrc;
+  const float4* recA;  // [nsrc][ns] local x, y, normal x, y
+  const float2* recB;  // [nsrc][ns] mean-free density
+  const double* Xsrc;  // the FP64 sources (targets within 6 spacings)
   const double* tang;
   const double* den;
+  const double* Xtar;
   const DLSrc* src;
   const DLMom* mom;
-  const double* Xtar;
   const float2* tloc;
   const float2* thi;
   const float2* tlo;
@@ -515,8 +533,11 @@ __device__ __forceinline__ int dl_order(float rp) {
   return kDLPMax;
 }
 
-// One CTA per target column (blockDim = ntp rounded up to a warp multiple, <= 128)
+// One CTA per target column (blockDim = ntp rounded up to a warp multiple, <= 128).
+// Dynamic shared memory: the direct-rule records of one source (ns float4 + ns float2).
 __global__ void __launch_bounds__(128) dl_mp_eval_kernel(DLMPArgs p) {
+  extern __shared__ __align__(16) float4 dA[];
+  float2* dB = reinterpret_cast<float2*>(dA + p.ns);
   __shared__ DLSrc ssrc[kDLStage];
   __shared__ DLMom smom[kDLStage][kDLPMax + 1];
   __shared__ float rmax_w[4];
@@ -600,25 +621,53 @@ __global__ void __launch_bounds__(128) dl_mp_eval_kernel(DLMPArgs p) {
           ay += 0.25 * (double)(t1i + t2i + t3i - t4i);
         }
       } else {
+        // direct rule over the upsampled points, FP32, coordinates relative to the source centre
+        __syncthreads();
+        const float4* A4 = p.recA + (long long)s * p.ns;
+        const float2* B2 = p.recB + (long long)s * p.ns;
+        for (int j = i; j < p.ns; j += blockDim.x) {
+          dA[j] = A4[j];
+          dB[j] = B2[j];
+        }
+        __syncthreads();
         bool excl = !valid;
         if (cand && valid) {
           const uint32_t w = p.excl_mask[((long long)col * p.maxc + cidx) * p.nwords + (i >> 5)];
           excl = (w >> (i & 31)) & 1u;
         }
         if (!excl) {
-          const double* xs = p.Xsrc + (long long)s * 2 * p.ns;
-          const double* ts = p.tang + (long long)s * 2 * p.ns;
-          const double* ds = p.den + (long long)s * 2 * p.ns;
-          double bx = 0.0, by = 0.0;
+          const float tx = tl.x + ox, ty = tl.y + oy;
+          float bx = 0.f, by = 0.f, dmin = 3.0e38f;
+#pragma unroll 4
           for (int j = 0; j < p.ns; ++j) {
-            const double dx = txa - xs[j], dy = tya - xs[p.ns + j];
-            const double d2 = dx * dx + dy * dy;
-            const double c = ((dx * ts[p.ns + j] - dy * ts[j]) / (d2 * d2)) * (dx * ds[j] + dy * ds[p.ns + j]);
-            bx = fma(c, dx, bx);
-            by = fma(c, dy, by);
+            const float4 a = dA[j];
+            const float2 b = dB[j];
+            const float dx = tx - a.x, dy = ty - a.y;
+            const float d2 = fmaf(dx, dx, dy * dy);
+            dmin = fminf(dmin, d2);
+            const float inv = 1.0f / d2;
+            const float c = fmaf(dx, a.z, dy * a.w) * fmaf(dx, b.x, dy * b.y) * (inv * inv);
+            bx = fmaf(c, dx, bx);
+            by = fmaf(c, dy, by);
           }
-          ax += bx;
-          ay += by;
+          if (dmin >= S.thr2) {
+            ax += (double)bx;
+            ay += (double)by;
+          } else {  // within 12 spacings: the full density in FP64
+            const double* xs = p.Xsrc + (long long)s * 2 * p.ns;
+            const double* ts = p.tang + (long long)s * 2 * p.ns;
+            const double* ds = p.den + (long long)s * 2 * p.ns;
+            double cx = 0.0, cy = 0.0;
+            for (int j = 0; j < p.ns; ++j) {
+              const double dx = txa - xs[j], dy = tya - xs[p.ns + j];
+              const double d2 = dx * dx + dy * dy;
+              const double c = ((dx * ts[p.ns + j] - dy * ts[j]) / (d2 * d2)) * (dx * ds[j] + dy * ds[p.ns + j]);
+              cx = fma(c, dx, cx);
+              cy = fma(c, dy, cy);
+            }
+            ax += cx;
+            ay += cy;
+          }
         }
       }
     }
@@ -636,6 +685,8 @@ int farfield_dl_mp_run(ves_ctx* c, int nsrc, int ns, const double* Xsrc, const d
                        const int* self_idx, const ves_near_lists* nl, double* out, WsCarver& ws, cudaStream_t s) {
   DLSrc* src = ws.take<DLSrc>(nsrc > 0 ? nsrc : 1);
   DLMom* mom = ws.take<DLMom>((size_t)(nsrc > 0 ? nsrc : 1) * (kDLPMax + 1));
+  float4* recA = ws.take<float4>((size_t)(nsrc > 0 ? nsrc : 1) * ns);
+  float2* recB = ws.take<float2>((size_t)(nsrc > 0 ? nsrc : 1) * ns);
   float2* tloc = ws.take<float2>((size_t)(nt > 0 ? nt : 1) * (ntp > 0 ? ntp : 1));
   float2* thi = ws.take<float2>(nt > 0 ? nt : 1);
   float2* tlo = ws.take<float2>(nt > 0 ? nt : 1);
@@ -659,19 +710,31 @@ int farfield_dl_mp_run(ves_ctx* c, int nsrc, int ns, const double* Xsrc, const d
     ves_record_error(VES_ERR_ARG, "farfield_dl: the multipole path needs the source jacobian sa");
     return VES_ERR_ARG;
   }
+  const size_t dsmem = (size_t)ns * (sizeof(float4) + sizeof(float2));
+  if (dsmem > 200 * 1024) {
+    ves_record_error(VES_ERR_SHAPE, "farfield_dl: %d source points per vesicle exceed the multipole path", ns);
+    return VES_ERR_SHAPE;
+  }
+  if (dsmem > 32 * 1024) {  // with the ~13 KB of static shared memory, past the 48 KB default
+    const int rc = ves_cuda_status(
+        cudaFuncSetAttribute(dl_mp_eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem), "dl smem");
+    if (rc) return rc;
+  }
   ves_count_launch(3);
-  dl_mp_prep_kernel<<<nsrc, 256, 0, s>>>(ns, Xsrc, tang, den, sa, visc, src, mom);
+  dl_mp_prep_kernel<<<nsrc, 256, 0, s>>>(ns, Xsrc, tang, den, sa, visc, src, mom, recA, recB);
   dl_mp_targets_kernel<<<nt, 256, 0, s>>>(ntp, Xtar, tloc, thi, tlo);
   DLMPArgs a;
   a.nsrc = nsrc;
   a.ns = ns;
   a.ntp = ntp;
+  a.recA = recA;
+  a.recB = recB;
   a.Xsrc = Xsrc;
   a.tang = tang;
   a.den = den;
+  a.Xtar = Xtar;
   a.src = src;
   a.mom = mom;
-  a.Xtar = Xtar;
   a.tloc = tloc;
   a.thi = thi;
   a.tlo = tlo;
@@ -682,7 +745,7 @@ int farfield_dl_mp_run(ves_ctx* c, int nsrc, int ns, const double* Xsrc, const d
   a.maxc = nl ? nl->maxc : 0;
   a.nwords = (ntp + 31) / 32;
   a.out = out;
-  dl_mp_eval_kernel<<<nt, ((ntp + 31) / 32) * 32, 0, s>>>(a);
+  dl_mp_eval_kernel<<<nt, ((ntp + 31) / 32) * 32, dsmem, s>>>(a);
   return ves_launch_check("farfield_dl multipole");
 }
 

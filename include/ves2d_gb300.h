@@ -480,6 +480,11 @@ VES_API int ves_ctx_stats(ves_ctx* ctx, ves_stats* out, int reset);
 /* Measured MUFU throughput of this GPU: lg2.approx + rcp.approx operations
  * per second over all SMs (a ~0.1 s probe on ``stream``). */
 VES_API int ves_probe_sfu_peak(double* ops_per_second, void* stream);
+/* Failure-path check: a kernel waits on an mbarrier that nothing completes,
+ * with the bounded wait of the tensor-core kernels (2^20 polls with sleeps:
+ * 0.13 s on a GB300); returns VES_ERR_TIMEOUT and leaves the context usable
+ * (no trap, no fault). */
+VES_API int ves_probe_wait_timeout(ves_ctx* ctx, void* stream);
 
 #ifdef __cplusplus
 }

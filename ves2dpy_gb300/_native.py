@@ -207,6 +207,7 @@ SIGNATURES = {
     "ves_ctx_stats": (_I, [_P, ctypes.POINTER(Stats), _I]),
     "ves_probe_sfu_peak": (_I, [ctypes.POINTER(ctypes.c_double), _P]),
     "ves_upsample_geometry": (_I, [_P, _I, _P, _P, _P, _P, _P, _P]),
+    "ves_probe_wait_timeout": (_I, [_P, _P]),
     "ves_stokes_dl_matrix": (_I, [_P, _I, _P, _P, _I, _P, _P, _SZ, _P]),
     "ves_stokes_dl_matrix_workspace": (_SZ, [_P, _I, _I]),
     "ves_dl_density": (_I, [_I, _I, _P, _P, _P, _P, _P]),

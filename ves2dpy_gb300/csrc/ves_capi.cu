@@ -3,6 +3,7 @@
 #include <string.h>
 
 #include "ves_internal.h"
+#include "ves_tc.cuh"
 
 static int finish(ves_ctx* c, cudaStream_t s, const char* what) {
   int rc = ves_launch_check(what);
@@ -265,4 +266,33 @@ extern "C" int ves_correct_area_length(ves_ctx* c, int nv, const double* X, cons
   VES_REQUIRE(c && X && area0 && length0 && Xout && ws && nv >= 0, "ves_correct_area_length: bad arguments");
   WsCarver w(ws, ws_bytes);
   return post_correct_area_length(c, nv, X, area0, length0, Xout, outer_iters, w, (cudaStream_t)stream);
+}
+
+// ---------------------------------------------------------------------------
+// Failure-path probe: one thread waits on an mbarrier that nothing completes,
+// with the bounded sleeping wait the tensor-core kernels use for MMA
+// completion.  The wait gives up, records VES_ERR_TIMEOUT in the context's
+// status word and the kernel returns, so the context stays usable.
+namespace {
+__global__ void wait_probe_kernel(VesDeviceStatus* st) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    tc_mbar_init(&bar, 1);
+    tc_mbar_fence_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) tc_mbar_wait_sleep(&bar, 0, st, 99);  // phase 0 never completes: nobody arrives
+  __syncthreads();
+}
+}  // namespace
+
+extern "C" int ves_probe_wait_timeout(ves_ctx* c, void* stream) {
+  VES_REQUIRE(c, "ves_probe_wait_timeout: bad arguments");
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = ves_reset_status(c, s);
+  if (rc) return rc;
+  ves_count_launch();
+  wait_probe_kernel<<<1, 32, 0, s>>>(c->status);
+  if ((rc = ves_launch_check("wait probe"))) return rc;
+  return ves_check_status(c, s, "wait probe");
 }

@@ -324,7 +324,7 @@ __device__ __forceinline__ Seg next_seg(long long lo, long long hi, int nv) {
 // KC1 / KCD: compile-time K chunk counts of the two conv pairs' outputs (0:
 // read them from the geometry); fixed counts let every epilogue and issue
 // loop unroll.  NG: warp groups per CTA, each running its own items (2: 256
-// TMEM columns each; 3: 128 columns each, when N1 + N2 <= 128 and three
+// TMEM columns each; 3 or 4: 128 columns each, when N1 + N2 <= 128 and the
 // groups' arrays fit in shared memory).
 template <int KC1, int KCD, int NG>
 __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
@@ -1007,13 +1007,14 @@ int tcnet_pack(const ves_net_block& b, int G, int L, const float* const* p, std:
   return VES_OK;
 }
 
-// Warp groups allowed in the down kernel (VES_TC_DOWN_GROUPS=2 forces two;
-// read once).
+// Warp groups allowed in the down kernel (VES_TC_DOWN_GROUPS=2 or 3 caps
+// them; read once).
 static int tcnet_down_groups_max() {
   static int v = -1;
   if (v < 0) {
     const char* e = getenv("VES_TC_DOWN_GROUPS");
-    v = (e && atoi(e) == 2) ? 2 : 3;
+    const int k = e ? atoi(e) : 4;
+    v = (k == 2 || k == 3) ? k : 4;
   }
   return v;
 }
@@ -1042,21 +1043,22 @@ int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_dow
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const int kc1 = g.kc1, kcd = g.kcd, Nd = kcd * 8;
   // warp groups per CTA: as many as TMEM (512 columns) and shared memory allow
-  const int down3 = g.dxs + 3 * g.dgrp + kTail, up1_4 = g.u1size + 4 * g.u1grp + kTail,
-            up2_3 = g.u2size + 3 * g.u2grp + kTail;
+  const int down3 = g.dxs + 3 * g.dgrp + kTail, down4 = g.dxs + 4 * g.dgrp + kTail,
+            up1_4 = g.u1size + 4 * g.u1grp + kTail, up2_3 = g.u2size + 3 * g.u2grp + kTail;
   const bool dn3 = (kc1 + kcd) * 8 <= 128 && down3 <= kMaxSmem && tcnet_down_groups_max() >= 3;
+  const bool dn4 = dn3 && down4 <= kMaxSmem && tcnet_down_groups_max() >= 4;
   const bool u14 = 2 * Nd <= 128 && up1_4 <= kMaxSmem;
   const bool u23 = 2 * Nd + (g.L / 128) * rup(g.cmix, 16) <= 160 && up2_3 <= kMaxSmem;
   // compiled chunk-count variants; others run the generic kernels
-  void (*dk)(KArgs) = dn3 ? down_kernel<0, 0, 3> : down_kernel<0, 0, 2>;
+  void (*dk)(KArgs) = dn4 ? down_kernel<0, 0, 4> : (dn3 ? down_kernel<0, 0, 3> : down_kernel<0, 0, 2>);
   void (*k1)(KArgs) = u14 ? up1_kernel<0, 4> : up1_kernel<0, 2>;
   void (*k2)(KArgs) = u23 ? up2_kernel<0, 3> : up2_kernel<0, 2>;
-#define VES_DK(A, B) dk = dn3 ? down_kernel<A, B, 3> : down_kernel<A, B, 2>
-  if (kc1 == 4 && kcd == 6) VES_DK(4, 6);
-  if (kc1 == 6 && kcd == 6) VES_DK(6, 6);
-  if (kc1 == 6 && kcd == 8) VES_DK(6, 8);
-  if (kc1 == 8 && kcd == 8) VES_DK(8, 8);
-#undef VES_DK
+#define VES_DK4(A, B) dk = dn4 ? down_kernel<A, B, 4> : (dn3 ? down_kernel<A, B, 3> : down_kernel<A, B, 2>)
+  if (kc1 == 4 && kcd == 6) VES_DK4(4, 6);
+  if (kc1 == 6 && kcd == 6) VES_DK4(6, 6);
+  if (kc1 == 6 && kcd == 8) VES_DK4(6, 8);
+  if (kc1 == 8 && kcd == 8) VES_DK4(8, 8);
+#undef VES_DK4
   if (kcd == 6) {
     k1 = u14 ? up1_kernel<6, 4> : up1_kernel<6, 2>;
     k2 = u23 ? up2_kernel<6, 3> : up2_kernel<6, 2>;
@@ -1065,7 +1067,7 @@ int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_dow
     k1 = u14 ? up1_kernel<8, 4> : up1_kernel<8, 2>;
     k2 = u23 ? up2_kernel<8, 3> : up2_kernel<8, 2>;
   }
-  const int ng_d = dn3 ? 3 : 2, ng_1 = u14 ? 4 : 2, ng_2 = u23 ? 3 : 2;
+  const int ng_d = dn4 ? 4 : (dn3 ? 3 : 2), ng_1 = u14 ? 4 : 2, ng_2 = u23 ? 3 : 2;
   // one CTA per SM (it allocates all 512 TMEM columns): at least 117 KB of
   // shared memory per CTA keeps a second one off the SM
   const int sm_d = std::max(g.dxs + ng_d * g.dgrp + kTail, kMinSmem);

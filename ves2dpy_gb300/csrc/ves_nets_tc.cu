@@ -62,9 +62,9 @@ struct Geo {
   // down image: W1 [11][kcin][n1][16B], W2 [11][kc1][d][16B], consts [6][128] f32
   int dw1, dw2, dcst, dsize;
   // down arrays of warp group 0 (group k at + k*dgrp): xs [2][kcin][L/2+6][16B],
-  // as [2][kc1][L/4+6][16B], stage [kcd][L/4][16B], xf [cin][L] f32 (the
+  // as [2][kc1][L/4+6][16B], xf [cin][L] f32 (the
   // block input as it arrives by bulk copy); a tail of 2 KB follows the groups
-  int dxs, das, dstage, dxf, dgrp;
+  int dxs, das, dxf, dgrp;
   // up1 image (transposed conv 1): W [2][5][kcd][d][16B] (output parity r, tap u),
   // consts [7][128] f32; arrays of warp group 0: bs [kcd][L/4+4][16B]
   int u1w, u1cst, u1size, u1bs, u1grp;
@@ -120,8 +120,6 @@ inline Geo make_geo(const ves_net_block& b, int L) {
   o += 2 * g.kcin * (L / 2 + 6) * 16;
   g.das = o;
   o += 2 * g.kc1 * (L / 4 + 6) * 16;
-  g.dstage = o;
-  o += g.kcd * (L / 4) * 16;
   g.dxf = o;
   o += rup(g.cin * L * 4, 16);
   g.dgrp = o - g.dxs;
@@ -184,11 +182,6 @@ __device__ __forceinline__ void group_sync_for_mma(int wg) {
   tc_fence_before_sync();
   group_sync(wg);
   tc_fence_after_sync();
-}
-__device__ __forceinline__ void copy16_g(unsigned char* dst, const unsigned char* src, int bytes, int t) {
-  const uint4* s = reinterpret_cast<const uint4*>(src);
-  uint4* d = reinterpret_cast<uint4*>(dst);
-  for (int i = t; i < bytes / 16; i += kGroupThreads) d[i] = s[i];
 }
 // Bounded wait of one warp group on an mbarrier; true when the phase
 // completed (the answer is uniform across the group).  Thread 0 of the group
@@ -364,7 +357,6 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
   const int P1 = L2 + 6, P2 = L4 + 6;
   uint4* xs = reinterpret_cast<uint4*>(sm + g.dxs + goff);
   uint4* as = reinterpret_cast<uint4*>(sm + g.das + goff);
-  uint4* stage = reinterpret_cast<uint4*>(sm + g.dstage + goff);
   float* xf = reinterpret_cast<float*>(sm + g.dxf + goff);
   const uint32_t xbytes = (uint32_t)(g.cin * L * 4);
   unsigned phase = 0, xphase = 0;
@@ -480,20 +472,20 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
       phase ^= 1;
       tc_fence_after_sync();
       if (32 * qd < L4) {
+        // the intermediate [kcd][L/4][16B] goes straight to global memory (coalesced 16-byte rows)
         const int p = 32 * qd + lane;
+        uint4* gmid = reinterpret_cast<uint4*>(a.mid + ((size_t)v * a.G + sg.grp) * g.mid_stride);
 #pragma unroll
         for (int k0 = 0; k0 < kcd; k0 += 4) {
           float vv[32];
           tc_ld32(d2 + ((uint32_t)(32 * qd) << 16) + 8 * k0, vv);
 #pragma unroll
           for (int k = 0; k < 4; ++k)
-            if (k0 + k < kcd) stage[(size_t)(k0 + k) * L4 + p] = act8(vv + 8 * k, cst, k0 + k, g.d, 384, 512, 640);
+            if (k0 + k < kcd) gmid[(size_t)(k0 + k) * L4 + p] = act8(vv + 8 * k, cst, k0 + k, g.d, 384, 512, 640);
         }
       }
       tc_fence_before_sync();
-      group_sync(wg);
-      copy16_g(a.mid + ((size_t)v * a.G + sg.grp) * g.mid_stride, reinterpret_cast<unsigned char*>(stage),
-               g.mid_bytes, gt);
+      group_sync(wg);  // every TMEM read done before the next item's MMAs
     }
     lo = sg.hi;
     failed = __syncthreads_or(failed ? 1 : 0) != 0;  // every thread takes part

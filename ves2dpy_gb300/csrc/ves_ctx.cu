@@ -295,12 +295,10 @@ extern "C" int ves_ctx_create(int N, ves_ctx** out) {
   }
   // host tables
   std::vector<double> d1N(N), d1Nup(Nup), pc(Nup), pcd(Nup), pcdd(Nup), qw(c->nquad), cq(14 * Nup),
-      ad(14 * Nup), Rm((size_t)N * Nup), Pm((size_t)Nup * N), lag(49), c6(6 * N), c6d(6 * N), cos6(6 * N),
+      ad(14 * Nup), Rm((size_t)N * Nup), Pm((size_t)Nup * N), lag(49), cos6(6 * N),
       sin6(6 * N), cosU(Nup), sinU(Nup);
   for (int r = 0; r < 6 * N; ++r) {
     const double t = 2.0 * VES_PI * r / (6 * N);
-    c6[r] = cardinal(N, t);
-    c6d[r] = cardinal_deriv(N, t);
     cos6[r] = cos(t);
     sin6[r] = sin(t);
   }
@@ -340,7 +338,7 @@ extern "C" int ves_ctx_create(int N, ves_ctx** out) {
 
   // one device buffer
   size_t nd = d1N.size() + d1Nup.size() + pc.size() + pcd.size() + pcdd.size() + qw.size() + cq.size() + ad.size() +
-              Rm.size() + Pm.size() + lag.size() + 4 * c6.size() + 2 * cosU.size();
+              Rm.size() + Pm.size() + lag.size() + 2 * cos6.size() + 2 * cosU.size();
   size_t nf = Rm.size() + Pm.size() + ad.size() + qw.size();
   size_t bytes = nd * sizeof(double) + nf * sizeof(float) + 1024;
   rc = ves_cuda_status(cudaMalloc(&c->d_buf, bytes), "cudaMalloc tables");
@@ -366,8 +364,6 @@ extern "C" int ves_ctx_create(int N, ves_ctx** out) {
   c->Rm = put(Rm);
   c->Pm = put(Pm);
   c->lag = put(lag);
-  c->c6 = put(c6);
-  c->c6d = put(c6d);
   c->cos6 = put(cos6);
   c->sin6 = put(sin6);
   c->cosU = put(cosU);

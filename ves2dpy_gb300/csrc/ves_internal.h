@@ -26,9 +26,7 @@ struct ves_ctx {
   double* Rm;      // [N][Nup] restriction
   double* Pm;      // [Nup][N] prolongation
   double* lag;     // [7][7]  Lagrange interpolation matrix (poten.py:977-990)
-  double* c6;      // [6N]  N->6N prolongation circulant (arc-length reparametrisation grid)
-  double* c6d;     // [6N]  its derivative
-  double* cos6;    // [6N]  cos(2 pi r / 6N)
+  double* cos6;    // [6N]  cos(2 pi r / 6N) (FFT twiddles of the arc-length reparametrisation grid)
   double* sin6;    // [6N]  sin(2 pi r / 6N)
   double* cosU;    // [Nup] cos(2 pi r / Nup)
   double* sinU;    // [Nup] sin(2 pi r / Nup)

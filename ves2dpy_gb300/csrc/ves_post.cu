@@ -111,8 +111,7 @@ __global__ void spread_kernel(int nchunk, int N, const double* __restrict__ part
 }
 
 // one redistributeArcLength pass; flags[k] = 1 if vesicle k was left as is
-__global__ void redistribute_kernel(int N, const double* __restrict__ d1, const double* __restrict__ c6,
-                                    const double* __restrict__ c6d, const double* __restrict__ cos6,
+__global__ void redistribute_kernel(int N, const double* __restrict__ d1, const double* __restrict__ cos6,
                                     const double* __restrict__ sin6, const double* __restrict__ spread_p,
                                     const double* __restrict__ X, double* __restrict__ Xout,
                                     int* __restrict__ flags) {
@@ -153,16 +152,43 @@ __global__ void redistribute_kernel(int N, const double* __restrict__ d1, const 
     return;
   }
   const double length = jsum * 2.0 * VES_PI / N;
-  // |dX/dt| of the interpolant on the 6N grid
+  // zh = fft(x + i y)/N, modes 0..N/2-1, -N/2..-1 (length-N FFT, twiddles
+  // from the 6N table); also the coefficients of the final evaluation
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    zr[j] = x[j];
+    zi[j] = y[j];
+  }
+  ves_fft(zr, zi, tre, tim, N, cos6, sin6, -1, 6);
+  for (int m = threadIdx.x; m < N; m += blockDim.x) {
+    zr[m] /= N;
+    zi[m] /= N;
+  }
+  __syncthreads();
+  // |dX/dt| of the interpolant on the 6N grid: the spectrum i k zh_k placed on
+  // the 6N grid and transformed back (the Nyquist mode split in two halves,
+  // +-N/2, so that its derivative is that of the real interpolant,
+  // -(N/2) c sin(N t / 2)); the same values as the circulant sum of the
+  // interpolant's derivative, with O(M log M) instead of O(M N) work
   for (int u = threadIdx.x; u < M; u += blockDim.x) {
-    double dx = 0, dy = 0;
-    int r = u;
-    for (int i = 0; i < N; ++i) {
-      dx = fma(c6d[r], x[i], dx);
-      dy = fma(c6d[r], y[i], dy);
-      r -= 6;
-      if (r < 0) r += M;
+    double cr = 0.0, ci = 0.0;
+    if (u < N / 2) {  // modes 0 .. N/2-1
+      cr = -u * zi[u];
+      ci = u * zr[u];
+    } else if (u > M - N / 2) {  // modes -(N/2-1) .. -1
+      const int k = u - M;
+      cr = -k * zi[N + k];
+      ci = k * zr[N + k];
+    } else if (u == N / 2 || u == M - N / 2) {  // the two halves of the Nyquist mode
+      const double h = (u == N / 2 ? 0.25 : -0.25) * N;  // (+-N/2) * 1/2
+      cr = -h * zi[N / 2];
+      ci = h * zr[N / 2];
     }
+    are[u] = cr;
+    aim[u] = ci;
+  }
+  ves_fft(are, aim, tre, tim, M, cos6, sin6, +1);
+  for (int u = threadIdx.x; u < M; u += blockDim.x) {
+    const double dx = are[u], dy = aim[u];
     are[u] = sqrt(dx * dx + dy * dy);
     aim[u] = 0.0;
   }
@@ -200,16 +226,6 @@ __global__ void redistribute_kernel(int N, const double* __restrict__ d1, const 
     }
     const int idx = (lo == 0) ? 0 : lo - 1;  // torch gathers idx-1 (wraps to -1 only if target <= al[0])
     th[i] = 2.0 * VES_PI * idx / M + (target - al[idx]) * (2.0 * VES_PI);
-  }
-  // fft(z)/N with the modes 0..N/2-1, -N/2..-1 (length-N FFT, twiddles from the 6N table)
-  for (int j = threadIdx.x; j < N; j += blockDim.x) {
-    zr[j] = x[j];
-    zi[j] = y[j];
-  }
-  ves_fft(zr, zi, tre, tim, N, cos6, sin6, -1, 6);
-  for (int m = threadIdx.x; m < N; m += blockDim.x) {
-    zr[m] /= N;
-    zi[m] /= N;
   }
   __syncthreads();
   // z(theta_i) = sum_m zh_m e^{i m theta_i}; powers of e^{i theta} by recurrence
@@ -511,7 +527,7 @@ int post_redistribute(ves_ctx* c, int nv, const double* X, double* Xout, int* fl
     if (rc) return rc;
   }
   ves_count_launch();
-  redistribute_kernel<<<nv, threads, sh, s>>>(N, c->d1N, c->c6, c->c6d, c->cos6, c->sin6, spread, X, Xout, flags);
+  redistribute_kernel<<<nv, threads, sh, s>>>(N, c->d1N, c->cos6, c->sin6, spread, X, Xout, flags);
   return ves_launch_check("redistribute");
 }
 

@@ -65,9 +65,11 @@ struct Geo {
   // as [2][kc1][L/4+6][16B], xf [cin][L] f32 (the
   // block input as it arrives by bulk copy); a tail of 2 KB follows the groups
   int dxs, das, dxf, dgrp;
-  // up1 image (transposed conv 1): W [2][5][kcd][d][16B] (output parity r, tap u),
+  // up1 image (transposed conv 1): W (u1merge = 0: [2][5][kcd][d][16B], output
+  // parity r, tap u, the parities M-split over the lanes; u1merge = 1: the
+  // merged layout of up2, both parities in one operand of N = 2*kcd*8),
   // consts [7][128] f32; arrays of warp group 0: bs [kcd][L/4+4][16B]
-  int u1w, u1cst, u1size, u1bs, u1grp;
+  int u1merge, u1w, u1cst, u1size, u1bs, u1grp;
   // up2 image (transposed conv 2 and mix): W (u2merge = 1: [5][kcd][2*kcd*8][16B],
   // both output parities in one operand of N = 2*kcd*8 rows, parity r at row
   // r*kcd*8; u2merge = 0: as up1), M [3][kcd][cmix][16B], consts [7][128] f32;
@@ -90,6 +92,19 @@ __host__ __device__ inline int dec_w_off(const Geo& g, int base, int r, int u, i
 // same in the merged layout [5][kcd][2*kcd*8][16B]
 __host__ __device__ inline int dec_w_off_merged(const Geo& g, int base, int r, int u, int kc, int o) {
   return base + ((u * g.kcd + kc) * 2 * g.kcd * 8 + r * g.kcd * 8 + o) * 16;
+}
+
+// transposed conv 1 with both output parities in one MMA (VES_TC_UP1_MERGE=0/1
+// overrides the default; read once)
+inline int tcnet_up1_merge(int L) {
+  static int v = -2;
+  if (v == -2) {
+    const char* e = getenv("VES_TC_UP1_MERGE");
+    v = e ? (atoi(e) ? 1 : 0) : -1;
+  }
+  if (v >= 0) return v;
+  (void)L;
+  return 1;  // measured 1-2% faster networks than the M-split at L = 128 and 256
 }
 
 inline Geo make_geo(const ves_net_block& b, int L) {
@@ -124,9 +139,11 @@ inline Geo make_geo(const ves_net_block& b, int L) {
   o += rup(g.cin * L * 4, 16);
   g.dgrp = o - g.dxs;
   const int dec_unmerged = 10 * g.kcd * g.d * 16;
-  // up1: always M-split (2 * L/4 <= 128), so the smaller unmerged layout
+  // up1: both parities in one MMA of N = 2*Nd (u1merge, fewer and larger MMAs,
+  // half the lanes busy) or M-split over the lanes (unmerged layout)
+  g.u1merge = tcnet_up1_merge(L);
   g.u1w = 0;
-  g.u1cst = dec_unmerged;
+  g.u1cst = g.u1merge ? 5 * g.kcd * 2 * g.kcd * 8 * 16 : dec_unmerged;
   g.u1size = g.u1cst + 7 * 128 * 4;
   g.u1bs = g.u1size;
   g.u1grp = g.kcd * (L / 4 + 4) * 16;
@@ -519,8 +536,8 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
 template <int KCD>
 __device__ __forceinline__ void deconv_issue(uint32_t dt, uint32_t sbase, uint32_t a_off, uint32_t lboA, int npos,
                                              int Nd, int kcd, bool merged, uint32_t w0, uint32_t w1, uint32_t bTap,
-                                             uint32_t lboB) {
-  const bool msplit = 2 * npos <= 128;
+                                             uint32_t lboB, bool allow_split = true) {
+  const bool msplit = allow_split && 2 * npos <= 128;
   const uint32_t stepA = (2 * lboA) >> 4;
   if (merged && !msplit) {
     const uint32_t idesc = tc_idesc_bf16(128, 2 * Nd);
@@ -546,8 +563,8 @@ __device__ __forceinline__ void deconv_issue(uint32_t dt, uint32_t sbase, uint32
 template <int KCD>
 __device__ __forceinline__ void deconv_epilogue(uint32_t dt, int qd, int lane, int npos, int Nd, int kcd, int nreal,
                                                 const float* cst, int ob, int os, int ot, uint4* dst, int pitch,
-                                                int row0) {
-  const bool msplit = 2 * npos <= 128;
+                                                int row0, bool allow_split = true) {
+  const bool msplit = allow_split && 2 * npos <= 128;
   const int lane0 = 32 * qd;
 #pragma unroll
   for (int r = 0; r < 2; ++r) {
@@ -608,8 +625,9 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) up1_kernel(KArgs a) {
   const int PB = L4 + 4;
   const int Nd = kcd * 8;
   uint4* bs = reinterpret_cast<uint4*>(sm + g.u1bs + wg * g.u1grp);
-  const uint32_t bTap = (uint32_t)(kcd * g.d * 16) >> 4;
-  const uint32_t w1 = (uint32_t)(g.u1w + 5 * kcd * g.d * 16);
+  const uint32_t bTap = (uint32_t)((g.u1merge ? 2 * Nd : g.d) * kcd * 16) >> 4;
+  const uint32_t lboB1 = (uint32_t)((g.u1merge ? 2 * Nd : g.d) * 16);
+  const uint32_t w1 = g.u1merge ? (uint32_t)(g.u1w + Nd * 16) : (uint32_t)(g.u1w + 5 * kcd * g.d * 16);
   unsigned phase = 0, mphase = 0;
   bool mpend = false;  // a bulk copy into bs is in flight
   // intermediate [kcd][L/4][16B] of an item -> bs rows 2 .. L/4+1 of each chunk
@@ -641,8 +659,8 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) up1_kernel(KArgs a) {
       mpend = false;
       tc_fence_after_sync();
       if (gt == 0) {
-        deconv_issue<KCD>(dt, sbase, g.u1bs + wg * g.u1grp, PB * 16, L4, Nd, kcd, false, g.u1w, w1, bTap,
-                          g.d * 16);
+        deconv_issue<KCD>(dt, sbase, g.u1bs + wg * g.u1grp, PB * 16, L4, Nd, kcd, g.u1merge != 0, g.u1w, w1, bTap,
+                          lboB1, g.u1merge == 0);
         tc_commit(&bar[wg]);
       }
       if (!group_wait_one(&bar[wg], phase, a.st, 23, wg, gt, &fail[wg])) {
@@ -654,7 +672,7 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) up1_kernel(KArgs a) {
       // bs is free once the MMAs have completed: this group's next item
       if (it + NG < sg.hi) fetch_mid(it + NG);
       uint4* dst = reinterpret_cast<uint4*>(a.mid + ((size_t)v * a.G + sg.grp) * g.mid_stride + g.mid_bytes);
-      deconv_epilogue<KCD>(dt, qd, lane, L4, Nd, kcd, g.d, cst, 0, 128, 256, dst, L2, 0);
+      deconv_epilogue<KCD>(dt, qd, lane, L4, Nd, kcd, g.d, cst, 0, 128, 256, dst, L2, 0, g.u1merge == 0);
       tc_fence_before_sync();
       group_sync(wg);  // every TMEM read done before the next item's MMAs
     }
@@ -970,7 +988,8 @@ int tcnet_pack(const ves_net_block& b, int G, int L, const float* const* p, std:
                 v8[e] = c < d ? W[((size_t)(grp * d + c) * d + o) * 10 + r + 2 * u] : 0.f;
               }
               if (layer == 0)
-                put_row(U1, dec_w_off(g, g.u1w, r, u, kc, o), v8);
+                put_row(U1, g.u1merge ? dec_w_off_merged(g, g.u1w, r, u, kc, o) : dec_w_off(g, g.u1w, r, u, kc, o),
+                        v8);
               else if (g.u2merge)
                 put_row(U2, dec_w_off_merged(g, g.u2w, r, u, kc, o), v8);
               else

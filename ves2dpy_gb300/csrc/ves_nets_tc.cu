@@ -170,6 +170,7 @@ inline Geo make_geo(const ves_net_block& b, int L) {
 struct KArgs {
   Geo g;
   int G, nv;
+  int m64;                   // layers of at most 64 positions use M = 64 MMAs
   long long items;
   const unsigned char* img;  // group 0 image of this block; group stride = image size
   const float* x;            // block input [nv][G*cin][L]
@@ -317,6 +318,26 @@ __device__ __forceinline__ uint4 act8(const float* v, const float* cst, int kc, 
   return make_uint4(pack_bf2(y[0], y[1]), pack_bf2(y[2], y[3]), pack_bf2(y[4], y[5]), pack_bf2(y[6], y[7]));
 }
 
+// Rows of an accumulator of M rows in TMEM: M = 128 puts row r on lane r;
+// M = 64 (half the A tile per MMA, for layers of at most 64 positions) puts
+// rows 16 q .. 16 q + 15 on lanes 32 q .. 32 q + 15 (measured on a GB300).
+// The row this thread's lane holds, or -1.
+__device__ __forceinline__ int acc_row(int M, int qd, int lane) {
+  return M == 128 ? 32 * qd + lane : (lane < 16 ? 16 * qd + lane : -1);
+}
+// first row held by warp quarter qd (uniform across the warp)
+__device__ __forceinline__ int acc_row0(int M, int qd) { return M == 128 ? 32 * qd : 16 * qd; }
+
+// accumulators of at most 64 rows use M = 64 MMAs (VES_TC_M64=0 turns this off; read once)
+inline bool tcnet_m64() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = getenv("VES_TC_M64");
+    v = (e && atoi(e) == 0) ? 0 : 1;
+  }
+  return v != 0;
+}
+
 // ---------------------------------------------------------------------------
 // Segments: the CTA's contiguous item range split where the channel group
 // changes; the weight image is reloaded (whole CTA) at each segment start and
@@ -437,8 +458,9 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
       group_sync_for_mma(wg);  // xs complete; xf fully read
       if (it + NG < sg.hi) fetch_x(it + NG);
       // conv pair 1: D1[p][o], p < L/2 on the lanes, o < n1 in the columns
+      const int M1 = (a.m64 && L2 <= 64) ? 64 : 128, M2 = (a.m64 && L4 <= 64) ? 64 : 128;
       if (gt == 0) {
-        const uint32_t idesc = tc_idesc_bf16(128, N1);
+        const uint32_t idesc = tc_idesc_bf16(M1, N1);
         const uint32_t lboA = P1 * 16, lboB = g.n1 * 16;
         const uint64_t a0 = tc_desc(sbase + g.dxs + goff, lboA, 128), b0 = tc_desc(sbase + g.dw1, lboB, 128);
 #define VES_CONV1(NK) issue_conv<NK>(d1, a0, b0, (g.kcin * lboA) >> 4, (g.kcin * lboB) >> 4, (2 * lboA) >> 4, (2 * lboB) >> 4, idesc)
@@ -452,29 +474,32 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
       }
       phase ^= 1;
       tc_fence_after_sync();
-      if (32 * qd < L2) {
-        const int p = 32 * qd + lane;
+      if (acc_row0(M1, qd) < L2) {  // uniform per warp: the TMEM loads are warp-wide
+        const int p = acc_row(M1, qd, lane);
+        const bool own = p >= 0 && p < L2;
         const int par = p & 1, q = p >> 1;
 #pragma unroll
         for (int k0 = 0; k0 < kc1; k0 += 4) {
           float vv[32];
           tc_ld32(d1 + ((uint32_t)(32 * qd) << 16) + 8 * k0, vv);
+          if (own) {
 #pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            const int kc = k0 + k;
-            if (kc >= kc1) break;
-            const uint4 val = act8(vv + 8 * k, cst, kc, g.n1, 0, 128, 256);
-            uint4* base = as + (size_t)(par * kc1 + kc) * P2;
-            base[q + 3] = val;
-            if (q >= L4 - 3) base[q + 3 - L4] = val;
-            if (q < 3) base[q + 3 + L4] = val;
+            for (int k = 0; k < 4; ++k) {
+              const int kc = k0 + k;
+              if (kc >= kc1) break;
+              const uint4 val = act8(vv + 8 * k, cst, kc, g.n1, 0, 128, 256);
+              uint4* base = as + (size_t)(par * kc1 + kc) * P2;
+              base[q + 3] = val;
+              if (q >= L4 - 3) base[q + 3 - L4] = val;
+              if (q < 3) base[q + 3 + L4] = val;
+            }
           }
         }
       }
       group_sync_for_mma(wg);
       // conv pair 2: D2[p][o], p < L/4, o < d
       if (gt == 0) {
-        const uint32_t idesc = tc_idesc_bf16(128, N2);
+        const uint32_t idesc = tc_idesc_bf16(M2, N2);
         const uint32_t lboA = P2 * 16, lboB = g.d * 16;
         const uint64_t a0 = tc_desc(sbase + g.das + goff, lboA, 128), b0 = tc_desc(sbase + g.dw2, lboB, 128);
 #define VES_CONV2(NK) issue_conv<NK>(d2, a0, b0, (kc1 * lboA) >> 4, (kc1 * lboB) >> 4, (2 * lboA) >> 4, (2 * lboB) >> 4, idesc)
@@ -488,17 +513,20 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
       }
       phase ^= 1;
       tc_fence_after_sync();
-      if (32 * qd < L4) {
+      if (acc_row0(M2, qd) < L4) {
         // the intermediate [kcd][L/4][16B] goes straight to global memory (coalesced 16-byte rows)
-        const int p = 32 * qd + lane;
+        const int p = acc_row(M2, qd, lane);
+        const bool own = p >= 0 && p < L4;
         uint4* gmid = reinterpret_cast<uint4*>(a.mid + ((size_t)v * a.G + sg.grp) * g.mid_stride);
 #pragma unroll
         for (int k0 = 0; k0 < kcd; k0 += 4) {
           float vv[32];
           tc_ld32(d2 + ((uint32_t)(32 * qd) << 16) + 8 * k0, vv);
+          if (own) {
 #pragma unroll
-          for (int k = 0; k < 4; ++k)
-            if (k0 + k < kcd) gmid[(size_t)(k0 + k) * L4 + p] = act8(vv + 8 * k, cst, k0 + k, g.d, 384, 512, 640);
+            for (int k = 0; k < 4; ++k)
+              if (k0 + k < kcd) gmid[(size_t)(k0 + k) * L4 + p] = act8(vv + 8 * k, cst, k0 + k, g.d, 384, 512, 640);
+          }
         }
       }
       tc_fence_before_sync();
@@ -536,11 +564,11 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
 template <int KCD>
 __device__ __forceinline__ void deconv_issue(uint32_t dt, uint32_t sbase, uint32_t a_off, uint32_t lboA, int npos,
                                              int Nd, int kcd, bool merged, uint32_t w0, uint32_t w1, uint32_t bTap,
-                                             uint32_t lboB, bool allow_split = true) {
+                                             uint32_t lboB, bool allow_split = true, int Mrows = 128) {
   const bool msplit = allow_split && 2 * npos <= 128;
   const uint32_t stepA = (2 * lboA) >> 4;
   if (merged && !msplit) {
-    const uint32_t idesc = tc_idesc_bf16(128, 2 * Nd);
+    const uint32_t idesc = tc_idesc_bf16(Mrows, 2 * Nd);
     const uint64_t a0 = tc_desc(sbase + a_off, lboA, 128), b0 = tc_desc(sbase + w0, lboB, 128);
 #define VES_DEC(NK) issue_deconv<NK>(dt, a0, b0, bTap, stepA, (2 * lboB) >> 4, idesc)
     VES_TC_NK_SWITCH(kcd / 2, VES_DEC)
@@ -563,27 +591,32 @@ __device__ __forceinline__ void deconv_issue(uint32_t dt, uint32_t sbase, uint32
 template <int KCD>
 __device__ __forceinline__ void deconv_epilogue(uint32_t dt, int qd, int lane, int npos, int Nd, int kcd, int nreal,
                                                 const float* cst, int ob, int os, int ot, uint4* dst, int pitch,
-                                                int row0, bool allow_split = true) {
+                                                int row0, bool allow_split = true, int Mrows = 128) {
   const bool msplit = allow_split && 2 * npos <= 128;
   const int lane0 = 32 * qd;
 #pragma unroll
   for (int r = 0; r < 2; ++r) {
     int q;
+    bool own = true;
     if (msplit) {
       if (lane0 < r * npos || lane0 >= (r + 1) * npos) continue;  // uniform per warp
       q = lane0 + lane - r * npos;
     } else {
-      if (lane0 >= npos) continue;
-      q = lane0 + lane;
+      if (acc_row0(Mrows, qd) >= npos) continue;  // uniform per warp
+      q = acc_row(Mrows, qd, lane);
+      own = q >= 0 && q < npos;
     }
 #pragma unroll
     for (int k0 = 0; k0 < (KCD ? KCD : 8); k0 += 4) {
       if (k0 >= kcd) break;
       float vv[32];
       tc_ld32(dt + ((uint32_t)lane0 << 16) + r * Nd + 8 * k0, vv);
+      if (own) {
 #pragma unroll
-      for (int k = 0; k < 4; ++k)
-        if (k0 + k < kcd) dst[(size_t)(k0 + k) * pitch + 2 * q + r + row0] = act8(vv + 8 * k, cst, k0 + k, nreal, ob, os, ot);
+        for (int k = 0; k < 4; ++k)
+          if (k0 + k < kcd)
+            dst[(size_t)(k0 + k) * pitch + 2 * q + r + row0] = act8(vv + 8 * k, cst, k0 + k, nreal, ob, os, ot);
+      }
     }
   }
 }
@@ -627,6 +660,7 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) up1_kernel(KArgs a) {
   uint4* bs = reinterpret_cast<uint4*>(sm + g.u1bs + wg * g.u1grp);
   const uint32_t bTap = (uint32_t)((g.u1merge ? 2 * Nd : g.d) * kcd * 16) >> 4;
   const uint32_t lboB1 = (uint32_t)((g.u1merge ? 2 * Nd : g.d) * 16);
+  const int M1 = (a.m64 && g.u1merge && L4 <= 64) ? 64 : 128;  // rows of the merged MMA
   const uint32_t w1 = g.u1merge ? (uint32_t)(g.u1w + Nd * 16) : (uint32_t)(g.u1w + 5 * kcd * g.d * 16);
   unsigned phase = 0, mphase = 0;
   bool mpend = false;  // a bulk copy into bs is in flight
@@ -660,7 +694,7 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) up1_kernel(KArgs a) {
       tc_fence_after_sync();
       if (gt == 0) {
         deconv_issue<KCD>(dt, sbase, g.u1bs + wg * g.u1grp, PB * 16, L4, Nd, kcd, g.u1merge != 0, g.u1w, w1, bTap,
-                          lboB1, g.u1merge == 0);
+                          lboB1, g.u1merge == 0, M1);
         tc_commit(&bar[wg]);
       }
       if (!group_wait_one(&bar[wg], phase, a.st, 23, wg, gt, &fail[wg])) {
@@ -672,7 +706,7 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) up1_kernel(KArgs a) {
       // bs is free once the MMAs have completed: this group's next item
       if (it + NG < sg.hi) fetch_mid(it + NG);
       uint4* dst = reinterpret_cast<uint4*>(a.mid + ((size_t)v * a.G + sg.grp) * g.mid_stride + g.mid_bytes);
-      deconv_epilogue<KCD>(dt, qd, lane, L4, Nd, kcd, g.d, cst, 0, 128, 256, dst, L2, 0, g.u1merge == 0);
+      deconv_epilogue<KCD>(dt, qd, lane, L4, Nd, kcd, g.d, cst, 0, 128, 256, dst, L2, 0, g.u1merge == 0, M1);
       tc_fence_before_sync();
       group_sync(wg);  // every TMEM read done before the next item's MMAs
     }
@@ -1044,6 +1078,7 @@ int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_dow
   const Geo& g = a.g;
   a.G = G;
   a.nv = nv;
+  a.m64 = tcnet_m64() ? 1 : 0;
   a.items = (long long)G * nv;
   a.x = x;
   a.out = out;

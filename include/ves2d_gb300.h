@@ -280,6 +280,23 @@ VES_API int ves_biem_step(ves_ctx* ctx, const ves_step_params* prm, int nv, cons
                   const double* sigma, double* Xout, double* sigma_out, ves_step_result* res,
                   void* ws, size_t ws_bytes, void* stream);
 VES_API size_t ves_biem_step_workspace(ves_ctx* ctx, const ves_step_params* prm, int nv);
+/* One implicit step of a suspension of several point counts: ngroups (1-4)
+ * groups, group g with nv[g] >= 1 vesicles of ctx[g]->N points, X[g] and
+ * sigma[g] in the layout of ves_biem_step.  Every vesicle of every group is
+ * in one GMRES system (group blocks in order).  Between groups the far field
+ * runs over the source group's upsampled points and the near zone and its
+ * correction follow matlab getZone / nearSingInt with a separate target set
+ * (matlab/capsules_py.m:194-467, matlab/poten_py.m:495-692), h = the source
+ * group's min length / N.  prm->near_scheme VES_NEAR_MATLAB or VES_NEAR_NONE;
+ * no viscosity contrast or repulsion (VES_ERR_ARG).  The reference holds one
+ * N per suspension (X[2N, nv]); with one group this is ves_biem_step with
+ * the MATLAB near rules. */
+VES_API int ves_biem_step_mixed(int ngroups, ves_ctx* const* ctx, const ves_step_params* prm, const int* nv,
+                                const double* const* X, const double* const* sigma, double* const* Xout,
+                                double* const* sigma_out, ves_step_result* res, void* ws, size_t ws_bytes,
+                                void* stream);
+VES_API size_t ves_biem_step_mixed_workspace(int ngroups, ves_ctx* const* ctx, const ves_step_params* prm,
+                                             const int* nv);
 
 /* ---- post-step shape conditioning (curve_batch_compile.py) ---------------- */
 /* One redistributeArcLength pass (curve_batch_compile.py:905-972, with

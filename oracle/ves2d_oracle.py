@@ -985,6 +985,164 @@ def time_step(X, sigma, prm: StepParams, tab: PotenTables | None = None) -> Step
 
 
 # --------------------------------------------------------------------------
+# Suspensions of several point counts (groups of vesicles with N_g points).
+# The reference layout X[2N, nv] holds one N; a mixed suspension is a list of
+# such arrays.  Between groups the MATLAB near-zone and near-singular rules
+# apply with a separate target set (getZone's NearOther, capsules_py.m:194-467
+# with vesicle2 as targets; nearSingInt with tEqualS false,
+# poten_py.m:495-692): h is the source set's min length / N_source.
+# --------------------------------------------------------------------------
+
+
+def get_zone_cross(Xs, Xt, h, interp=LAGRANGE_INTERP):
+    """Near entries of the target points of Xt (N_t points per vesicle) w.r.t.
+    the source vesicles of Xs (N_s points): k1 indexes Xs, k2 and j Xt."""
+    Ns, nvs = Xs.shape[0] // 2, Xs.shape[1]
+    Nt, nvt = Xt.shape[0] // 2, Xt.shape[1]
+    entries = []
+    for k in range(nvs):
+        for k2 in range(nvt):
+            for ipt in range(Nt):
+                d2 = (Xt[ipt, k2] - Xs[:Ns, k]) ** 2 + (Xt[ipt + Nt, k2] - Xs[Ns:, k]) ** 2
+                loc = int(np.argmin(d2))
+                if math.sqrt(d2[loc]) < 2 * h:
+                    dist, nx, ny, th = closest_point(Xs, k, Xt[ipt, k2], Xt[ipt + Nt, k2], loc, interp)
+                    if dist < h:
+                        entries.append(NearEntry(k, k2, ipt, loc, dist, nx, ny, th))
+    return entries
+
+
+def near_sing_int_matlab_cross(Xs, f, vself, Xt, entries, h, tab: PotenTables):
+    """Layer potential of every source vesicle of Xs at the points of Xt, the
+    near entries replaced by the Lagrange extrapolation (nearSingInt with
+    tEqualS false)."""
+    Ns = Xs.shape[0] // 2
+    Nt, nvt = Xt.shape[0] // 2, Xt.shape[1]
+    Nup = tab.Nup
+    Xup = interpft_vec(Xs, Nup)
+    fup = interpft_vec(f, Nup)
+    sa_up, _, _ = diff_prop(Xup)
+    out = np.zeros((2 * Nt, nvt))
+    K1 = np.arange(Xs.shape[1])
+    for k2 in range(nvt):
+        out[:, k2] = exact_stokes_sl_points(Xup, sa_up, fup, Xt[:, k2:k2 + 1], K1)[:, 0]
+    interp = tab.interp
+    order = interp.shape[0]
+    p = (order + 2) // 2
+    beta = 1.1
+    for e in entries:
+        pn = np.mod(np.arange(e.icp - p + 1, e.icp - p + 1 + order), Ns)
+        velx = lagrange_eval(interp @ vself[pn, e.k1], e.theta)
+        vely = lagrange_eval(interp @ vself[pn + Ns, e.k1], e.theta)
+        tx, ty = Xt[e.j, e.k2], Xt[e.j + Nt, e.k2]
+        pot = exact_stokes_sl_points(Xup, sa_up, fup, np.array([[tx], [ty]]), [e.k1])
+        out[e.j, e.k2] -= pot[0, 0]
+        out[e.j + Nt, e.k2] -= pot[1, 0]
+        nx = (tx - e.nx) / e.dist
+        ny = (ty - e.ny) / e.dist
+        sl = beta * h * np.arange(1, order)
+        XL = np.concatenate([e.nx + sl * nx, e.ny + sl * ny])[:, None]
+        lag = exact_stokes_sl_points(Xup, sa_up, fup, XL, [e.k1]).reshape(-1)
+        Px = interp @ np.concatenate([[velx], lag[:order - 1]])
+        Py = interp @ np.concatenate([[vely], lag[order - 1:]])
+        ds = e.dist / (beta * h * (order - 1))
+        out[e.j, e.k2] += lagrange_eval(Px, ds)
+        out[e.j + Nt, e.k2] += lagrange_eval(Py, ds)
+    return out
+
+
+def time_step_mixed(Xs, sigmas, prm: StepParams):
+    """One implicit BIEM step of a suspension given as groups (tstep_biem.py:181-428
+    with every vesicle of every group in one GMRES system, group after group;
+    near interactions by the MATLAB rules, ``prm.near`` 'matlab' or 'none')."""
+    if prm.near not in ('matlab', 'none'):
+        raise ValueError("time_step_mixed: near must be 'matlab' or 'none'")
+    ng = len(Xs)
+    Ns = [X.shape[0] // 2 for X in Xs]
+    nvs = [X.shape[1] for X in Xs]
+    tabs = [PotenTables(N) for N in Ns]
+    vess = [Capsule(X, prm.kappa) for X in Xs]
+    Gs = [stokes_sl_matrix(X, t) for X, t in zip(Xs, tabs)]
+    hs = [v.length / N for v, N in zip(vess, Ns)]
+    zones = {}
+    if prm.near == 'matlab':
+        for g in range(ng):
+            for q in range(ng):
+                zones[g, q] = get_zone(Xs[g], hs[g])[0] if g == q else get_zone_cross(Xs[q], Xs[g], hs[q])
+    offs = np.cumsum([0] + [3 * N * nv for N, nv in zip(Ns, nvs)])
+    rhs, x0, lus = [], [], []
+    for g in range(ng):
+        X, N, nv = Xs[g], Ns[g], nvs[g]
+        r1 = X + prm.dt * bg_flow(X, prm.far_field, prm.speed, prm.chan_width, prm.vortex_size)
+        r2 = vess[g].surface_div(X)
+        rhs.append(np.concatenate([r1, r2], axis=0).T.reshape(-1))
+        x0.append(np.concatenate([X, sigmas[g]], axis=0).T.reshape(-1))
+        if prm.use_preco:
+            Ben, Ten, Div = vess[g].compute_derivs()
+            lu = []
+            for k in range(nv):
+                M = np.zeros((3 * N, 3 * N))
+                M[:2 * N, :2 * N] = np.eye(2 * N) + prm.dt * prm.kappa * (Gs[g][:, :, k] @ Ben[:, :, k])
+                M[:2 * N, 2 * N:] = -prm.dt * (Gs[g][:, :, k] @ Ten[:, :, k])
+                M[2 * N:, :2 * N] = Div[:, :, k]
+                lu.append(sla.lu_factor(M))
+            lus.append(lu)
+    counter = {'n': 0}
+
+    def matvec(v):
+        counter['n'] += 1
+        v = np.asarray(v, dtype=np.float64)
+        Xm, fs, Gfs = [], [], []
+        for g in range(ng):
+            N, nv = Ns[g], nvs[g]
+            vr = v[offs[g]:offs[g + 1]].reshape(nv, 3, N)
+            Xm.append(vr[:, :2, :].reshape(nv, 2 * N).T)
+            f = vess[g].trac_jump(Xm[g], vr[:, 2, :].T)
+            fs.append(f)
+            Gfs.append(exact_stokes_sl_diag(Gs[g], f))
+        out = []
+        for g in range(ng):
+            N, nv = Ns[g], nvs[g]
+            Fslp = np.zeros((2 * N, nv))
+            for q in range(ng):
+                if q == g:
+                    if nv > 1:
+                        Fslp += near_sing_int_matlab(Xs[g], fs[g], Gfs[g], zones.get((g, g), []), hs[g], tabs[g])
+                else:
+                    Fslp += near_sing_int_matlab_cross(Xs[q], fs[q], Gfs[q], Xs[g], zones.get((g, q), []), hs[q],
+                                                       tabs[q])
+            valPos = Xm[g] - prm.dt * Gfs[g] - prm.dt * Fslp
+            valTen = vess[g].surface_div(Xm[g])
+            out.append(np.concatenate([valPos.reshape(2, N, nv), valTen.reshape(1, N, nv)], axis=0)
+                       .reshape(3 * N, nv).T.reshape(-1))
+        return np.concatenate(out)
+
+    def psolve(z):
+        z = np.asarray(z, dtype=np.float64)
+        parts = []
+        for g in range(ng):
+            zr = z[offs[g]:offs[g + 1]].reshape(nvs[g], 3 * Ns[g])
+            parts.append(np.concatenate([sla.lu_solve(lus[g][k], zr[k]) for k in range(nvs[g])]))
+        return np.concatenate(parts)
+
+    n = int(offs[-1])
+    A = spla.LinearOperator((n, n), matvec=matvec)
+    b = np.concatenate(rhs)
+    if prm.use_preco:
+        Mop = spla.LinearOperator((n, n), matvec=psolve)
+        xs, info = spla.gmres(A, b, rtol=prm.gmres_tol, maxiter=prm.gmres_maxiter, M=Mop, x0=np.concatenate(x0))
+    else:
+        xs, info = spla.gmres(A, b, rtol=prm.gmres_tol, maxiter=prm.gmres_maxiter, x0=np.concatenate(x0))
+    Xo, so = [], []
+    for g in range(ng):
+        N, nv = Ns[g], nvs[g]
+        xr = xs[offs[g]:offs[g + 1]].reshape(nv, 3, N)
+        Xo.append(xr[:, :2, :].reshape(nv, 2 * N).T.copy())
+        so.append(xr[:, 2, :].T.copy())
+    return Xo, so, counter['n'], int(info)
+
+
+# --------------------------------------------------------------------------
 # Synthetic suspensions (seeded generators for the benchmark configurations)
 # --------------------------------------------------------------------------
 

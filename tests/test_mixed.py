@@ -1,0 +1,64 @@
+"""Suspensions of several point counts, CPU side.
+
+The oracle's multi-group step (every vesicle of every group in one GMRES
+system, MATLAB near rules between groups with the source group's h) must
+reduce to the single-N step when the groups share N: the same suspension
+split into two groups gives the same step.  For equal near-zone widths both
+groups hold a vesicle of the minimum length (a far copy of the shortest one).
+"""
+import numpy as np
+
+from oracle import ves2d_oracle as O
+
+
+def small_suspension(N=16, nv=5, seed=1):
+    from ves2dpy_gb300.suspension import vesicle_shape
+    rng = np.random.default_rng(seed)
+    X = np.zeros((2 * N, nv))
+    for k in range(nv):
+        x, y = vesicle_shape(N, rng, 0.8, area=0.06)
+        X[:N, k] = x + (k % 3) * 0.32
+        X[N:, k] = y + (k // 3) * 0.30
+    return X
+
+
+def split_with_shortest(X, cut):
+    """Groups X[:, :cut] and X[:, cut:], the group without the shortest
+    vesicle extended by a copy of it moved far away."""
+    N = X.shape[0] // 2
+    k = int(np.argmin(O.geom_prop(X)[2]))
+    far = X[:, k:k + 1].copy()
+    far[:N] += 40.0
+    A, B = X[:, :cut], X[:, cut:]
+    if k < cut:
+        B = np.concatenate([B, far], axis=1)
+    else:
+        A = np.concatenate([A, far], axis=1)
+    return A, B
+
+
+def test_mixed_oracle_reduces_to_single_n():
+    X = small_suspension()
+    A, B = split_with_shortest(X, 2)
+    U = np.concatenate([A, B], axis=1)
+    N = X.shape[0] // 2
+    prm = O.StepParams(dt=1e-4, speed=2.0, near="matlab")
+    ref = O.time_step(U, np.zeros((N, U.shape[1])), prm)
+    Xo, so, it, info = O.time_step_mixed([A, B], [np.zeros((N, A.shape[1])), np.zeros((N, B.shape[1]))], prm)
+    assert info == 0 and it == ref.iters
+    Xm = np.concatenate(Xo, axis=1)
+    sm = np.concatenate(so, axis=1)
+    assert np.abs(Xm - ref.X).max() < 1e-12 * np.abs(ref.X).max()
+    assert np.abs(sm - ref.sigma).max() < 1e-9 * np.abs(ref.sigma).max()
+
+
+def test_cross_zone_matches_single_set_zone():
+    """Entries between two subsets = the single-set zone's entries between them."""
+    X = small_suspension(nv=6, seed=3)
+    N = X.shape[0] // 2
+    ent, h = O.get_zone(X)
+    src, tar = [0, 2, 4], [1, 3, 5]
+    cross = O.get_zone_cross(X[:, src], X[:, tar], h)
+    want = sorted((src.index(e.k1), tar.index(e.k2), e.j, e.icp) for e in ent if e.k1 in src and e.k2 in tar)
+    got = sorted((e.k1, e.k2, e.j, e.icp) for e in cross)
+    assert got == want and len(got) > 0

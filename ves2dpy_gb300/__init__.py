@@ -9,10 +9,10 @@ the C-ABI library ``_lib/libves2d_gb300.so`` (declared in
 ``include/ves2d_gb300.h``); there is no CPU fallback.
 """
 from ._native import GmresNotConverged, NearListOverflow, VesError, load_library  # noqa: F401
-from .suspension import config1_suspension, lattice_suspension, random_suspension  # noqa: F401
+from .suspension import config1_suspension, lattice_suspension, mixed_suspension, random_suspension  # noqa: F401
 
-__all__ = ["Poten", "capsules", "Curve", "TStepBiem", "naiveNearZoneInfo", "load_library",
-           "config1_suspension", "lattice_suspension", "random_suspension"]
+__all__ = ["Poten", "capsules", "Curve", "TStepBiem", "TStepBiemMixed", "naiveNearZoneInfo", "load_library",
+           "config1_suspension", "lattice_suspension", "mixed_suspension", "random_suspension"]
 
 
 def __getattr__(name):
@@ -28,6 +28,9 @@ def __getattr__(name):
     if name == "TStepBiem":
         from .tstep_biem import TStepBiem
         return TStepBiem
+    if name == "TStepBiemMixed":
+        from .tstep_biem import TStepBiemMixed
+        return TStepBiemMixed
     if name == "naiveNearZoneInfo":
         from .biem_support import naiveNearZoneInfo
         return naiveNearZoneInfo

@@ -157,6 +157,12 @@ int near_sing_int_run(ves_ctx* c, int scheme, int precision, int nv, const doubl
                       const double* sa_up, const double* Xup, const double* f, const double* vself,
                       const ves_near_lists* nl, double h, double* LP, double* near_only, WsCarver& ws,
                       cudaStream_t s);
+// between two vesicle sets (targets: ct, Xt; sources: cs, Xs / Xup_s, den_s, vself_s)
+int near_zone_matlab_cross(ves_ctx* ct, ves_ctx* cs, int nvt, const double* Xt, int nvs, const double* Xs, double h,
+                           const ves_near_lists* nl, WsCarver& ws, cudaStream_t s);
+int near_sing_int_cross_add(ves_ctx* ct, ves_ctx* cs, int scheme, int precision, int nvt, const double* Xt, int nvs,
+                            const double* Xup_s, const double* den_s, const double* vself_s,
+                            const ves_near_lists* nl, double h, double* LP, WsCarver& ws, cudaStream_t s);
 
 // double layer (viscosity contrast)
 int stokes_dl_matrix(ves_ctx* c, int nv, const double* X, const double* visc, int precision, double* D, WsCarver& ws,

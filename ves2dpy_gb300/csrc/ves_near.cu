@@ -61,19 +61,21 @@ __global__ void bbox_kernel(int n, const double* __restrict__ X, double* __restr
   if (threadIdx.x < 4) box[k * 4 + threadIdx.x] = red[threadIdx.x][0];
 }
 
-// one warp per target vesicle; candidates in ascending order
-__global__ void candidates_kernel(int nv, const double* __restrict__ tbox, const double* __restrict__ sbox,
-                                  double thr, int maxc, int* __restrict__ cand_count, int* __restrict__ cand_src,
-                                  VesDeviceStatus* st) {
+// one warp per target vesicle; candidates in ascending order.  nt target and
+// ns source vesicles; same_set: the two sets are one (a vesicle is not its own
+// candidate).
+__global__ void candidates_kernel(int nt, int ns, bool same_set, const double* __restrict__ tbox,
+                                  const double* __restrict__ sbox, double thr, int maxc, int* __restrict__ cand_count,
+                                  int* __restrict__ cand_src, VesDeviceStatus* st) {
   const int t = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
   const int lane = threadIdx.x % 32;
-  if (t >= nv) return;
+  if (t >= nt) return;
   const double tx0 = tbox[t * 4], tx1 = tbox[t * 4 + 1], ty0 = tbox[t * 4 + 2], ty1 = tbox[t * 4 + 3];
   int count = 0;
-  for (int base = 0; base < nv; base += 32) {
+  for (int base = 0; base < ns; base += 32) {
     const int s = base + lane;
     bool hit = false;
-    if (s < nv && s != t) {
+    if (s < ns && !(same_set && s == t)) {
       const double gx = fmax(0.0, fmax(sbox[s * 4] - tx1, tx0 - sbox[s * 4 + 1]));
       const double gy = fmax(0.0, fmax(sbox[s * 4 + 2] - ty1, ty0 - sbox[s * 4 + 3]));
       hit = gx * gx + gy * gy < thr * thr;
@@ -180,8 +182,11 @@ __global__ void hh_apply_kernel(int nv, int N, int Nup, int maxc, const double* 
   }
 }
 
-// MATLAB scheme: per (target vesicle t, candidate source s) and target point j
-__global__ void __launch_bounds__(128) matlab_zone_kernel(int N, int maxc, double h, const double* __restrict__ X,
+// MATLAB scheme: per (target vesicle t, candidate source s) and target point j;
+// targets Xt with Nt points per vesicle, sources Xs with Ns (one set: Xt = Xs)
+__global__ void __launch_bounds__(128) matlab_zone_kernel(int Nt, int Ns, int maxc, double h,
+                                                          const double* __restrict__ Xt,
+                                                          const double* __restrict__ Xs,
                                                           const double* __restrict__ lag,
                                                           const int* __restrict__ cand_count,
                                                           const int* __restrict__ cand_src,
@@ -191,26 +196,26 @@ __global__ void __launch_bounds__(128) matlab_zone_kernel(int N, int maxc, doubl
                                                           VesDeviceStatus* st) {
   extern __shared__ double sh[];
   const int t = blockIdx.y, slot = blockIdx.x;
-  const int wN = (N + 31) / 32;
+  const int wN = (Nt + 31) / 32;
   uint32_t* em = excl_mask + ((long long)t * maxc + slot) * wN;
   if (slot >= cand_count[t]) return;
   const int s = cand_src[(long long)t * maxc + slot];
   double* sx = sh;
-  double* sy = sx + N;
-  double* L = sy + N;  // 49
+  double* sy = sx + Ns;
+  double* L = sy + Ns;  // 49
   uint32_t* bits = (uint32_t*)(L + 49);
-  for (int i = threadIdx.x; i < N; i += blockDim.x) {
-    sx[i] = X[(long long)s * 2 * N + i];
-    sy[i] = X[(long long)s * 2 * N + N + i];
+  for (int i = threadIdx.x; i < Ns; i += blockDim.x) {
+    sx[i] = Xs[(long long)s * 2 * Ns + i];
+    sy[i] = Xs[(long long)s * 2 * Ns + Ns + i];
   }
   for (int i = threadIdx.x; i < 49; i += blockDim.x) L[i] = lag[i];
   for (int i = threadIdx.x; i < wN; i += blockDim.x) bits[i] = 0;
   __syncthreads();
-  for (int j = threadIdx.x; j < N; j += blockDim.x) {
-    const double xt = X[(long long)t * 2 * N + j], yt = X[(long long)t * 2 * N + N + j];
+  for (int j = threadIdx.x; j < Nt; j += blockDim.x) {
+    const double xt = Xt[(long long)t * 2 * Nt + j], yt = Xt[(long long)t * 2 * Nt + Nt + j];
     double best = 1e300;
     int icp = 0;
-    for (int i = 0; i < N; ++i) {
+    for (int i = 0; i < Ns; ++i) {
       const double dx = xt - sx[i], dy = yt - sy[i];
       const double d2 = dx * dx + dy * dy;
       if (d2 < best) {
@@ -226,7 +231,7 @@ __global__ void __launch_bounds__(128) matlab_zone_kernel(int N, int maxc, doubl
       double ax = 0, ay = 0;
 #pragma unroll
       for (int q = 0; q < 7; ++q) {
-        const int idx = ((icp - 3 + q) % N + N) % N;
+        const int idx = ((icp - 3 + q) % Ns + Ns) % Ns;
         ax = fma(L[r * 7 + q], sx[idx], ax);
         ay = fma(L[r * 7 + q], sy[idx], ay);
       }
@@ -283,8 +288,10 @@ __global__ void __launch_bounds__(128) matlab_zone_kernel(int N, int maxc, doubl
 // Lagrange points is the double layer (kernelDirect = exactStokesDL,
 // tstep_biem.py:236,501), with normals (ty, -tx) of the upsampled source and
 // den already scaled by (1 - visc); otherwise the single layer.
+// Targets Xt and LP with Nt points per vesicle; sources with Ns points (vself)
+// and Nup upsampled points (Xup, tang_up, den).
 template <bool DL>
-__global__ void matlab_correct_kernel(int N, int Nup, double h, const double* __restrict__ X,
+__global__ void matlab_correct_kernel(int Nt, int Ns, int Nup, double h, const double* __restrict__ Xt,
                                       const double* __restrict__ Xup, const double* __restrict__ tang_up,
                                       const double* __restrict__ den,
                                       const double* __restrict__ vself, const double* __restrict__ lag,
@@ -300,7 +307,7 @@ __global__ void matlab_correct_kernel(int N, int Nup, double h, const double* __
   const int icp = ent_icp[e];
   const double dist = ent_geo[4 * e], nxp = ent_geo[4 * e + 1], nyp = ent_geo[4 * e + 2], th = ent_geo[4 * e + 3];
   const double beta = 1.1;
-  const double xt = X[(long long)t * 2 * N + j], yt = X[(long long)t * 2 * N + N + j];
+  const double xt = Xt[(long long)t * 2 * Nt + j], yt = Xt[(long long)t * 2 * Nt + Nt + j];
   const double ux = (xt - nxp) / dist, uy = (yt - nyp) / dist;
   // layer potential of source vesicle s at the 6 Lagrange points
   double ax[6], ay[6];
@@ -346,7 +353,7 @@ __global__ void matlab_correct_kernel(int N, int Nup, double h, const double* __
   for (int comp = 0; comp < 2; ++comp) {
     // on-curve value: Lagrange interpolant of vself around icp at theta
     double coef[7], stencil[7];
-    for (int q = 0; q < 7; ++q) stencil[q] = vself[(long long)s * 2 * N + comp * N + ((icp - 3 + q) % N + N) % N];
+    for (int q = 0; q < 7; ++q) stencil[q] = vself[(long long)s * 2 * Ns + comp * Ns + ((icp - 3 + q) % Ns + Ns) % Ns];
     for (int r = 0; r < 7; ++r) {
       double a = 0;
       for (int q = 0; q < 7; ++q) a = fma(lag[r * 7 + q], stencil[q], a);
@@ -363,11 +370,11 @@ __global__ void matlab_correct_kernel(int N, int Nup, double h, const double* __
     }
     vals[comp] = horner7(coef, dist / (beta * h * 6.0));
   }
-  atomicAdd(&LP[(long long)t * 2 * N + j], vals[0]);
-  atomicAdd(&LP[(long long)t * 2 * N + N + j], vals[1]);
+  atomicAdd(&LP[(long long)t * 2 * Nt + j], vals[0]);
+  atomicAdd(&LP[(long long)t * 2 * Nt + Nt + j], vals[1]);
   if (near_only) {
-    atomicAdd(&near_only[(long long)t * 2 * N + j], vals[0]);
-    atomicAdd(&near_only[(long long)t * 2 * N + N + j], vals[1]);
+    atomicAdd(&near_only[(long long)t * 2 * Nt + j], vals[0]);
+    atomicAdd(&near_only[(long long)t * 2 * Nt + Nt + j], vals[1]);
   }
 }
 
@@ -387,6 +394,11 @@ __global__ void min_reduce_kernel(int n, const double* __restrict__ a, double* _
 __global__ void identity_index_kernel(int n, int* __restrict__ idx) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) idx[i] = i;
+}
+
+__global__ void add_kernel(long long n, const double* __restrict__ a, double* __restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] += a[i];
 }
 
 }  // namespace
@@ -415,7 +427,8 @@ int near_zone_py(ves_ctx* c, int nv, const double* X, const double* Xup_in, doub
   ves_count_launch();
   bbox_kernel<<<nv, 128, 0, s>>>(Nup, Xu, sbox);
   ves_count_launch();
-  candidates_kernel<<<ceil_div((long long)nv * 32, 256), 256, 0, s>>>(nv, tbox, sbox, thr, nl->maxc, nl->cand_count,
+  candidates_kernel<<<ceil_div((long long)nv * 32, 256), 256, 0, s>>>(nv, nv, true, tbox, sbox, thr, nl->maxc,
+                                                                      nl->cand_count,
                                                                       nl->cand_src, c->status);
   const size_t sh = (size_t)2 * N * sizeof(double) + (c->nwords_N + c->nwords_up) * sizeof(uint32_t);
   dim3 grid(nl->maxc, nv);
@@ -457,12 +470,12 @@ int near_zone_matlab(ves_ctx* c, int nv, const double* X, double h, const ves_ne
   ves_count_launch();
   bbox_kernel<<<nv, 128, 0, s>>>(N, X, box);
   ves_count_launch();
-  candidates_kernel<<<ceil_div((long long)nv * 32, 256), 256, 0, s>>>(nv, box, box, 2.0 * h, nl->maxc,
+  candidates_kernel<<<ceil_div((long long)nv * 32, 256), 256, 0, s>>>(nv, nv, true, box, box, 2.0 * h, nl->maxc,
                                                                       nl->cand_count, nl->cand_src, c->status);
   const size_t sh = (size_t)(2 * N + 49) * sizeof(double) + c->nwords_N * sizeof(uint32_t);
   dim3 grid(nl->maxc, nv);
   ves_count_launch();
-  matlab_zone_kernel<<<grid, 128, sh, s>>>(N, nl->maxc, h, X, c->lag, nl->cand_count, nl->cand_src,
+  matlab_zone_kernel<<<grid, 128, sh, s>>>(N, N, nl->maxc, h, X, X, c->lag, nl->cand_count, nl->cand_src,
                                            nl->excl_mask, nl->max_entries, nl->n_entries, nl->ent_tsj,
                                            nl->ent_icp, nl->ent_geo, c->status);
   return ves_launch_check("near_zone_matlab");
@@ -519,11 +532,82 @@ int near_sing_int_run(ves_ctx* c, int scheme, int precision, int nv, const doubl
   } else if (scheme == VES_NEAR_MATLAB) {
     const long long warps = nl->max_entries;
     ves_count_launch();
-    matlab_correct_kernel<false><<<ceil_div(warps * 32, 256), 256, 0, s>>>(N, Nup, h, X, Xup, nullptr, den, vself, c->lag,
+    matlab_correct_kernel<false><<<ceil_div(warps * 32, 256), 256, 0, s>>>(N, N, Nup, h, X, Xup, nullptr, den, vself,
+                                                                           c->lag,
                                                                     nl->n_entries, nl->max_entries, nl->ent_tsj,
                                                                     nl->ent_icp, nl->ent_geo, LP, near_only);
   }
   return ves_launch_check("near_sing_int");
+}
+
+// Two vesicle sets of different point counts (a mixed suspension): the near
+// zone of the target points of one set w.r.t. the source vesicles of the
+// other (getZone's NearOther, matlab/capsules_py.m:194-467, with the source
+// set's h) and the source set's single layer at the target points with those
+// entries corrected (nearSingInt with tEqualS false, matlab/poten_py.m:495-692).
+int near_zone_matlab_cross(ves_ctx* ct, ves_ctx* cs, int nvt, const double* Xt, int nvs, const double* Xs, double h,
+                           const ves_near_lists* nl, WsCarver& ws, cudaStream_t s) {
+  const int Nt = ct->N, Ns = cs->N;
+  double* tbox = ws.take<double>((size_t)nvt * 4);
+  double* sbox = ws.take<double>((size_t)nvs * 4);
+  if (ws.sizing) return VES_OK;
+  if (!ws.ok()) {
+    ves_record_error(VES_ERR_WORKSPACE, "near_zone_cross: workspace too small");
+    return VES_ERR_WORKSPACE;
+  }
+  if (!nl || !nl->cand_count || !nl->cand_src || !nl->excl_mask || !nl->n_entries || !nl->ent_tsj ||
+      !nl->ent_icp || !nl->ent_geo || nl->maxc <= 0 || h <= 0) {
+    ves_record_error(VES_ERR_ARG, "near_zone_cross: incomplete near lists or h <= 0");
+    return VES_ERR_ARG;
+  }
+  int rc = ves_cuda_status(cudaMemsetAsync(nl->n_entries, 0, sizeof(int), s), "zero entries");
+  if (rc || nvt <= 0) return rc;
+  ves_count_launch(nvs > 0 ? 3 : 2);
+  bbox_kernel<<<nvt, 128, 0, s>>>(Nt, Xt, tbox);
+  if (nvs > 0) bbox_kernel<<<nvs, 128, 0, s>>>(Ns, Xs, sbox);
+  candidates_kernel<<<ceil_div((long long)nvt * 32, 256), 256, 0, s>>>(nvt, nvs, false, tbox, sbox, 2.0 * h, nl->maxc,
+                                                                       nl->cand_count, nl->cand_src, ct->status);
+  const size_t sh = (size_t)(2 * Ns + 49) * sizeof(double) + ct->nwords_N * sizeof(uint32_t);
+  dim3 grid(nl->maxc, nvt);
+  ves_count_launch();
+  matlab_zone_kernel<<<grid, 128, sh, s>>>(Nt, Ns, nl->maxc, h, Xt, Xs, ct->lag, nl->cand_count, nl->cand_src,
+                                           nl->excl_mask, nl->max_entries, nl->n_entries, nl->ent_tsj, nl->ent_icp,
+                                           nl->ent_geo, ct->status);
+  return ves_launch_check("near_zone_cross");
+}
+
+int near_sing_int_cross_add(ves_ctx* ct, ves_ctx* cs, int scheme, int precision, int nvt, const double* Xt, int nvs,
+                            const double* Xup_s, const double* den_s, const double* vself_s,
+                            const ves_near_lists* nl, double h, double* LP, WsCarver& ws, cudaStream_t s) {
+  const int Nt = ct->N, Ns = cs->N, Nups = cs->Nup;
+  double* tmp = ws.take<double>((size_t)nvt * 2 * Nt);
+  const ves_near_lists* excl = (scheme == VES_NEAR_MATLAB) ? nl : nullptr;
+  if (ws.sizing) {
+    farfield_run(ct, precision, nvs, Nups, Xup_s, den_s, nvt, Nt, Xt, nullptr, excl, tmp, ws, s);
+    return VES_OK;
+  }
+  if (!ws.ok()) {
+    ves_record_error(VES_ERR_WORKSPACE, "near_sing_int_cross: workspace too small");
+    return VES_ERR_WORKSPACE;
+  }
+  if (scheme != VES_NEAR_NONE && scheme != VES_NEAR_MATLAB) {
+    ves_record_error(VES_ERR_ARG, "near_sing_int_cross: scheme %d (between sets: matlab or none)", scheme);
+    return VES_ERR_ARG;
+  }
+  if (nvt <= 0 || nvs <= 0) return VES_OK;
+  int rc = farfield_run(ct, precision, nvs, Nups, Xup_s, den_s, nvt, Nt, Xt, nullptr, excl, tmp, ws, s);
+  if (rc) return rc;
+  const long long n = (long long)nvt * 2 * Nt;
+  ves_count_launch();
+  add_kernel<<<ceil_div(n, 256), 256, 0, s>>>(n, tmp, LP);
+  if (scheme == VES_NEAR_MATLAB) {
+    const long long warps = nl->max_entries;
+    ves_count_launch();
+    matlab_correct_kernel<false><<<ceil_div(warps * 32, 256), 256, 0, s>>>(
+        Nt, Ns, Nups, h, Xt, Xup_s, nullptr, den_s, vself_s, ct->lag, nl->n_entries, nl->max_entries, nl->ent_tsj,
+        nl->ent_icp, nl->ent_geo, LP, nullptr);
+  }
+  return ves_launch_check("near_sing_int_cross");
 }
 
 // nearSingInt with kernelDirect = exactStokesDL (tstep_biem.py:236,501;
@@ -581,7 +665,7 @@ int near_sing_int_dl_run(ves_ctx* c, int scheme, int precision, int nv, const do
     const long long warps = nl->max_entries;
     ves_count_launch();
     matlab_correct_kernel<true><<<ceil_div(warps * 32, 256), 256, 0, s>>>(
-        N, Nup, h, X, Xup, tang_up, den, vself, c->lag, nl->n_entries, nl->max_entries, nl->ent_tsj, nl->ent_icp,
+        N, N, Nup, h, X, Xup, tang_up, den, vself, c->lag, nl->n_entries, nl->max_entries, nl->ent_tsj, nl->ent_icp,
         nl->ent_geo, LP, near_only);
   }
   return ves_launch_check("near_sing_int_dl");

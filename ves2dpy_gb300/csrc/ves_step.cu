@@ -249,21 +249,98 @@ struct GmresBufs {
   double* ydev;
 };
 
-int device_norm(StepState& S, GmresBufs& B, const double* a, double* dst) {
+template <class St>
+int device_norm(St& S, GmresBufs& B, const double* a, double* dst) {
   launch_dot_partials(S.n, a, a, B.partials, S.s);
   ves_count_launch();
   finalize_dot_kernel<<<1, 512, 0, S.s>>>(B.partials, dot_partial_blocks(), dst, 1);
   return ves_launch_check("norm");
 }
 
-int read_scalars(StepState& S, GmresBufs& B, const double* src, int count) {
+template <class St>
+int read_scalars(St& S, GmresBufs& B, const double* src, int count) {
   int rc = ves_cuda_status(cudaMemcpyAsync(B.hsc, src, count * sizeof(double), cudaMemcpyDeviceToHost, S.s), "read");
   if (rc) return rc;
   return ves_cuda_status(cudaStreamSynchronize(S.s), "read sync");
 }
 
+// A suspension of several point counts: groups of vesicles, group g with N_g
+// points and its own context, in one GMRES system (the groups' [nv][3][N]
+// blocks one after the other).  Between groups the far field runs over the
+// source group's upsampled points and the near zone and its correction follow
+// the MATLAB rules with a separate target set (source group's h).
+constexpr int kMaxGroups = 4;
+
+struct MixedState {
+  const ves_step_params* prm;
+  int ng;
+  long long n;
+  cudaStream_t s;
+  StepState g[kMaxGroups];
+  long long off[kMaxGroups + 1];
+  double *fup[kMaxGroups], *den[kMaxGroups];
+  ves_near_lists xl[kMaxGroups][kMaxGroups];  // [target group][source group]
+  double h[kMaxGroups];
+  char* scratch;
+  size_t scratch_bytes;
+  int matvecs;
+};
+
+int matvec(MixedState& M, const double* v, double* out) {
+  M.matvecs++;
+  const ves_step_params* prm = M.prm;
+  for (int q = 0; q < M.ng; ++q) {
+    StepState& S = M.g[q];
+    const int nv = S.nv, N = S.N;
+    const double* vq = v + M.off[q];
+    launch_trac_jump(S.c, nv, prm->kappa, S.isa, S.tang, vq, 3LL * N, vq + 2 * N, 3LL * N, S.f, M.s);
+    launch_bgemv_f64(nv, 2 * N, 2 * N, S.G, S.f, 2LL * N, S.Gf, 2LL * N, M.s);
+    if (M.ng > 1) {
+      launch_upsample(S.c, nv, 2, S.f, 2LL * N, M.fup[q], M.s);
+      launch_density(nv, S.Nup, M.fup[q], S.sa_up, M.den[q], M.s);
+    }
+  }
+  int rc;
+  for (int g = 0; g < M.ng; ++g) {
+    StepState& S = M.g[g];
+    {
+      WsCarver sub(M.scratch, M.scratch_bytes);
+      if ((rc = near_sing_int_run(S.c, prm->near_scheme, prm->farfield_precision, S.nv, S.X, S.sa_up, S.Xup, S.f,
+                                  S.Gf, &S.nl, S.h, S.LP, nullptr, sub, M.s)))
+        return rc;
+    }
+    for (int q = 0; q < M.ng; ++q) {
+      if (q == g) continue;
+      const StepState& Q = M.g[q];
+      WsCarver sub(M.scratch, M.scratch_bytes);
+      if ((rc = near_sing_int_cross_add(S.c, Q.c, prm->near_scheme, prm->farfield_precision, S.nv, S.X, Q.nv, Q.Xup,
+                                        M.den[q], Q.Gf, &M.xl[g][q], M.h[q], S.LP, sub, M.s)))
+        return rc;
+    }
+    const int nv = S.nv, N = S.N;
+    const double* vg = v + M.off[g];
+    double* og = out + M.off[g];
+    ves_count_launch();
+    combine_pos_kernel<<<ceil_div((long long)nv * 2 * N, 256), 256, 0, M.s>>>(nv, N, prm->dt, vg, S.Gf, S.LP, nullptr,
+                                                                              nullptr, nullptr, og);
+    launch_surface_div(S.c, nv, S.isa, S.tang, vg, 3LL * N, og + 2 * N, 3LL * N, M.s);
+  }
+  return ves_launch_check("matvec mixed");
+}
+
+int psolve(MixedState& M, const double* z, double* out) {
+  if (!M.prm->use_preco) {
+    return ves_cuda_status(cudaMemcpyAsync(out, z, M.n * sizeof(double), cudaMemcpyDeviceToDevice, M.s),
+                           "psolve copy");
+  }
+  for (int g = 0; g < M.ng; ++g)
+    launch_lu_solve(M.g[g].nv, 3 * M.g[g].N, M.g[g].LU, M.g[g].piv, z + M.off[g], out + M.off[g], M.s);
+  return ves_launch_check("psolve mixed");
+}
+
 // scipy.sparse.linalg.gmres (scipy/sparse/linalg/_isolve/iterative.py), device vectors
-int gmres(StepState& S, GmresBufs& B, ves_step_result* res) {
+template <class St>
+int gmres(St& S, GmresBufs& B, ves_step_result* res) {
   const long long n = S.n;
   const int restart = std::min<long long>(S.prm->gmres_restart > 0 ? S.prm->gmres_restart : 20, n);
   const int maxiter = S.prm->gmres_maxiter > 0 ? S.prm->gmres_maxiter : (int)std::min<long long>(n * 10, 1 << 30);
@@ -677,4 +754,273 @@ extern "C" int ves_biem_step(ves_ctx* c, const ves_step_params* prm, int nv, con
   memset(res, 0, sizeof(*res));
   WsCarver w(ws, ws_bytes);
   return biem_step_impl(c, prm, nv, X, sigma, Xout, sigma_out, res, w, (cudaStream_t)stream);
+}
+
+// ---------------------------------------------------------------------------
+// One implicit step of a suspension given as groups of different point counts
+// (every group's vesicles in one GMRES system; no viscosity contrast, no
+// repulsion; near scheme matlab or none).  Within a group the step is the
+// single-N step's; between groups see MixedState.
+static int biem_step_mixed_impl(int ng, ves_ctx* const* ctx, const ves_step_params* prm, const int* nvs,
+                                const double* const* X, const double* const* sigma, double* const* Xout,
+                                double* const* sigma_out, ves_step_result* res, WsCarver& ws, cudaStream_t s) {
+  if (ng < 1 || ng > kMaxGroups || !ctx || !prm || !nvs) {
+    if (!ws.sizing) ves_record_error(VES_ERR_ARG, "biem_step_mixed: 1 to %d groups", kMaxGroups);
+    return VES_ERR_ARG;
+  }
+  for (int g = 0; g < ng; ++g)
+    if (!ctx[g] || nvs[g] < 1) {
+      if (!ws.sizing) ves_record_error(VES_ERR_ARG, "biem_step_mixed: bad group %d", g);
+      return VES_ERR_ARG;
+    }
+  const int maxc = prm->maxc > 0 ? prm->maxc : 64;
+  MixedState M;
+  memset(&M, 0, sizeof(M));
+  M.prm = prm;
+  M.ng = ng;
+  M.s = s;
+  M.off[0] = 0;
+  for (int g = 0; g < ng; ++g) M.off[g + 1] = M.off[g] + 3LL * ctx[g]->N * nvs[g];
+  const long long n = M.off[ng];
+  M.n = n;
+  const int restart = (int)std::min<long long>(prm->gmres_restart > 0 ? prm->gmres_restart : 20, n > 0 ? n : 1);
+  double* vinf[kMaxGroups];
+  double* rhs2[kMaxGroups];
+  for (int g = 0; g < ng; ++g) {
+    ves_ctx* c = ctx[g];
+    const int nv = nvs[g], N = c->N, Nup = c->Nup;
+    const int maxe = prm->max_entries > 0 ? prm->max_entries : std::max(1024, nv * N);
+    StepState& S = M.g[g];
+    S.c = c;
+    S.prm = prm;
+    S.nv = nv;
+    S.N = N;
+    S.Nup = Nup;
+    S.n = 3LL * N * nv;
+    S.s = s;
+    S.X = X ? X[g] : nullptr;
+    S.sa = ws.take<double>((size_t)nv * N);
+    S.isa = ws.take<double>((size_t)nv * N);
+    S.tang = ws.take<double>((size_t)nv * 2 * N);
+    S.Xup = ws.take<double>((size_t)nv * 2 * Nup);
+    S.sa_up = ws.take<double>((size_t)nv * Nup);
+    S.G = ws.take<double>((size_t)nv * 4 * N * N);
+    S.LU = ws.take<double>((size_t)nv * 9 * N * N);
+    S.piv = ws.take<int>((size_t)nv * 3 * N);
+    S.f = ws.take<double>((size_t)nv * 2 * N);
+    S.Gf = ws.take<double>((size_t)nv * 2 * N);
+    S.LP = ws.take<double>((size_t)nv * 2 * N);
+    S.nl.maxc = maxc;
+    S.nl.cand_count = ws.take<int>(nv);
+    S.nl.cand_src = ws.take<int>((size_t)nv * maxc);
+    S.nl.excl_mask = ws.take<uint32_t>((size_t)nv * maxc * c->nwords_N);
+    S.nl.hh_mask = ws.take<uint32_t>((size_t)nv * maxc * c->nwords_up);
+    S.nl.max_entries = maxe;
+    S.nl.n_entries = ws.take<int>(1);
+    S.nl.ent_tsj = ws.take<int>((size_t)maxe * 3);
+    S.nl.ent_icp = ws.take<int>((size_t)maxe);
+    S.nl.ent_geo = ws.take<double>((size_t)maxe * 4);
+    M.fup[g] = ws.take<double>((size_t)nv * 2 * Nup);
+    M.den[g] = ws.take<double>((size_t)nv * 2 * Nup);
+    vinf[g] = ws.take<double>((size_t)nv * 2 * N);
+    rhs2[g] = ws.take<double>((size_t)nv * N);
+    for (int q = 0; q < ng; ++q) {
+      if (q == g) continue;
+      ves_near_lists& L = M.xl[g][q];
+      L.maxc = maxc;
+      L.cand_count = ws.take<int>(nv);
+      L.cand_src = ws.take<int>((size_t)nv * maxc);
+      L.excl_mask = ws.take<uint32_t>((size_t)nv * maxc * c->nwords_N);
+      L.max_entries = maxe;
+      L.n_entries = ws.take<int>(1);
+      L.ent_tsj = ws.take<int>((size_t)maxe * 3);
+      L.ent_icp = ws.take<int>((size_t)maxe);
+      L.ent_geo = ws.take<double>((size_t)maxe * 4);
+    }
+  }
+  GmresBufs B;
+  B.V = ws.take<double>((size_t)(restart + 1) * n);
+  B.w = ws.take<double>(n);
+  B.r = ws.take<double>(n);
+  B.b = ws.take<double>(n);
+  B.x = ws.take<double>(n);
+  B.t = ws.take<double>(n);
+  B.partials = ws.take<double>(dot_partial_blocks());
+  B.dsc = ws.take<double>(restart + 8);
+  B.ydev = ws.take<double>(restart + 2);
+  size_t scratch = 0;
+  for (int g = 0; g < ng; ++g) {
+    ves_ctx* c = ctx[g];
+    const int nv = nvs[g], N = c->N;
+    {
+      WsCarver w(nullptr, 0);
+      alpert_sl_matrix(c, nv, nullptr, prm->sl_precision, nullptr, w, s);
+      scratch = std::max(scratch, w.off);
+    }
+    {
+      WsCarver w(nullptr, 0);
+      derivs_and_precond(c, nv, nullptr, nullptr, nullptr, 0, 0, nullptr, nullptr, nullptr, (double*)1, w, s);
+      w.take<double>((size_t)nv * 2 * N * N);  // Ten
+      w.take<double>((size_t)nv * 2 * N * N);  // Div
+      scratch = std::max(scratch, w.off);
+    }
+    {
+      WsCarver w(nullptr, 0);
+      near_zone_matlab(c, nv, nullptr, 0, nullptr, w, s);
+      scratch = std::max(scratch, w.off);
+    }
+    {
+      WsCarver w(nullptr, 0);
+      near_sing_int_run(c, prm->near_scheme, prm->farfield_precision, nv, nullptr, nullptr, nullptr, nullptr, nullptr,
+                        nullptr, 0, nullptr, nullptr, w, s);
+      scratch = std::max(scratch, w.off);
+    }
+    for (int q = 0; q < ng; ++q) {
+      if (q == g) continue;
+      WsCarver w(nullptr, 0);
+      near_zone_matlab_cross(c, ctx[q], nv, nullptr, nvs[q], nullptr, 1.0, nullptr, w, s);
+      scratch = std::max(scratch, w.off);
+      WsCarver w2(nullptr, 0);
+      near_sing_int_cross_add(c, ctx[q], prm->near_scheme, prm->farfield_precision, nv, nullptr, nvs[q], nullptr,
+                              nullptr, nullptr, nullptr, 1.0, nullptr, w2, s);
+      scratch = std::max(scratch, w2.off);
+    }
+  }
+  M.scratch = ws.take<char>(scratch + 1024);
+  M.scratch_bytes = scratch + 1024;
+  if (ws.sizing) return VES_OK;
+  if (!ws.ok()) {
+    ves_record_error(VES_ERR_WORKSPACE, "biem_step_mixed: workspace too small (%zu needed)", ws.off);
+    return VES_ERR_WORKSPACE;
+  }
+  if (!X || !sigma || !Xout || !sigma_out || !res) {
+    ves_record_error(VES_ERR_ARG, "biem_step_mixed: bad arguments");
+    return VES_ERR_ARG;
+  }
+  if (prm->near_scheme != VES_NEAR_NONE && prm->near_scheme != VES_NEAR_MATLAB) {
+    ves_record_error(VES_ERR_ARG, "biem_step_mixed: near scheme must be matlab or none");
+    return VES_ERR_ARG;
+  }
+  if (prm->visc_cont || prm->repulsion) {
+    ves_record_error(VES_ERR_ARG, "biem_step_mixed: no viscosity contrast or repulsion between groups");
+    return VES_ERR_ARG;
+  }
+  if (restart + 8 > 256) {
+    ves_record_error(VES_ERR_ARG, "biem_step_mixed: restart %d too large", restart);
+    return VES_ERR_ARG;
+  }
+  int rc = 0;
+  for (int g = 0; g < ng; ++g)
+    if ((rc = ves_reset_status(ctx[g], s))) return rc;
+  B.hsc = ctx[0]->h_scal;
+  // geometry, h = min length / N of each group (capsules.py:46-47), in-group zones
+  {
+    std::vector<double> hl;
+    for (int g = 0; g < ng; ++g) {
+      StepState& S = M.g[g];
+      if (S.nv == 0) continue;
+      launch_diff_prop(S.c, 0, S.nv, S.X, S.sa, S.isa, S.tang, nullptr, s);
+      launch_upsample_deriv(S.c, S.nv, S.X, S.Xup, nullptr, S.sa_up, s);
+      WsCarver sub(M.scratch, M.scratch_bytes);
+      if ((rc = alpert_sl_matrix(S.c, S.nv, S.X, prm->sl_precision, S.G, sub, s))) return rc;
+      double* len = (double*)M.scratch;
+      launch_geom_prop(S.c, S.nv, S.X, nullptr, nullptr, len, s);
+      hl.resize(S.nv);
+      if ((rc = ves_cuda_status(cudaMemcpyAsync(hl.data(), len, S.nv * sizeof(double), cudaMemcpyDeviceToHost, s),
+                                "len")))
+        return rc;
+      if ((rc = ves_cuda_status(cudaStreamSynchronize(s), "len sync"))) return rc;
+      M.h[g] = S.h = *std::min_element(hl.begin(), hl.end()) / S.N;
+      if (prm->near_scheme == VES_NEAR_MATLAB) {
+        WsCarver sub2(M.scratch, M.scratch_bytes);
+        if ((rc = near_zone_matlab(S.c, S.nv, S.X, S.h, &S.nl, sub2, s))) return rc;
+      }
+    }
+  }
+  if (prm->near_scheme == VES_NEAR_MATLAB) {
+    for (int g = 0; g < ng; ++g)
+      for (int q = 0; q < ng; ++q) {
+        if (q == g || M.g[g].nv == 0) continue;
+        WsCarver sub(M.scratch, M.scratch_bytes);
+        if ((rc = near_zone_matlab_cross(ctx[g], ctx[q], M.g[g].nv, X[g], M.g[q].nv, X[q],
+                                         M.g[q].nv > 0 ? M.h[q] : 1.0, &M.xl[g][q], sub, s)))
+          return rc;
+      }
+  }
+  // right-hand side and initial guess, group by group; the preconditioner blocks
+  for (int g = 0; g < ng; ++g) {
+    StepState& S = M.g[g];
+    const int nv = S.nv, N = S.N;
+    if (nv == 0) continue;
+    const long long n2 = (long long)nv * 2 * N;
+    launch_bg_flow(nv, N, prm->flow, prm->speed, prm->chan_width, prm->vortex_size, S.X, vinf[g], s);
+    ves_count_launch();
+    rhs_pos_kernel<<<ceil_div(n2, 256), 256, 0, s>>>(n2, N, prm->dt, S.X, vinf[g], nullptr, nullptr, nullptr, nullptr,
+                                                     nullptr, vinf[g]);
+    launch_surface_div(S.c, nv, S.isa, S.tang, S.X, 2LL * N, rhs2[g], N, s);
+    ves_count_launch();
+    pack_kernel<<<ceil_div(S.n, 256), 256, 0, s>>>(nv, N, vinf[g], rhs2[g], B.b + M.off[g]);
+    if (prm->use_preco) {
+      ves_count_launch();
+      pack_kernel<<<ceil_div(S.n, 256), 256, 0, s>>>(nv, N, S.X, sigma[g], B.x + M.off[g]);
+      WsCarver sub(M.scratch, M.scratch_bytes);
+      double* Ten = sub.take<double>((size_t)nv * 2 * N * N);
+      double* Div = sub.take<double>((size_t)nv * 2 * N * N);
+      if ((rc = derivs_and_precond(S.c, nv, S.isa, S.tang, S.G, prm->dt, prm->kappa, nullptr, Ten, Div, S.LU, sub, s)))
+        return rc;
+      if ((rc = launch_lu_factor(S.c, nv, 3 * N, S.LU, S.piv, s))) return rc;
+    }
+  }
+  if (!prm->use_preco && n > 0)
+    if ((rc = ves_cuda_status(cudaMemsetAsync(B.x, 0, n * sizeof(double), s), "x0"))) return rc;
+  for (int g = 0; g < ng; ++g)
+    if ((rc = ves_check_status(ctx[g], s, "biem_step_mixed setup"))) return rc;
+  M.matvecs = 0;
+  if ((rc = gmres(M, B, res))) return rc;
+  res->matvecs = M.matvecs;
+  int nn_total = 0;
+  for (int g = 0; g < ng; ++g) {
+    StepState& S = M.g[g];
+    if (S.nv == 0) continue;
+    ves_count_launch();
+    unpack_kernel<<<ceil_div(S.n, 256), 256, 0, s>>>(S.nv, S.N, B.x + M.off[g], Xout[g], sigma_out[g]);
+    if (prm->near_scheme == VES_NEAR_MATLAB) {
+      int nn = 0;
+      cudaMemcpyAsync(&nn, S.nl.n_entries, sizeof(int), cudaMemcpyDeviceToHost, s);
+      cudaStreamSynchronize(s);
+      nn_total += nn;
+      for (int q = 0; q < ng; ++q) {
+        if (q == g) continue;
+        cudaMemcpyAsync(&nn, M.xl[g][q].n_entries, sizeof(int), cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        nn_total += nn;
+      }
+    }
+  }
+  res->n_near_entries = nn_total;
+  for (int g = 0; g < ng; ++g)
+    if ((rc = ves_check_status(ctx[g], s, "biem_step_mixed"))) return rc;
+  if (res->info != 0) {
+    ves_record_error(VES_ERR_GMRES_MAXIT, "biem_step_mixed: GMRES reached maxiter (resid %.3e)", res->resid);
+    return VES_ERR_GMRES_MAXIT;
+  }
+  return VES_OK;
+}
+
+extern "C" size_t ves_biem_step_mixed_workspace(int ngroups, ves_ctx* const* ctx, const ves_step_params* prm,
+                                                const int* nv) {
+  WsCarver w(nullptr, 0);
+  ves_step_result r;
+  if (biem_step_mixed_impl(ngroups, ctx, prm, nv, nullptr, nullptr, nullptr, nullptr, &r, w, 0)) return 0;
+  return w.off + 256;
+}
+
+extern "C" int ves_biem_step_mixed(int ngroups, ves_ctx* const* ctx, const ves_step_params* prm, const int* nv,
+                                   const double* const* X, const double* const* sigma, double* const* Xout,
+                                   double* const* sigma_out, ves_step_result* res, void* ws, size_t ws_bytes,
+                                   void* stream) {
+  if (!ctx || !prm || !res || !ws || !nv) return VES_ERR_ARG;
+  memset(res, 0, sizeof(*res));
+  WsCarver w(ws, ws_bytes);
+  return biem_step_mixed_impl(ngroups, ctx, prm, nv, X, sigma, Xout, sigma_out, res, w, (cudaStream_t)stream);
 }

@@ -147,6 +147,66 @@ def random_suspension(nv: int, N: int, area_fraction: float, min_gap: float = 0.
     return X
 
 
+def mixed_suspension(groups, area_fraction: float, box_aspect: float = 1.0, min_gap: float = 0.05,
+                     reduced_area=0.65, area: float = math.pi, seed: int = 0, max_tries: int = 2000):
+    """Vesicles of several point counts: ``groups`` = [(nv_g, N_g), ...].
+
+    Centres uniform in a [0, Lx] x [-Ly/2, Ly/2] rectangle with Lx / Ly =
+    ``box_aspect``, sized for the area fraction; vesicles are placed in a
+    seeded random order over the groups with the rejection rule of
+    ``random_suspension``.  Returns a list of X[2N_g, nv_g] arrays.
+    """
+    rng = np.random.default_rng(seed)
+    nv_tot = sum(nv for nv, _ in groups)
+    tot_area = nv_tot * area / area_fraction
+    Ly = math.sqrt(tot_area / box_aspect)
+    Lx = tot_area / Ly
+    Xs = [np.zeros((2 * N, nv)) for nv, N in groups]
+    order = np.concatenate([np.full(nv, g) for g, (nv, _) in enumerate(groups)])
+    rng.shuffle(order)
+    ra_lo = min(reduced_area) if isinstance(reduced_area, tuple) else reduced_area
+    cell = 2.0 * ellipse_axes(ra_lo, area)[0] * 1.2 + min_gap
+    nx, ny = max(1, int(Lx // cell)), max(1, int(Ly // cell))
+    grid: dict = {}
+    placed = []   # (group, column, cx, cy, r)
+    count = [0] * len(groups)
+    for g in order:
+        N = groups[g][1]
+        for _ in range(max_tries):
+            ra = rng.uniform(*reduced_area) if isinstance(reduced_area, tuple) else reduced_area
+            x, y = vesicle_shape(N, rng, ra, area)
+            cx, cy = rng.uniform(0, Lx), rng.uniform(-0.5 * Ly, 0.5 * Ly)
+            r = float(np.sqrt(x ** 2 + y ** 2).max())
+            gx, gy = int(cx / Lx * nx), int((cy + 0.5 * Ly) / Ly * ny)
+            ok = True
+            for ix in range(gx - 1, gx + 2):
+                for iy in range(gy - 1, gy + 2):
+                    for q in grid.get((ix, iy), ()):
+                        pg, pc, pcx, pcy, pr = placed[q]
+                        if math.hypot(cx - pcx, cy - pcy) > r + pr + min_gap:
+                            continue
+                        Np = groups[pg][1]
+                        Xp = Xs[pg]
+                        if _min_gap(x + cx, y + cy, Xp[:Np, pc], Xp[Np:, pc]) < min_gap:
+                            ok = False
+                            break
+                    if not ok:
+                        break
+                if not ok:
+                    break
+            if ok:
+                break
+        else:
+            raise RuntimeError("mixed_suspension: could not place a vesicle of group %d" % g)
+        c = count[g]
+        Xs[g][:N, c] = x + cx
+        Xs[g][N:, c] = y + cy
+        count[g] += 1
+        grid.setdefault((gx, gy), []).append(len(placed))
+        placed.append((g, c, cx, cy, r))
+    return Xs
+
+
 def config1_suspension(N: int = 32, seed: int = 0):
     """nv=16 vesicles of reduced area 0.65, area pi, on a 4x4 lattice, spacing 3.0, gap >= 0.3."""
     return lattice_suspension(4, N, spacing=3.0, jitter=0.1, min_gap=0.3, seed=seed)

@@ -147,3 +147,79 @@ class TStepBiem:
                                       speed, float(kwargs.get("chanWidth", 1.0)), float(kwargs.get("vortexSize", 1.0)),
                                       Xv.data_ptr(), out.data_ptr(), nat.stream_ptr(self.device)), "bg_flow")
         return from_vm(out)
+
+
+class TStepBiemMixed:
+    """One implicit step of a suspension of several point counts.
+
+    ``Xs`` is a list of groups, each an X[2N_g, nv_g] array in the reference
+    layout (the reference itself holds one N per suspension; this class has
+    no counterpart there).  Every vesicle of every group is in one GMRES
+    system.  Within a group the step is TStepBiem's with the given ``near``
+    rule; between groups the far field runs over the source group's
+    upsampled points and the near zone and its correction follow the MATLAB
+    rules with a separate target set (getZone's NearOther and nearSingInt
+    with tEqualS false, matlab/capsules_py.m:194-467,
+    matlab/poten_py.m:495-692), h = the source group's min length / N.
+    ``near`` is "matlab" or "none"; no viscosity contrast, repulsion or walls.
+    """
+
+    def __init__(self, Xs, options, prams, near: str = "matlab", farfield_precision: str = "fp32c",
+                 sl_precision: str = "fp32c", device=None):
+        if near not in ("matlab", "none"):
+            raise NotImplementedError("TStepBiemMixed: near must be 'matlab' or 'none'")
+        if not 1 <= len(Xs) <= 4:
+            raise ValueError("TStepBiemMixed: 1 to 4 groups")
+        if options.get("repulsion", False):
+            raise NotImplementedError("TStepBiemMixed: no repulsion between groups")
+        self.groups = [TStepBiem(X, None, options, prams, near=near, farfield_precision=farfield_precision,
+                                 sl_precision=sl_precision, device=device) for X in Xs]
+        if any(g._visc is not None for g in self.groups):
+            raise NotImplementedError("TStepBiemMixed: no viscosity contrast")
+        if any(g.nv < 1 for g in self.groups):
+            raise ValueError("TStepBiemMixed: every group needs a vesicle")
+        self.device = self.groups[0].device
+        self.last = None
+
+    def _arrays(self):
+        ng = len(self.groups)
+        ctxs = (ctypes.c_void_p * ng)(*[g._ctx.handle for g in self.groups])
+        nvs = (ctypes.c_int * ng)(*[g.nv for g in self.groups])
+        return ng, ctxs, nvs
+
+    def workspace_bytes(self) -> int:
+        ng, ctxs, nvs = self._arrays()
+        p = self.groups[0].params()
+        lib = self.groups[0]._ctx.lib
+        return int(lib.ves_biem_step_mixed_workspace(ng, ctypes.cast(ctxs, ctypes.c_void_p), ctypes.byref(p),
+                                                     ctypes.cast(nvs, ctypes.c_void_p)))
+
+    def time_step(self, Xs, sigs):
+        """-> (list of X, list of sigma, iter, iflag); ``iter`` counts the
+        operator applications plus one, as TStepBiem.time_step."""
+        ng, ctxs, nvs = self._arrays()
+        p = self.groups[0].params()
+        lib = self.groups[0]._ctx.lib
+        Xv = [to_vm(as_device_f64(X, self.device)) for X in Xs]
+        sv = [to_vm(as_device_f64(s, self.device)) for s in sigs]
+        for g, X, sg in zip(self.groups, Xv, sv):
+            if X.shape != (g.nv, 2 * g.N) or sg.shape != (g.nv, g.N):
+                raise ValueError("TStepBiemMixed.time_step: group shapes changed")
+        Xo = [torch.empty_like(X) for X in Xv]
+        so = [torch.empty_like(s) for s in sv]
+
+        def ptrs(ts):
+            return ctypes.cast((ctypes.c_void_p * ng)(*[t.data_ptr() for t in ts]), ctypes.c_void_p)
+
+        nbytes = self.workspace_bytes()
+        if nbytes == 0:
+            nat.check(nat.VES_ERR_ARG, "time_step (mixed): workspace query")
+        ws = self.groups[0]._ctx.workspace(nbytes)
+        res = nat.StepResult()
+        rc = lib.ves_biem_step_mixed(ng, ctypes.cast(ctxs, ctypes.c_void_p), ctypes.byref(p),
+                                     ctypes.cast(nvs, ctypes.c_void_p), ptrs(Xv), ptrs(sv), ptrs(Xo), ptrs(so),
+                                     ctypes.byref(res), ws.data_ptr(), ws.numel(), nat.stream_ptr(self.device))
+        if rc not in (nat.VES_OK, nat.VES_ERR_GMRES_MAXIT):
+            nat.check(rc, "time_step (mixed)")
+        self.last = res
+        return [from_vm(X) for X in Xo], [from_vm(s) for s in so], res.matvecs + 1, res.info != 0

@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-net-timing", action="store_true", help="skip the per-network forward timings")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="fixed launch shapes for the network kernels (no timing of the shapes on the first step)")
     ap.add_argument("--only-net", default=None, help="time one network's forward pass at --nv and exit "
                     "(relax, adv, near, selften, advten)")
     return ap.parse_args()
@@ -230,7 +232,7 @@ def run_mlarm(a, dev, X0, state_dicts):
     m = MLARM_manyfree_py(STEP["dt"], vinf, Curve(), False, 1e2, -1, nrm["adv_in"], nrm["adv_out"],
                           nrm["relax_in"], nrm["relax_out"], nrm["near_in"], nrm["near_out"], nrm["selften_in"],
                           nrm["selften_out"], nrm["advten_in"], nrm["advten_out"], dev, state_dicts=state_dicts,
-                          net_precision=a.nets, farfield_precision=a.precision)
+                          net_precision=a.nets, farfield_precision=a.precision, autotune=not a.no_autotune)
     Xd = torch.tensor(X0, dtype=torch.float64, device=dev)
     _, area0, len0 = Curve().geomProp(Xd)
     m.area0, m.len0 = area0, len0
@@ -454,6 +456,7 @@ def run_gb300(a, rank, world):
                         f"nv={a.nv}, N={a.N}, Nup=1536, unit-length vesicles of reduced area 0.65, area fraction "
                         f"{a.area_fraction}, shear rate 2, dt=1e-5",
             "networks": a.nets, "farfield_precision": a.precision,
+            "network_autotune": not a.no_autotune,
             "l2": "inputs larger than L2 (network activations 11 GB, upsampled sources 50 MB x 2 + near lists, "
                   "per step)",
             "parallelism": "replicas only" if world > 1 else "single GPU",
@@ -523,7 +526,7 @@ def run_only_net(a):
     from ves2dpy_gb300.mlarm_weights import NETS, synthetic_state_dict
     dev = torch.device("cuda", 0)
     spec = NETS[a.only_net]
-    net = Network(a.only_net, synthetic_state_dict(a.only_net, 0), a.nets, dev)
+    net = Network(a.only_net, synthetic_state_dict(a.only_net, 0), a.nets, dev, autotune=not a.no_autotune)
     x = torch.randn(a.nv, spec.rep * spec.cin, spec.L, device=dev, dtype=net.dtype)
     net(x)
     e0, e1 = _events()

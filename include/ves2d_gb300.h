@@ -360,6 +360,15 @@ VES_API int ves_net_info(const ves_net* net, int* precision, int* groups, int* l
 VES_API int ves_net_forward(const ves_net* net, int nv, const void* in, void* out, void* ws, size_t ws_bytes,
                             void* stream);
 VES_API size_t ves_net_forward_workspace(const ves_net* net, int nv);
+/* Autotuner of the BF16 tensor-core network (VES_NET_BF16; no effect on
+ * the other precisions).  With on != 0, the first forward pass at each
+ * vesicle count times every launch shape that fits of each block's three
+ * kernels (warp groups per CTA; M = 64 MMAs for layers of at most 64
+ * positions on or off) on that call's input, synchronising the stream, and
+ * keeps the fastest for later passes at that count.  Results do not depend
+ * on the shape.  Concurrent first passes of one network must be serialised
+ * by the caller. */
+VES_API int ves_net_set_autotune(ves_net* net, int on);
 
 /* ---- MLARM step (newtorch/wrapper_MLARM_batch_compile_N128.py) ------------- */
 /* Normalisation constants of the five networks, host FP64, the shapes the

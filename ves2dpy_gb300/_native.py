@@ -187,6 +187,7 @@ SIGNATURES = {
     "ves_biem_step_mixed_workspace": (_SZ, [_I, _P, ctypes.POINTER(StepParams), _P]),
     "ves_redistribute_arclength": (_I, [_P, _I, _P, _P, _P, ctypes.POINTER(_I), _P, _SZ, _P]),
     "ves_redistribute_arclength_workspace": (_SZ, [_P, _I]),
+    "ves_net_set_autotune": (_I, [_P, _I]),
     "ves_net_create": (_I, [_I, _I, _I, _I, ctypes.POINTER(NetBlock), ctypes.POINTER(ctypes.c_void_p),
                             ctypes.POINTER(_P)]),
     "ves_net_destroy": (_I, [_P]),

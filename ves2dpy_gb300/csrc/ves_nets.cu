@@ -202,6 +202,7 @@ struct ves_net {
   unsigned char* d_tc = nullptr;
   int mid_max = 0;
   VesDeviceStatus* d_status = nullptr;
+  int autotune = 0;             // tensor-core path: time the launch shapes on the first call per nv
 };
 
 namespace {
@@ -297,7 +298,7 @@ int net_forward_t(const ves_net* net, int nv, const Real* in, Real* out, WsCarve
       const TcBlock& tb = net->tcb[bi];
       rc = tcnet_run_block(tb, net->groups, nv, net->d_tc + tb.down_off, net->d_tc + tb.up1_off, net->d_tc + tb.up2_off,
                            reinterpret_cast<const float*>(src), reinterpret_cast<float*>(dst), mid,
-                           st ? st : net->d_status, s);
+                           st ? st : net->d_status, s, net->autotune != 0);
     } else {
       rc = run_block<Real>(net, bi, nv, src, dst, s);
     }
@@ -458,6 +459,12 @@ extern "C" int ves_net_destroy(ves_net* net) {
   if (net->d_tc) cudaFree(net->d_tc);
   if (net->d_status) cudaFree(net->d_status);
   delete net;
+  return VES_OK;
+}
+
+extern "C" int ves_net_set_autotune(ves_net* net, int on) {
+  if (!net) return VES_ERR_ARG;
+  net->autotune = on ? 1 : 0;
   return VES_OK;
 }
 

@@ -33,6 +33,7 @@
 // for its MMAs the others run their epilogues.  Splitting the transposed
 // convs over two kernels keeps each weight image small enough for that.
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -1064,9 +1065,48 @@ static int tcnet_down_groups_max() {
   return v;
 }
 
+namespace {
+
+// compiled chunk-count variants; others run the generic kernels
+void (*pick_down(int kc1, int kcd, int ng))(tcnet::KArgs) {
+  using namespace tcnet;
+#define VES_DK(A, B) return ng == 4 ? down_kernel<A, B, 4> : (ng == 3 ? down_kernel<A, B, 3> : down_kernel<A, B, 2>)
+  if (kc1 == 4 && kcd == 6) VES_DK(4, 6);
+  if (kc1 == 6 && kcd == 6) VES_DK(6, 6);
+  if (kc1 == 6 && kcd == 8) VES_DK(6, 8);
+  if (kc1 == 8 && kcd == 8) VES_DK(8, 8);
+  VES_DK(0, 0);
+#undef VES_DK
+}
+
+void (*pick_up1(int kcd, int ng))(tcnet::KArgs) {
+  using namespace tcnet;
+  if (kcd == 6) return ng == 4 ? up1_kernel<6, 4> : up1_kernel<6, 2>;
+  if (kcd == 8) return ng == 4 ? up1_kernel<8, 4> : up1_kernel<8, 2>;
+  return ng == 4 ? up1_kernel<0, 4> : up1_kernel<0, 2>;
+}
+
+void (*pick_up2(int kcd, int ng))(tcnet::KArgs) {
+  using namespace tcnet;
+  if (kcd == 6) return ng == 3 ? up2_kernel<6, 3> : up2_kernel<6, 2>;
+  if (kcd == 8) return ng == 3 ? up2_kernel<8, 3> : up2_kernel<8, 2>;
+  return ng == 3 ? up2_kernel<0, 3> : up2_kernel<0, 2>;
+}
+
+bool autotune_log() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = getenv("VES_TC_AUTOTUNE_LOG");
+    v = (e && atoi(e)) ? 1 : 0;
+  }
+  return v != 0;
+}
+
+}  // namespace
+
 int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_down, const unsigned char* d_up1,
                     const unsigned char* d_up2, const float* x, float* out, unsigned char* mid, VesDeviceStatus* st,
-                    cudaStream_t s) {
+                    cudaStream_t s, bool autotune) {
   using namespace tcnet;
   // the block input and the intermediates are fetched by 16-byte bulk copies
   if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(mid)) & 15u) {
@@ -1078,7 +1118,7 @@ int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_dow
   const Geo& g = a.g;
   a.G = G;
   a.nv = nv;
-  a.m64 = tcnet_m64() ? 1 : 0;
+  a.m64 = 0;
   a.items = (long long)G * nv;
   a.x = x;
   a.out = out;
@@ -1088,48 +1128,107 @@ int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_dow
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const int kc1 = g.kc1, kcd = g.kcd, Nd = kcd * 8;
-  // warp groups per CTA: as many as TMEM (512 columns) and shared memory allow
+  // warp groups per CTA that fit: TMEM (512 columns) and shared memory
   const int down3 = g.dxs + 3 * g.dgrp + kTail, down4 = g.dxs + 4 * g.dgrp + kTail,
             up1_4 = g.u1size + 4 * g.u1grp + kTail, up2_3 = g.u2size + 3 * g.u2grp + kTail;
-  const bool dn3 = (kc1 + kcd) * 8 <= 128 && down3 <= kMaxSmem && tcnet_down_groups_max() >= 3;
-  const bool dn4 = dn3 && down4 <= kMaxSmem && tcnet_down_groups_max() >= 4;
+  const bool dn3 = (kc1 + kcd) * 8 <= 128 && down3 <= kMaxSmem;
+  const bool dn4 = dn3 && down4 <= kMaxSmem;
   const bool u14 = 2 * Nd <= 128 && up1_4 <= kMaxSmem;
   const bool u23 = 2 * Nd + (g.L / 128) * rup(g.cmix, 16) <= 160 && up2_3 <= kMaxSmem;
-  // compiled chunk-count variants; others run the generic kernels
-  void (*dk)(KArgs) = dn4 ? down_kernel<0, 0, 4> : (dn3 ? down_kernel<0, 0, 3> : down_kernel<0, 0, 2>);
-  void (*k1)(KArgs) = u14 ? up1_kernel<0, 4> : up1_kernel<0, 2>;
-  void (*k2)(KArgs) = u23 ? up2_kernel<0, 3> : up2_kernel<0, 2>;
-#define VES_DK4(A, B) dk = dn4 ? down_kernel<A, B, 4> : (dn3 ? down_kernel<A, B, 3> : down_kernel<A, B, 2>)
-  if (kc1 == 4 && kcd == 6) VES_DK4(4, 6);
-  if (kc1 == 6 && kcd == 6) VES_DK4(6, 6);
-  if (kc1 == 6 && kcd == 8) VES_DK4(6, 8);
-  if (kc1 == 8 && kcd == 8) VES_DK4(8, 8);
-#undef VES_DK4
-  if (kcd == 6) {
-    k1 = u14 ? up1_kernel<6, 4> : up1_kernel<6, 2>;
-    k2 = u23 ? up2_kernel<6, 3> : up2_kernel<6, 2>;
-  }
-  if (kcd == 8) {
-    k1 = u14 ? up1_kernel<8, 4> : up1_kernel<8, 2>;
-    k2 = u23 ? up2_kernel<8, 3> : up2_kernel<8, 2>;
-  }
-  const int ng_d = dn4 ? 4 : (dn3 ? 3 : 2), ng_1 = u14 ? 4 : 2, ng_2 = u23 ? 3 : 2;
+  const int grid = (int)std::min<long long>(a.items, (long long)nsm);
   // one CTA per SM (it allocates all 512 TMEM columns): at least 117 KB of
   // shared memory per CTA keeps a second one off the SM
-  const int sm_d = std::max(g.dxs + ng_d * g.dgrp + kTail, kMinSmem);
-  const int sm_1 = std::max(g.u1size + ng_1 * g.u1grp + kTail, kMinSmem);
-  const int sm_2 = std::max(g.u2size + ng_2 * g.u2grp + kTail, kMinSmem);
-  int rc = ves_cuda_status(cudaFuncSetAttribute(dk, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_d), "tc down smem");
-  if (!rc) rc = ves_cuda_status(cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_1), "tc up1 smem");
-  if (!rc) rc = ves_cuda_status(cudaFuncSetAttribute(k2, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_2), "tc up2 smem");
-  if (rc) return rc;
-  const int grid = (int)std::min<long long>(a.items, (long long)nsm);
-  ves_count_launch(3);
-  a.img = d_down;
-  dk<<<grid, ng_d * kGroupThreads, sm_d, s>>>(a);
-  a.img = d_up1;
-  k1<<<grid, ng_1 * kGroupThreads, sm_1, s>>>(a);
-  a.img = d_up2;
-  k2<<<grid, ng_2 * kGroupThreads, sm_2, s>>>(a);
-  return ves_launch_check("tc net block");
+  auto launch = [&](int which, int ng, int m64) -> int {
+    KArgs b = a;
+    b.m64 = m64;
+    void (*fn)(KArgs);
+    int smem;
+    if (which == 0) {
+      fn = pick_down(kc1, kcd, ng);
+      smem = std::max(g.dxs + ng * g.dgrp + kTail, kMinSmem);
+      b.img = d_down;
+    } else if (which == 1) {
+      fn = pick_up1(kcd, ng);
+      smem = std::max(g.u1size + ng * g.u1grp + kTail, kMinSmem);
+      b.img = d_up1;
+    } else {
+      fn = pick_up2(kcd, ng);
+      smem = std::max(g.u2size + ng * g.u2grp + kTail, kMinSmem);
+      b.img = d_up2;
+    }
+    int rc = ves_cuda_status(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                             "tc smem attribute");
+    if (rc) return rc;
+    ves_count_launch();
+    fn<<<grid, ng * kGroupThreads, smem, s>>>(b);
+    return ves_launch_check("tc net block");
+  };
+  // the fixed rule: the most warp groups that fit, M = 64 MMAs where allowed
+  const int m64_default = tcnet_m64() ? 1 : 0;
+  const int dmax = tcnet_down_groups_max();
+  TcPlan plan{nv, (dn4 && dmax >= 4) ? 4 : ((dn3 && dmax >= 3) ? 3 : 2), m64_default, u14 ? 4 : 2, m64_default,
+              u23 ? 3 : 2};
+  const TcPlan* found = nullptr;
+  for (const TcPlan& p : tb.plans)
+    if (p.nv == nv) found = &p;
+  if (found) {
+    plan = *found;
+  } else if (autotune) {
+    cudaEvent_t e0, e1;
+    int rc = ves_cuda_status(cudaEventCreate(&e0), "tune event");
+    if (!rc) rc = ves_cuda_status(cudaEventCreate(&e1), "tune event");
+    if (rc) return rc;
+    auto timed = [&](int which, int ng, int m64, float& ms) -> int {
+      ms = 1e30f;
+      for (int rep = 0; rep < 2; ++rep) {
+        int r = ves_cuda_status(cudaEventRecord(e0, s), "tune record");
+        if (!r) r = launch(which, ng, m64);
+        if (!r) r = ves_cuda_status(cudaEventRecord(e1, s), "tune record");
+        if (!r) r = ves_cuda_status(cudaEventSynchronize(e1), "tune sync");
+        float t = 0.f;
+        if (!r) r = ves_cuda_status(cudaEventElapsedTime(&t, e0, e1), "tune elapsed");
+        if (r) return r;
+        ms = std::min(ms, t);
+      }
+      return VES_OK;
+    };
+    float best = 1e30f, t = 0.f;
+    // each kernel in the order the block runs them, so that the next one reads a valid input
+    const int ngd[3] = {2, 3, 4};
+    for (int i = 0; i < 3 && !rc; ++i) {
+      const int ng = ngd[i];
+      if ((ng == 3 && !dn3) || (ng == 4 && !dn4)) continue;
+      for (int m = 0; m < 2 && !rc; ++m) {
+        if ((rc = timed(0, ng, m, t))) break;
+        if (t < best) best = t, plan.ng_down = ng, plan.m64_down = m;
+      }
+    }
+    if (!rc) rc = launch(0, plan.ng_down, plan.m64_down);
+    best = 1e30f;
+    for (int ng = 2; ng <= 4 && !rc; ng += 2) {
+      if (ng == 4 && !u14) continue;
+      for (int m = 0; m < 2 && !rc; ++m) {
+        if ((rc = timed(1, ng, m, t))) break;
+        if (t < best) best = t, plan.ng_up1 = ng, plan.m64_up1 = m;
+      }
+    }
+    if (!rc) rc = launch(1, plan.ng_up1, plan.m64_up1);
+    best = 1e30f;
+    for (int ng = 2; ng <= 3 && !rc; ++ng) {
+      if (ng == 3 && !u23) continue;
+      if ((rc = timed(2, ng, 0, t))) break;
+      if (t < best) best = t, plan.ng_up2 = ng;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    tb.plans.push_back(plan);
+    if (autotune_log())
+      fprintf(stderr, "tcnet autotune: L=%d kc1=%d kcd=%d nv=%d -> down %d groups m64 %d, up1 %d groups m64 %d, up2 %d groups\n",
+              g.L, kc1, kcd, nv, plan.ng_down, plan.m64_down, plan.ng_up1, plan.m64_up1, plan.ng_up2);
+  }
+  int rc = launch(0, plan.ng_down, plan.m64_down);
+  if (!rc) rc = launch(1, plan.ng_up1, plan.m64_up1);
+  if (!rc) rc = launch(2, plan.ng_up2, 0);
+  return rc;
 }

@@ -36,9 +36,11 @@ def load_state_dict(path: str):
 
 class Network:
     """One network on the device (``ves_net``), built from a state dict in the
-    reference's parameter naming."""
+    reference's parameter naming.  ``autotune`` (BF16 tensor-core networks):
+    the first forward pass at each vesicle count times the launch shapes of
+    every block and keeps the fastest (ves_net_set_autotune)."""
 
-    def __init__(self, name: str, state_dict, precision: str = "fp32", device=None):
+    def __init__(self, name: str, state_dict, precision: str = "fp32", device=None, autotune: bool = True):
         self.name = name
         self.spec = NETS[name]
         self.precision = precision
@@ -61,6 +63,8 @@ class Network:
                                          blocks, ptrs, ctypes.byref(h)), f"ves_net_create({name})")
         self.handle = h
         self._ws = None
+        if autotune and precision == "bf16":
+            nat.check(lib.ves_net_set_autotune(h, 1), f"ves_net_set_autotune({name})")
 
     def forward(self, x: torch.Tensor) -> torch.Tensor:
         """model(x) for x of shape (nv, rep*cin, L) on the device."""
@@ -97,9 +101,10 @@ class MLARM_manyfree_py:
     reference's TorchScript files under ``model_dir``), ``net_precision``
     ("fp32", the reference networks' type, "fp64", or "bf16" on the tensor
     cores), ``farfield_precision``
-    ("fp32c" or "fp64") and ``eval_near_net`` (evaluate the near-field
+    ("fp32c" or "fp64"), ``eval_near_net`` (evaluate the near-field
     network as the reference does; its output enters the step only through
-    the repulsion force).
+    the repulsion force) and ``autotune`` (launch shapes of the BF16 network
+    kernels timed on the first step at each vesicle count).
     """
 
     def __init__(self, dt, vinf, oc, use_repulsion, repStrength, rbf_upsample: int,
@@ -107,7 +112,7 @@ class MLARM_manyfree_py:
                  nearNetInputNorm, nearNetOutputNorm, tenSelfNetInputNorm, tenSelfNetOutputNorm,
                  tenAdvNetInputNorm, tenAdvNetOutputNorm, device, logger=None, *, state_dicts=None,
                  model_dir: str = "../trained/torch_script_models", net_precision: str = "fp32",
-                 farfield_precision: str = "fp32c", eval_near_net: bool = True):
+                 farfield_precision: str = "fp32c", eval_near_net: bool = True, autotune: bool = True):
         if use_repulsion:
             raise NotImplementedError("MLARM_manyfree_py: repulsion is not supported")
         self.dt = float(dt)
@@ -141,7 +146,7 @@ class MLARM_manyfree_py:
         if state_dicts is None:
             state_dicts = {n: load_state_dict(os.path.join(model_dir, MODEL_FILES[n])) for n in NETS}
         with torch.cuda.device(self.device):
-            self.nets = {n: Network(n, state_dicts[n], net_precision, self.device) for n in NETS}
+            self.nets = {n: Network(n, state_dicts[n], net_precision, self.device, autotune=autotune) for n in NETS}
         self.ctx = nat.context(128, self.device)
         lib = self.ctx.lib
         self.lib = lib

@@ -64,6 +64,74 @@ __global__ void __launch_bounds__(256) bgemm_kernel(int M, int N, int K, T alpha
   }
 }
 
+// FP32 variant for aligned shapes: 128x128 tiles, K steps of 8, 8x8 outputs
+// per thread (rows ty*4+i and 64+ty*4+i, columns tx*4+j and 64+tx*4+j), 16-byte
+// operand loads.  Needs K % 8 == 0, N % 4 == 0, lda/ldb/sA/sB multiples of 4
+// and 16-byte aligned A and B.
+__global__ void __launch_bounds__(256) bgemm128_f32_kernel(int M, int N, int K, float alpha,
+                                                           const float* __restrict__ A, int lda, long long sA,
+                                                           const float* __restrict__ B, int ldb, long long sB,
+                                                           float beta, float* __restrict__ C, int ldc,
+                                                           long long sC) {
+  constexpr int TK = 8, LDS = 132;  // padded rows: the transposed A stores are conflict-free
+  __shared__ __align__(16) float As[TK][LDS];
+  __shared__ __align__(16) float Bs[TK][LDS];
+  const long long b = blockIdx.z;
+  const float* Ab = A + b * sA;
+  const float* Bb = B + b * sB;
+  float* Cb = C + b * sC;
+  const int row0 = blockIdx.y * 128, col0 = blockIdx.x * 128;
+  const int t = threadIdx.x, tx = t % 16, ty = t / 16;
+  // load assignments: A row t/2, k chunk (t%2)*4; B row t/32, columns (t%32)*4
+  const int ar = t >> 1, ak = (t & 1) * 4;
+  const int bk = t >> 5, bc = (t & 31) * 4;
+  const bool arow_ok = row0 + ar < M;
+  const bool bcol_ok = col0 + bc < N;  // N % 4 == 0: the whole float4 is in range
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+  for (int k0 = 0; k0 < K; k0 += TK) {
+    const float4 av = arow_ok ? *reinterpret_cast<const float4*>(Ab + (long long)(row0 + ar) * lda + k0 + ak)
+                              : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 bv = bcol_ok ? *reinterpret_cast<const float4*>(Bb + (long long)(k0 + bk) * ldb + col0 + bc)
+                              : make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+    As[ak + 0][ar] = av.x;
+    As[ak + 1][ar] = av.y;
+    As[ak + 2][ar] = av.z;
+    As[ak + 3][ar] = av.w;
+    *reinterpret_cast<float4*>(&Bs[bk][bc]) = bv;
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < TK; ++kk) {
+      const float4 a0 = *reinterpret_cast<const float4*>(&As[kk][ty * 4]);
+      const float4 a1 = *reinterpret_cast<const float4*>(&As[kk][64 + ty * 4]);
+      const float4 b0 = *reinterpret_cast<const float4*>(&Bs[kk][tx * 4]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&Bs[kk][64 + tx * 4]);
+      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(a[i], bb[j], acc[i][j]);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int gr = row0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + i - 4);
+    if (gr >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int gc = col0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + j - 4);
+      if (gc >= N) continue;
+      float* cp = Cb + (long long)gr * ldc + gc;
+      *cp = (beta == 0.f) ? alpha * acc[i][j] : fmaf(alpha, acc[i][j], beta * *cp);
+    }
+  }
+}
+
 template <typename T>
 static void bgemm_launch(int batch, int M, int N, int K, T alpha, const T* A, int lda, long long sA,
                          const T* B, int ldb, long long sB, T beta, T* C, int ldc, long long sC,
@@ -85,7 +153,19 @@ void launch_bgemm_f64(int batch, int M, int N, int K, double alpha, const double
 void launch_bgemm_f32(int batch, int M, int N, int K, float alpha, const float* A, int lda,
                       long long sA, const float* B, int ldb, long long sB, float beta, float* C,
                       int ldc, long long sC, cudaStream_t s) {
-  bgemm_launch<float>(batch, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, s);
+  const bool aligned = K % 8 == 0 && N % 4 == 0 && lda % 4 == 0 && ldb % 4 == 0 && sA % 4 == 0 && sB % 4 == 0 &&
+                       ((reinterpret_cast<uintptr_t>(A) | reinterpret_cast<uintptr_t>(B)) & 15u) == 0;
+  if (!aligned || M < 64) {
+    bgemm_launch<float>(batch, M, N, K, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, s);
+    return;
+  }
+  for (int b0 = 0; b0 < batch; b0 += 65535) {
+    const int nb = batch - b0 < 65535 ? batch - b0 : 65535;
+    dim3 grid(ceil_div(N, 128), ceil_div(M, 128), nb);
+    ves_count_launch();
+    bgemm128_f32_kernel<<<grid, 256, 0, s>>>(M, N, K, alpha, A + b0 * sA, lda, sA, B + b0 * sB, ldb, sB, beta,
+                                             C + b0 * sC, ldc, sC);
+  }
 }
 
 // ----------------------------------------------------------------------------

@@ -62,3 +62,26 @@ def test_cross_zone_matches_single_set_zone():
     want = sorted((src.index(e.k1), tar.index(e.k2), e.j, e.icp) for e in ent if e.k1 in src and e.k2 in tar)
     got = sorted((e.k1, e.k2, e.j, e.icp) for e in cross)
     assert got == want and len(got) > 0
+
+
+def test_mixed_step_argument_checks():
+    """Host-side checks of the multi-group stepper (no device needed)."""
+    import ctypes
+
+    import pytest
+
+    from ves2dpy_gb300 import _native as nat
+    from ves2dpy_gb300.tstep_biem import TStepBiemMixed
+    X = small_suspension()
+    prams = dict(dt=1e-4, kappa=1.0, gmresTol=1e-10, gmresMaxIter=200)
+    with pytest.raises(NotImplementedError):
+        TStepBiemMixed([X, X], {}, prams, near="py_hh")
+    with pytest.raises(ValueError):
+        TStepBiemMixed([X] * 5, {}, prams)
+    with pytest.raises(NotImplementedError):
+        TStepBiemMixed([X, X], {"repulsion": True}, prams)
+    # the C entry point rejects a bad group count without touching a device
+    lib = nat.load_library()
+    p = nat.StepParams()
+    assert lib.ves_biem_step_mixed_workspace(0, None, ctypes.byref(p), None) == 0
+    assert lib.ves_biem_step_mixed_workspace(5, None, ctypes.byref(p), None) == 0

@@ -3,6 +3,7 @@
 // stencil held in shared memory, which is the exact operator the reference
 // applies through torch.fft (curve_batch_compile.py:379-423, 1188-1200).
 #include "ves_internal.h"
+#include "ves_fft.cuh"
 
 // y[j] = sum_l d[(j - l) mod n] * a[l]   (a, d in shared memory)
 __device__ __forceinline__ double circ_apply(const double* __restrict__ d, const double* __restrict__ a,
@@ -39,12 +40,75 @@ __global__ void upsample_kernel(int N, int Nup, int m, const double* __restrict_
   }
 }
 
+// interpft N -> Nup of both components of a vesicle at once, as filter.py
+// interpft does it (fft, zero-padded spectrum, ifft, times Nup/N): z = x + i y,
+// FFT of length N, the Nyquist mode split in half between +N/2 and -N/2 (the
+// real part of the reference's one-sided placement, so both components stay
+// real), inverse FFT of length Nup, divided by N.
+__global__ void __launch_bounds__(256) upsample_fft_kernel(int N, int Nup, const double* __restrict__ cosU,
+                                                           const double* __restrict__ sinU,
+                                                           const double* __restrict__ in, long long in_stride,
+                                                           double* __restrict__ out) {
+  extern __shared__ double sh[];
+  double* zr = sh;
+  double* zi = zr + Nup;
+  double* tre = zi + Nup;
+  double* tim = tre + Nup;
+  const int k = blockIdx.x;
+  const double* src = in + (long long)k * in_stride;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    zr[i] = src[i];
+    zi[i] = src[N + i];
+  }
+  ves_fft(zr, zi, tre, tim, N, cosU, sinU, -1, Nup / N);
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    tre[i] = zr[i];
+    tim[i] = zi[i];
+  }
+  __syncthreads();
+  const int h = N / 2, top = Nup - N;
+  for (int u = threadIdx.x; u < Nup; u += blockDim.x) {
+    double vr = 0.0, vi = 0.0;
+    if (u < h) {
+      vr = tre[u];
+      vi = tim[u];
+    } else if (u == h || u == Nup - h) {
+      vr = 0.5 * tre[h];
+      vi = 0.5 * tim[h];
+    } else if (u > Nup - h) {
+      vr = tre[u - top];
+      vi = tim[u - top];
+    }
+    zr[u] = vr;
+    zi[u] = vi;
+  }
+  ves_fft(zr, zi, tre, tim, Nup, cosU, sinU, +1);
+  const double inv = 1.0 / N;
+  double* dst = out + (long long)k * 2 * Nup;
+  for (int u = threadIdx.x; u < Nup; u += blockDim.x) {
+    dst[u] = zr[u] * inv;
+    dst[Nup + u] = zi[u] * inv;
+  }
+}
+
 void launch_upsample(const ves_ctx* c, int nv, int ncomp, const double* in, long long in_stride,
                      double* out, cudaStream_t s) {
   if (nv <= 0) return;
-  size_t sh = (size_t)(c->N + c->Nup) * sizeof(double);
+  const int N = c->N, Nup = c->Nup;
+  if (ncomp == 2 && in_stride == 2LL * N && N % 2 == 0 && Nup > N && ves_fft_size_ok(N) && ves_fft_size_ok(Nup)) {
+    const size_t shf = (size_t)4 * Nup * sizeof(double);
+    if (shf > 48 * 1024 &&
+        cudaFuncSetAttribute(upsample_fft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shf) != cudaSuccess) {
+      cudaGetLastError();  // the dense sums below need no opt-in
+    } else {
+      ves_count_launch();
+      upsample_fft_kernel<<<nv, 256, shf, s>>>(N, Nup, c->cosU, c->sinU, in, in_stride, out);
+      return;
+    }
+  }
+  size_t sh = (size_t)(N + Nup) * sizeof(double);
   ves_count_launch();
-  upsample_kernel<<<nv * ncomp, 256, sh, s>>>(c->N, c->Nup, c->m, c->pc, ncomp, in, in_stride, out);
+  upsample_kernel<<<nv * ncomp, 256, sh, s>>>(N, Nup, c->m, c->pc, ncomp, in, in_stride, out);
 }
 
 // Xup, its parametric derivative and the upsampled jacobian sa_up = |dXup|,

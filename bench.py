@@ -29,6 +29,7 @@ import math
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -163,12 +164,14 @@ def cpu_estimates(a, state_dicts, biem_matvecs):
 
 # ---------------------------------------------------------------------------
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling during the timed region (raw samples written to
+    $VES_CLOCKS_DIR, default the system temporary directory)."""
 
     def __init__(self, index=0):
         self.proc = None
         self.index = index
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.path = os.path.join(os.environ.get("VES_CLOCKS_DIR", tempfile.gettempdir()),
+                                 f"clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         try:

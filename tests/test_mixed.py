@@ -85,3 +85,26 @@ def test_mixed_step_argument_checks():
     p = nat.StepParams()
     assert lib.ves_biem_step_mixed_workspace(0, None, ctypes.byref(p), None) == 0
     assert lib.ves_biem_step_mixed_workspace(5, None, ctypes.byref(p), None) == 0
+
+
+def test_mixed_suspension_generator():
+    """Groups keep their point counts; every pair of curves keeps the gap;
+    centres lie in the rectangle sized for the area fraction; the reduced
+    areas spread over the requested range."""
+    import math
+
+    from ves2dpy_gb300.suspension import mixed_suspension
+    groups = [(24, 16), (6, 32)]
+    Xs = mixed_suspension(groups, 0.2, box_aspect=2.0, min_gap=0.05, reduced_area=(0.6, 0.9), seed=3)
+    assert [X.shape for X in Xs] == [(2 * N, nv) for nv, N in groups]
+    curves = [(X[: X.shape[0] // 2, k], X[X.shape[0] // 2:, k]) for X in Xs for k in range(X.shape[1])]
+    gap = min(np.sqrt(((xa[:, None] - xb[None, :]) ** 2 + (ya[:, None] - yb[None, :]) ** 2).min())
+              for i, (xa, ya) in enumerate(curves) for (xb, yb) in curves[i + 1:])
+    assert gap >= 0.05
+    Ly = math.sqrt(30 * math.pi / 0.2 / 2.0)
+    cy = np.array([c[1].mean() for c in curves])
+    assert np.abs(cy).max() <= 0.5 * Ly + 2.0
+    # base ellipses drawn with reduced areas in [0.6, 0.9]; the k = 2..8
+    # perturbation moves the measured value by a few hundredths
+    ra = np.concatenate([O.geom_prop(X)[0] for X in Xs])
+    assert np.ptp(ra) > 0.2 and ra.min() > 0.45 and ra.max() < 1.0

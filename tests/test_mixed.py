@@ -108,3 +108,22 @@ def test_mixed_suspension_generator():
     # perturbation moves the measured value by a few hundredths
     ra = np.concatenate([O.geom_prop(X)[0] for X in Xs])
     assert np.ptp(ra) > 0.2 and ra.min() > 0.45 and ra.max() < 1.0
+
+
+def test_mixed_oracle_three_groups_reduce_to_single_n():
+    """Three one-N groups (each holding a vesicle of the minimum length) give the single-N step."""
+    X = small_suspension(nv=5, seed=1)
+    N = X.shape[0] // 2
+    k = int(np.argmin(O.geom_prop(X)[2]))
+    groups = [X[:, :2], X[:, 2:4], X[:, 4:]]
+    for g in range(3):
+        if not any(np.array_equal(X[:, k], groups[g][:, j]) for j in range(groups[g].shape[1])):
+            far = X[:, k:k + 1].copy()
+            far[:N] += 40.0 * (g + 1)
+            groups[g] = np.concatenate([groups[g], far], axis=1)
+    U = np.concatenate(groups, axis=1)
+    prm = O.StepParams(dt=1e-4, speed=2.0, near="matlab")
+    ref = O.time_step(U, np.zeros((N, U.shape[1])), prm)
+    Xo, so, it, info = O.time_step_mixed(groups, [np.zeros((N, G.shape[1])) for G in groups], prm)
+    assert info == 0 and it == ref.iters
+    assert np.abs(np.concatenate(Xo, axis=1) - ref.X).max() < 1e-12 * np.abs(ref.X).max()

@@ -80,6 +80,14 @@ VES_API int ves_ctx_create(int N, ves_ctx** out);
 VES_API int ves_ctx_destroy(ves_ctx* ctx);
 /* N, Nup = N*ceil(sqrt(N)) (poten.py:24), number of Alpert nodes */
 VES_API int ves_ctx_info(const ves_ctx* ctx, int* N, int* Nup, int* nquad);
+/* Largest number of near-pair candidates (source vesicles whose box comes
+ * within the near threshold of one target vesicle's box) met by the near-zone
+ * builds since the last call on this context began; the capacity
+ * (ves_near_lists.maxc, ves_step_params.maxc, ves_mlarm_params.maxc) a
+ * caller needs after VES_ERR_NEARLIST_OVERFLOW.  The reference's
+ * naiveNearZoneInfo (biem_support.py:520-613) has no capacity; the device
+ * lists have one and report the size they need instead of truncating. */
+VES_API int ves_ctx_max_candidates(const ves_ctx* ctx);
 /* Text of the last error recorded on this thread (never NULL). */
 VES_API const char* ves_last_error(void);
 

@@ -158,6 +158,7 @@ SIGNATURES = {
     "ves_ctx_create": (_I, [_I, ctypes.POINTER(_P)]),
     "ves_ctx_destroy": (_I, [_P]),
     "ves_ctx_info": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    "ves_ctx_max_candidates": (_I, [_P]),
     "ves_last_error": (ctypes.c_char_p, []),
     "ves_diff_prop": (_I, [_P, _I, _I, _P, _P, _P, _P, _P]),
     "ves_geom_prop": (_I, [_P, _I, _P, _P, _P, _P, _P]),
@@ -271,6 +272,15 @@ def check(rc: int, what: str = "") -> None:
     raise VesError(rc, msg)
 
 
+def grow_capacity(need: int, floor: int = 16) -> int:
+    """A list capacity for ``need`` entries with room to spare: the next power
+    of two at or above 1.25 x need (at least ``floor``)."""
+    c = max(int(floor), 1)
+    while c < 1.25 * need:
+        c *= 2
+    return c
+
+
 def ptr(t) -> int | None:
     return None if t is None else t.data_ptr()
 
@@ -296,6 +306,10 @@ class Context:
         self.Nup = nup.value
         self.nquad = nq.value
         self._ws = None
+
+    def max_candidates(self) -> int:
+        """Largest near-pair candidate count of the last call's near-zone builds."""
+        return int(self.lib.ves_ctx_max_candidates(self.handle))
 
     def set_timing(self, on: bool) -> None:
         check(self.lib.ves_ctx_set_timing(self.handle, 1 if on else 0), "set_timing")

@@ -65,8 +65,9 @@ class NearZone:
             st = nz.struct()
             rc = ctx.lib.ves_near_zone_py(ctx.handle, nv, Xv.data_ptr(), nat.ptr(Xupv), float(thresh),
                                           ctypes.byref(st), ws.data_ptr(), ws.numel(), nat.stream_ptr(Xv.device))
-            if rc == nat.VES_ERR_NEARLIST_OVERFLOW and maxc < nv:
-                maxc = min(nv, maxc * 2)
+            need = ctx.max_candidates()
+            if rc == nat.VES_ERR_NEARLIST_OVERFLOW and need > maxc:
+                maxc = nat.grow_capacity(need, maxc)
                 continue
             nat.check(rc, "naiveNearZoneInfo")
             return nz
@@ -83,14 +84,15 @@ class NearZone:
             rc = ctx.lib.ves_near_zone_matlab(ctx.handle, nv, Xv.data_ptr(), float(h), ctypes.byref(st),
                                               ws.data_ptr(), ws.numel(), nat.stream_ptr(Xv.device))
             if rc == nat.VES_ERR_NEARLIST_OVERFLOW:
+                need = ctx.max_candidates()
+                if need > maxc:  # the candidate search stops before the entries are made
+                    maxc = nat.grow_capacity(need, maxc)
+                    continue
                 ne = int(nz.n_entries[0].item())
                 if ne > max_entries:
                     max_entries = ne + 64
-                elif maxc < nv:
-                    maxc = min(nv, maxc * 2)
-                else:
-                    nat.check(rc, "getZone")
-                continue
+                    continue
+                nat.check(rc, "getZone")
             nat.check(rc, "getZone")
             if h <= 0:
                 geo = torch.empty(3, nv, dtype=torch.float64, device=Xv.device)

@@ -192,6 +192,7 @@ int ves_cuda_status(cudaError_t e, const char* what) {
 int ves_launch_check(const char* what) { return ves_cuda_status(cudaGetLastError(), what); }
 
 int ves_reset_status(ves_ctx* ctx, cudaStream_t s) {
+  ctx->last_max_cand = 0;
   return ves_cuda_status(cudaMemsetAsync(ctx->status, 0, sizeof(VesDeviceStatus), s), "reset status");
 }
 
@@ -385,6 +386,7 @@ extern "C" int ves_ctx_create(int N, ves_ctx** out) {
   if (!rc)
     rc = ves_cuda_status(cudaMallocHost(&c->h_status, sizeof(VesDeviceStatus)), "cudaMallocHost");
   if (!rc) rc = ves_cuda_status(cudaMallocHost(&c->h_scal, 256 * sizeof(double)), "cudaMallocHost scal");
+  if (!rc) rc = ves_cuda_status(cudaMallocHost(&c->h_ints, 16 * sizeof(int)), "cudaMallocHost ints");
   if (!rc) rc = ves_cuda_status(cudaDeviceSynchronize(), "table upload");
   if (rc) {
     ves_ctx_destroy(c);
@@ -400,6 +402,7 @@ extern "C" int ves_ctx_destroy(ves_ctx* c) {
   if (c->status) cudaFree(c->status);
   if (c->h_status) cudaFreeHost(c->h_status);
   if (c->h_scal) cudaFreeHost(c->h_scal);
+  if (c->h_ints) cudaFreeHost(c->h_ints);
   if (c->ev[0])
     for (int i = 0; i < 2 * 256; ++i) cudaEventDestroy(c->ev[i]);
   if (c->d_mp) cudaFree(c->d_mp);
@@ -408,6 +411,8 @@ extern "C" int ves_ctx_destroy(ves_ctx* c) {
   free(c);
   return VES_OK;
 }
+
+extern "C" int ves_ctx_max_candidates(const ves_ctx* c) { return c ? c->last_max_cand : -1; }
 
 extern "C" int ves_ctx_info(const ves_ctx* c, int* N, int* Nup, int* nquad) {
   if (!c) return VES_ERR_ARG;

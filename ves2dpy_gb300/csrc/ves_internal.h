@@ -38,6 +38,8 @@ struct ves_ctx {
   VesDeviceStatus* status;  // device status word (reset per API call)
   VesDeviceStatus* h_status;// pinned host mirror
   double* h_scal;            // pinned host scalars (GMRES read-back), 256 doubles
+  int* h_ints;               // pinned host ints (near-list candidate count read-back), 16
+  int last_max_cand;         // largest candidate count of the last near-zone build (any vesicle)
   // optional timing of the all-pairs kernel
   int timing;
   int n_ev;                  // recorded event pairs not yet accumulated

@@ -32,17 +32,27 @@ __device__ __forceinline__ double horner7(const double* c, double t) {
   return v;
 }
 
-// bounding boxes [nv][4] = xmin, xmax, ymin, ymax of n-point curves
-__global__ void bbox_kernel(int n, const double* __restrict__ X, double* __restrict__ box) {
+// bounding boxes [nv][4] = xmin, xmax, ymin, ymax of n-point curves.  A
+// curve with a non-finite coordinate gets the empty box (+inf, -inf, +inf,
+// -inf), which meets no other box, and raises VES_ERR_NONFINITE (site 22,
+// detail = the vesicle): a NaN must not turn into a near pair with every
+// vesicle.
+__global__ void bbox_kernel(int n, const double* __restrict__ X, double* __restrict__ box,
+                            VesDeviceStatus* st) {
   __shared__ double red[4][128];
+  __shared__ int bad;
   const int k = blockIdx.x;
   const double* x = X + (long long)k * 2 * n;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
   double a = 1e300, b = -1e300, c = 1e300, d = -1e300;
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
-    a = fmin(a, x[j]);
-    b = fmax(b, x[j]);
-    c = fmin(c, x[n + j]);
-    d = fmax(d, x[n + j]);
+    const double xv = x[j], yv = x[n + j];
+    if (!isfinite(xv) || !isfinite(yv)) bad = 1;
+    a = fmin(a, xv);
+    b = fmax(b, xv);
+    c = fmin(c, yv);
+    d = fmax(d, yv);
   }
   red[0][threadIdx.x] = a;
   red[1][threadIdx.x] = b;
@@ -58,36 +68,218 @@ __global__ void bbox_kernel(int n, const double* __restrict__ X, double* __restr
     }
     __syncthreads();
   }
-  if (threadIdx.x < 4) box[k * 4 + threadIdx.x] = red[threadIdx.x][0];
+  if (threadIdx.x < 4) {
+    const double inf = __longlong_as_double(0x7ff0000000000000LL);
+    box[k * 4 + threadIdx.x] = bad ? ((threadIdx.x & 1) ? -inf : inf) : red[threadIdx.x][0];
+  }
+  if (threadIdx.x == 0 && bad) ves_set_error(st, VES_ERR_NONFINITE, 22, (long long)k);
 }
 
-// one warp per target vesicle; candidates in ascending order.  nt target and
-// ns source vesicles; same_set: the two sets are one (a vesicle is not its own
-// candidate).
-__global__ void candidates_kernel(int nt, int ns, bool same_set, const double* __restrict__ tbox,
-                                  const double* __restrict__ sbox, double thr, int maxc, int* __restrict__ cand_count,
-                                  int* __restrict__ cand_src, VesDeviceStatus* st) {
+// ---- bucket-sorted candidate search ----------------------------------------
+// The source boxes' centres are counting-sorted into a uniform grid whose
+// cell is at least (max target box + max source box)/2 + threshold wide, so
+// every source whose box comes within the threshold of a target's box has
+// its centre in one of the 3 x 3 cells around the target's centre.  One warp
+// per target then tests the boxes of those cells only: O(nv) work for a
+// suspension instead of O(nv^2).
+struct GridParams {
+  double x0, y0, inv_cell;
+  int nx, ny;
+};
+
+__device__ __forceinline__ bool box_valid(const double* b) { return b[0] <= b[1] && b[2] <= b[3]; }
+
+// one block of 1024 threads: extents of the valid boxes, cell size and grid
+// dimensions (at most cap_cells cells)
+__global__ void __launch_bounds__(1024) grid_setup_kernel(int ns, const double* __restrict__ sbox, int nt,
+                                                          const double* __restrict__ tbox, double thr, int cap_cells,
+                                                          GridParams* __restrict__ gp) {
+  double x0 = 1e300, x1 = -1e300, y0 = 1e300, y1 = -1e300, ws = 0.0, wt = 0.0;
+  for (int i = threadIdx.x; i < ns; i += blockDim.x) {
+    const double* b = sbox + 4 * (long long)i;
+    if (!box_valid(b)) continue;
+    const double cx = 0.5 * (b[0] + b[1]), cy = 0.5 * (b[2] + b[3]);
+    x0 = fmin(x0, cx);
+    x1 = fmax(x1, cx);
+    y0 = fmin(y0, cy);
+    y1 = fmax(y1, cy);
+    ws = fmax(ws, fmax(b[1] - b[0], b[3] - b[2]));
+  }
+  for (int i = threadIdx.x; i < nt; i += blockDim.x) {
+    const double* b = tbox + 4 * (long long)i;
+    if (box_valid(b)) wt = fmax(wt, fmax(b[1] - b[0], b[3] - b[2]));
+  }
+  // reduce: min x0,y0 (as -max of negatives), max x1,y1,ws,wt
+  double v[6] = {-x0, x1, -y0, y1, ws, wt};
+  for (int q = 0; q < 6; ++q)
+    for (int o = 16; o > 0; o >>= 1) v[q] = fmax(v[q], __shfl_xor_sync(0xffffffffu, v[q], o));
+  __shared__ double part[6][32];
+  const int w = threadIdx.x / 32, l = threadIdx.x % 32;
+  if (l == 0)
+    for (int q = 0; q < 6; ++q) part[q][w] = v[q];
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x / 32;
+    for (int q = 0; q < 6; ++q) {
+      double t = l < nw ? part[q][l] : -1e300;
+      for (int o = 16; o > 0; o >>= 1) t = fmax(t, __shfl_xor_sync(0xffffffffu, t, o));
+      v[q] = t;
+    }
+    if (l == 0) {
+      GridParams g;
+      double gx0 = -v[0], gx1 = v[1], gy0 = -v[2], gy1 = v[3];
+      if (!(gx0 <= gx1)) gx0 = gx1 = gy0 = gy1 = 0.0;  // no valid source box
+      double cell = 0.5 * (v[4] + fmax(v[5], 0.0)) + thr;
+      if (!(cell > 0.0)) cell = 1.0;
+      const double ex = gx1 - gx0, ey = gy1 - gy0;
+      // grow the cell until the grid has at most cap_cells cells
+      for (int it = 0; it < 64; ++it) {
+        const double nx = floor(ex / cell) + 1.0, ny = floor(ey / cell) + 1.0;
+        if (nx * ny <= (double)cap_cells) break;
+        cell *= 1.25;
+      }
+      g.x0 = gx0;
+      g.y0 = gy0;
+      g.inv_cell = 1.0 / cell;
+      g.nx = (int)(floor(ex / cell) + 1.0);
+      g.ny = (int)(floor(ey / cell) + 1.0);
+      if (g.nx < 1) g.nx = 1;
+      if (g.ny < 1) g.ny = 1;
+      if ((long long)g.nx * g.ny > cap_cells) g.nx = g.ny = 1;  // unreachable for finite extents
+      *gp = g;
+    }
+  }
+}
+
+__device__ __forceinline__ int grid_coord(double c, double c0, double inv, int n) {
+  const double f = floor((c - c0) * inv);
+  return (int)fmin(fmax(f, -2.0), (double)n + 1.0);  // off-grid targets stay off-grid
+}
+
+__global__ void grid_count_kernel(int ns, const double* __restrict__ sbox, const GridParams* __restrict__ gp,
+                                  int* __restrict__ cell_of, int* __restrict__ counts) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ns) return;
+  const double* b = sbox + 4 * (long long)i;
+  if (!box_valid(b)) {
+    cell_of[i] = -1;
+    return;
+  }
+  const GridParams g = *gp;
+  const int cx = min(max(grid_coord(0.5 * (b[0] + b[1]), g.x0, g.inv_cell, g.nx), 0), g.nx - 1);
+  const int cy = min(max(grid_coord(0.5 * (b[2] + b[3]), g.y0, g.inv_cell, g.ny), 0), g.ny - 1);
+  const int cell = cy * g.nx + cx;
+  cell_of[i] = cell;
+  atomicAdd(&counts[cell], 1);
+}
+
+// exclusive scan of n counts (one block of 1024 threads); start[n] = total
+__global__ void __launch_bounds__(1024) scan_kernel(int n, const int* __restrict__ counts, int* __restrict__ start) {
+  __shared__ int wsum[32];
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x % 32, w = threadIdx.x / 32;
+  for (int base = 0; base < n; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    const int v = i < n ? counts[i] : 0;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    if (w == 0) {
+      int t = wsum[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, t, o);
+        if (lane >= o) t += y;
+      }
+      wsum[lane] = t;
+    }
+    __syncthreads();
+    const int excl = carry + (w > 0 ? wsum[w - 1] : 0) + x - v;
+    if (i < n) start[i] = excl;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) start[n] = carry;
+}
+
+__global__ void grid_fill_kernel(int ns, const int* __restrict__ cell_of, const int* __restrict__ start,
+                                 int* __restrict__ fill, int* __restrict__ sorted) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ns || cell_of[i] < 0) return;
+  const int c = cell_of[i];
+  sorted[start[c] + atomicAdd(&fill[c], 1)] = i;
+}
+
+// one warp per target vesicle: boxes of the 3 x 3 cells around its centre;
+// hits appended (order fixed by sort_candidates_kernel); the true count is
+// kept for the capacity check
+__global__ void grid_candidates_kernel(int nt, bool same_set, const double* __restrict__ tbox,
+                                       const double* __restrict__ sbox, double thr, const GridParams* __restrict__ gp,
+                                       const int* __restrict__ start, const int* __restrict__ sorted, int maxc,
+                                       int* __restrict__ cand_count, int* __restrict__ cand_src,
+                                       int* __restrict__ max_count) {
   const int t = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
   const int lane = threadIdx.x % 32;
   if (t >= nt) return;
-  const double tx0 = tbox[t * 4], tx1 = tbox[t * 4 + 1], ty0 = tbox[t * 4 + 2], ty1 = tbox[t * 4 + 3];
+  const double* tb = tbox + 4 * (long long)t;
   int count = 0;
-  for (int base = 0; base < ns; base += 32) {
-    const int s = base + lane;
-    bool hit = false;
-    if (s < ns && !(same_set && s == t)) {
-      const double gx = fmax(0.0, fmax(sbox[s * 4] - tx1, tx0 - sbox[s * 4 + 1]));
-      const double gy = fmax(0.0, fmax(sbox[s * 4 + 2] - ty1, ty0 - sbox[s * 4 + 3]));
-      hit = gx * gx + gy * gy < thr * thr;
-    }
-    const unsigned m = __ballot_sync(0xffffffffu, hit);
-    const int pos = count + __popc(m & ((1u << lane) - 1u));
-    if (hit && pos < maxc) cand_src[(long long)t * maxc + pos] = s;
-    count += __popc(m);
+  if (box_valid(tb)) {
+    const GridParams g = *gp;
+    const double tx0 = tb[0], tx1 = tb[1], ty0 = tb[2], ty1 = tb[3];
+    const int ix = grid_coord(0.5 * (tx0 + tx1), g.x0, g.inv_cell, g.nx);
+    const int iy = grid_coord(0.5 * (ty0 + ty1), g.y0, g.inv_cell, g.ny);
+    for (int cy = max(iy - 1, 0); cy <= min(iy + 1, g.ny - 1); ++cy)
+      for (int cx = max(ix - 1, 0); cx <= min(ix + 1, g.nx - 1); ++cx) {
+        const int cell = cy * g.nx + cx;
+        const int b0 = start[cell], b1 = start[cell + 1];
+        for (int base = b0; base < b1; base += 32) {
+          const int k = base + lane;
+          bool hit = false;
+          int sidx = -1;
+          if (k < b1) {
+            sidx = sorted[k];
+            if (!(same_set && sidx == t)) {
+              const double* sb = sbox + 4 * (long long)sidx;
+              const double gx = fmax(0.0, fmax(sb[0] - tx1, tx0 - sb[1]));
+              const double gy = fmax(0.0, fmax(sb[2] - ty1, ty0 - sb[3]));
+              hit = gx * gx + gy * gy < thr * thr;
+            }
+          }
+          const unsigned m = __ballot_sync(0xffffffffu, hit);
+          const int pos = count + __popc(m & ((1u << lane) - 1u));
+          if (hit && pos < maxc) cand_src[(long long)t * maxc + pos] = sidx;
+          count += __popc(m);
+        }
+      }
   }
   if (lane == 0) {
     cand_count[t] = count < maxc ? count : maxc;
-    if (count > maxc) ves_set_error(st, VES_ERR_NEARLIST_OVERFLOW, 20, (long long)t);
+    atomicMax(max_count, count);
+  }
+}
+
+// ascending order of each target's candidate list (the far-field kernels
+// walk the lists with a cursor); one block per target, rank sort in shared
+// memory (the lists hold distinct vesicle indices)
+__global__ void sort_candidates_kernel(int maxc, const int* __restrict__ cand_count, int* __restrict__ cand_src) {
+  extern __shared__ int lst[];
+  const int t = blockIdx.x;
+  const int n = cand_count[t];
+  if (n <= 1) return;
+  int* row = cand_src + (long long)t * maxc;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) lst[i] = row[i];
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int v = lst[i];
+    int r = 0;
+    for (int j = 0; j < n; ++j) r += lst[j] < v;
+    row[r] = v;
   }
 }
 
@@ -401,6 +593,82 @@ __global__ void add_kernel(long long n, const double* __restrict__ a, double* __
   if (i < n) out[i] += a[i];
 }
 
+
+// Scratch of one candidate search: grid parameters, per-cell counts, starts
+// and fill cursors, the sources sorted by cell and the largest count.
+struct CandScratch {
+  GridParams* gp;
+  int *cell_of, *counts, *start, *fill, *sorted, *max_count;
+  int cap_cells;
+};
+
+CandScratch carve_candidates(WsCarver& ws, int nt, int ns) {
+  CandScratch c;
+  c.cap_cells = 2 * ns + 64;
+  c.gp = ws.take<GridParams>(1);
+  c.cell_of = ws.take<int>((size_t)ns + 1);
+  c.counts = ws.take<int>((size_t)c.cap_cells * 2 + 2);  // counts | fill cursors
+  c.fill = c.counts ? c.counts + c.cap_cells + 1 : nullptr;
+  c.start = ws.take<int>((size_t)c.cap_cells + 1);
+  c.sorted = ws.take<int>((size_t)ns + 1);
+  c.max_count = ws.take<int>(1);
+  (void)nt;
+  return c;
+}
+
+// Candidate lists of nt target boxes against ns source boxes (threshold thr
+// on the box gap), written into nl (capacity nl->maxc per target, ascending
+// source indices).  Synchronises the stream once to read the largest count:
+// a non-finite curve (site 22) or a count above the capacity is reported
+// here, before any list is used, with the count needed in the message and in
+// ctx->last_max_cand.  *max_out receives that count.
+int find_candidates(ves_ctx* c, int nt, int ns, bool same_set, const double* tbox, const double* sbox, double thr,
+                    const ves_near_lists* nl, const CandScratch& cs, int* max_out, cudaStream_t s,
+                    const char* what) {
+  *max_out = 0;
+  if (nl->maxc > 12288) {
+    ves_record_error(VES_ERR_ARG, "%s: candidate capacity %d above 12288", what, nl->maxc);
+    return VES_ERR_ARG;
+  }
+  int rc = ves_cuda_status(cudaMemsetAsync(cs.counts, 0, ((size_t)cs.cap_cells * 2 + 2) * sizeof(int), s), what);
+  if (!rc) rc = ves_cuda_status(cudaMemsetAsync(cs.max_count, 0, sizeof(int), s), what);
+  if (rc) return rc;
+  if (ns > 0) {
+    ves_count_launch(4);
+    grid_setup_kernel<<<1, 1024, 0, s>>>(ns, sbox, nt, tbox, thr, cs.cap_cells, cs.gp);
+    grid_count_kernel<<<ceil_div(ns, 256), 256, 0, s>>>(ns, sbox, cs.gp, cs.cell_of, cs.counts);
+    scan_kernel<<<1, 1024, 0, s>>>(cs.cap_cells, cs.counts, cs.start);
+    grid_fill_kernel<<<ceil_div(ns, 256), 256, 0, s>>>(ns, cs.cell_of, cs.start, cs.fill, cs.sorted);
+    ves_count_launch();
+    grid_candidates_kernel<<<ceil_div((long long)nt * 32, 256), 256, 0, s>>>(
+        nt, same_set, tbox, sbox, thr, cs.gp, cs.start, cs.sorted, nl->maxc, nl->cand_count, nl->cand_src,
+        cs.max_count);
+    ves_count_launch();
+    sort_candidates_kernel<<<nt, 128, (size_t)nl->maxc * sizeof(int), s>>>(nl->maxc, nl->cand_count, nl->cand_src);
+  } else {
+    rc = ves_cuda_status(cudaMemsetAsync(nl->cand_count, 0, (size_t)nt * sizeof(int), s), what);
+    if (rc) return rc;
+  }
+  if ((rc = ves_launch_check(what))) return rc;
+  rc = ves_cuda_status(cudaMemcpyAsync(c->h_ints, cs.max_count, sizeof(int), cudaMemcpyDeviceToHost, s), what);
+  if (rc) return rc;
+  if ((rc = ves_check_status(c, s, what))) {
+    if (rc == VES_ERR_NONFINITE && c->h_status->where == 22)
+      ves_record_error(rc, "%s: vesicle %lld has a non-finite coordinate (site 22)", what, c->h_status->aux);
+    return rc;
+  }
+  const int mx = c->h_ints[0];
+  if (mx > c->last_max_cand) c->last_max_cand = mx;
+  *max_out = mx;
+  if (mx > nl->maxc) {
+    ves_record_error(VES_ERR_NEARLIST_OVERFLOW,
+                     "%s: a vesicle has %d near-pair candidates, the lists hold %d (site 20; capacity needed %d)",
+                     what, mx, nl->maxc, mx);
+    return VES_ERR_NEARLIST_OVERFLOW;
+  }
+  return VES_OK;
+}
+
 }  // namespace
 
 int near_zone_py(ves_ctx* c, int nv, const double* X, const double* Xup_in, double thresh,
@@ -409,6 +677,7 @@ int near_zone_py(ves_ctx* c, int nv, const double* X, const double* Xup_in, doub
   double* tbox = ws.take<double>((size_t)nv * 4);
   double* sbox = ws.take<double>((size_t)nv * 4);
   double* Xup = Xup_in ? nullptr : ws.take<double>((size_t)nv * 2 * Nup);
+  const CandScratch cs = carve_candidates(ws, nv, nv);
   if (ws.sizing) return VES_OK;
   if (!ws.ok()) {
     ves_record_error(VES_ERR_WORKSPACE, "near_zone_py: workspace too small");
@@ -422,16 +691,14 @@ int near_zone_py(ves_ctx* c, int nv, const double* X, const double* Xup_in, doub
   const double thr = thresh > 0 ? thresh : 1.0 / N;
   if (!Xup_in) launch_upsample(c, nv, 2, X, 2LL * N, Xup, s);
   const double* Xu = Xup_in ? Xup_in : Xup;
-  ves_count_launch();
-  bbox_kernel<<<nv, 128, 0, s>>>(N, X, tbox);
-  ves_count_launch();
-  bbox_kernel<<<nv, 128, 0, s>>>(Nup, Xu, sbox);
-  ves_count_launch();
-  candidates_kernel<<<ceil_div((long long)nv * 32, 256), 256, 0, s>>>(nv, nv, true, tbox, sbox, thr, nl->maxc,
-                                                                      nl->cand_count,
-                                                                      nl->cand_src, c->status);
+  ves_count_launch(2);
+  bbox_kernel<<<nv, 128, 0, s>>>(N, X, tbox, c->status);
+  bbox_kernel<<<nv, 128, 0, s>>>(Nup, Xu, sbox, c->status);
+  int mx = 0;
+  int rc = find_candidates(c, nv, nv, true, tbox, sbox, thr, nl, cs, &mx, s, "near_zone_py");
+  if (rc) return rc;
   const size_t sh = (size_t)2 * N * sizeof(double) + (c->nwords_N + c->nwords_up) * sizeof(uint32_t);
-  dim3 grid(nl->maxc, nv);
+  dim3 grid(mx > 0 ? mx : 1, nv);
   ves_count_launch();
   py_masks_kernel<<<grid, 256, sh, s>>>(N, Nup, nl->maxc, thr * thr, X, Xu, nl->cand_count, nl->cand_src,
                                         nl->excl_mask, nl->hh_mask);
@@ -444,6 +711,7 @@ int near_zone_matlab(ves_ctx* c, int nv, const double* X, double h, const ves_ne
   double* box = ws.take<double>((size_t)nv * 4);
   double* len = ws.take<double>((size_t)nv);
   double* hmin = ws.take<double>(1);
+  const CandScratch cs = carve_candidates(ws, nv, nv);
   if (ws.sizing) return VES_OK;
   if (!ws.ok()) {
     ves_record_error(VES_ERR_WORKSPACE, "near_zone_matlab: workspace too small");
@@ -468,12 +736,11 @@ int near_zone_matlab(ves_ctx* c, int nv, const double* X, double h, const ves_ne
   int rc = ves_cuda_status(cudaMemsetAsync(nl->n_entries, 0, sizeof(int), s), "zero entries");
   if (rc) return rc;
   ves_count_launch();
-  bbox_kernel<<<nv, 128, 0, s>>>(N, X, box);
-  ves_count_launch();
-  candidates_kernel<<<ceil_div((long long)nv * 32, 256), 256, 0, s>>>(nv, nv, true, box, box, 2.0 * h, nl->maxc,
-                                                                      nl->cand_count, nl->cand_src, c->status);
+  bbox_kernel<<<nv, 128, 0, s>>>(N, X, box, c->status);
+  int mx = 0;
+  if ((rc = find_candidates(c, nv, nv, true, box, box, 2.0 * h, nl, cs, &mx, s, "near_zone_matlab"))) return rc;
   const size_t sh = (size_t)(2 * N + 49) * sizeof(double) + c->nwords_N * sizeof(uint32_t);
-  dim3 grid(nl->maxc, nv);
+  dim3 grid(mx > 0 ? mx : 1, nv);
   ves_count_launch();
   matlab_zone_kernel<<<grid, 128, sh, s>>>(N, N, nl->maxc, h, X, X, c->lag, nl->cand_count, nl->cand_src,
                                            nl->excl_mask, nl->max_entries, nl->n_entries, nl->ent_tsj,
@@ -550,6 +817,7 @@ int near_zone_matlab_cross(ves_ctx* ct, ves_ctx* cs, int nvt, const double* Xt, 
   const int Nt = ct->N, Ns = cs->N;
   double* tbox = ws.take<double>((size_t)nvt * 4);
   double* sbox = ws.take<double>((size_t)nvs * 4);
+  const CandScratch csc = carve_candidates(ws, nvt, nvs);
   if (ws.sizing) return VES_OK;
   if (!ws.ok()) {
     ves_record_error(VES_ERR_WORKSPACE, "near_zone_cross: workspace too small");
@@ -562,13 +830,13 @@ int near_zone_matlab_cross(ves_ctx* ct, ves_ctx* cs, int nvt, const double* Xt, 
   }
   int rc = ves_cuda_status(cudaMemsetAsync(nl->n_entries, 0, sizeof(int), s), "zero entries");
   if (rc || nvt <= 0) return rc;
-  ves_count_launch(nvs > 0 ? 3 : 2);
-  bbox_kernel<<<nvt, 128, 0, s>>>(Nt, Xt, tbox);
-  if (nvs > 0) bbox_kernel<<<nvs, 128, 0, s>>>(Ns, Xs, sbox);
-  candidates_kernel<<<ceil_div((long long)nvt * 32, 256), 256, 0, s>>>(nvt, nvs, false, tbox, sbox, 2.0 * h, nl->maxc,
-                                                                       nl->cand_count, nl->cand_src, ct->status);
+  ves_count_launch(nvs > 0 ? 2 : 1);
+  bbox_kernel<<<nvt, 128, 0, s>>>(Nt, Xt, tbox, ct->status);
+  if (nvs > 0) bbox_kernel<<<nvs, 128, 0, s>>>(Ns, Xs, sbox, ct->status);
+  int mx = 0;
+  if ((rc = find_candidates(ct, nvt, nvs, false, tbox, sbox, 2.0 * h, nl, csc, &mx, s, "near_zone_cross"))) return rc;
   const size_t sh = (size_t)(2 * Ns + 49) * sizeof(double) + ct->nwords_N * sizeof(uint32_t);
-  dim3 grid(nl->maxc, nvt);
+  dim3 grid(mx > 0 ? mx : 1, nvt);
   ves_count_launch();
   matlab_zone_kernel<<<grid, 128, sh, s>>>(Nt, Ns, nl->maxc, h, Xt, Xs, ct->lag, nl->cand_count, nl->cand_src,
                                            nl->excl_mask, nl->max_entries, nl->n_entries, nl->ent_tsj, nl->ent_icp,

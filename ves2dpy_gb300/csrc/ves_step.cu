@@ -736,6 +736,13 @@ static int biem_step_impl(ves_ctx* c, const ves_step_params* prm, int nv, const 
     rc = VES_ERR_GMRES_MAXIT;
   }
 done:
+  if (rc == VES_ERR_NEARLIST_OVERFLOW && prm->near_scheme == VES_NEAR_MATLAB && res && S.nl.n_entries) {
+    // the MATLAB entry count keeps running past the capacity: report what is needed
+    int nn = 0;
+    if (cudaMemcpyAsync(&nn, S.nl.n_entries, sizeof(int), cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+        cudaStreamSynchronize(s) == cudaSuccess)
+      res->n_near_entries = nn;
+  }
   return rc;
 }
 
@@ -974,7 +981,22 @@ static int biem_step_mixed_impl(int ng, ves_ctx* const* ctx, const ves_step_para
   if (!prm->use_preco && n > 0)
     if ((rc = ves_cuda_status(cudaMemsetAsync(B.x, 0, n * sizeof(double), s), "x0"))) return rc;
   for (int g = 0; g < ng; ++g)
-    if ((rc = ves_check_status(ctx[g], s, "biem_step_mixed setup"))) return rc;
+    if ((rc = ves_check_status(ctx[g], s, "biem_step_mixed setup"))) {
+      if (rc == VES_ERR_NEARLIST_OVERFLOW && prm->near_scheme == VES_NEAR_MATLAB) {
+        // report the largest MATLAB entry count met (they run past the capacity)
+        int worst = 0;
+        for (int a = 0; a < ng; ++a)
+          for (int q = 0; q < ng; ++q) {
+            const int* ne = (a == q) ? M.g[a].nl.n_entries : M.xl[a][q].n_entries;
+            int nn = 0;
+            if (M.g[a].nv > 0 && ne && cudaMemcpyAsync(&nn, ne, sizeof(int), cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+                cudaStreamSynchronize(s) == cudaSuccess && nn > worst)
+              worst = nn;
+          }
+        res->n_near_entries = worst;
+      }
+      return rc;
+    }
   M.matvecs = 0;
   if ((rc = gmres(M, B, res))) return rc;
   res->matvecs = M.matvecs;

@@ -160,10 +160,13 @@ class MLARM_manyfree_py:
                   "ves_mlarm_create")
         self.handle = h
         self.last_result = None
+        # near-pair candidate capacity per vesicle; grows (and the step is
+        # re-run from its unchanged inputs) when a step reports more candidates
+        self._maxc = 32
 
     def _params(self):
         return nat.MlarmParams(self.dt, self.kappa, nat.FLOW["shear"], 0.0, 0.0, 0.0,
-                               nat.PREC[self.farfield_precision], 1 if self.eval_near_net else 0, 0)
+                               nat.PREC[self.farfield_precision], 1 if self.eval_near_net else 0, self._maxc)
 
     def _step(self, Xold, tenOld, trace=None):
         X = as_device_f64(Xold, self.device)
@@ -179,14 +182,21 @@ class MLARM_manyfree_py:
         l0 = as_device_f64(self.len0, self.device).reshape(-1).contiguous()
         Xo = torch.empty_like(Xv)
         to = torch.empty_like(tv)
-        prm = self._params()
-        ws = self.ctx.workspace(self.lib.ves_mlarm_step_workspace(self.handle, ctypes.byref(prm), nv))
         res = nat.MlarmResult()
         tr = ctypes.byref(trace) if trace is not None else None
-        nat.check(self.lib.ves_mlarm_step(self.handle, ctypes.byref(prm), nv, Xv.data_ptr(), tv.data_ptr(),
-                                          vb.data_ptr(), a0.data_ptr(), l0.data_ptr(), Xo.data_ptr(), to.data_ptr(),
-                                          ctypes.byref(res), tr, ws.data_ptr(), ws.numel(),
-                                          nat.stream_ptr(self.device)), "ves_mlarm_step")
+        while True:
+            prm = self._params()
+            ws = self.ctx.workspace(self.lib.ves_mlarm_step_workspace(self.handle, ctypes.byref(prm), nv))
+            rc = self.lib.ves_mlarm_step(self.handle, ctypes.byref(prm), nv, Xv.data_ptr(), tv.data_ptr(),
+                                         vb.data_ptr(), a0.data_ptr(), l0.data_ptr(), Xo.data_ptr(), to.data_ptr(),
+                                         ctypes.byref(res), tr, ws.data_ptr(), ws.numel(), nat.stream_ptr(self.device))
+            need = self.ctx.max_candidates()
+            if rc == nat.VES_ERR_NEARLIST_OVERFLOW and need > self._maxc:
+                # the lists are built before anything reads them: grow and re-run
+                self._maxc = nat.grow_capacity(need, self._maxc)
+                continue
+            nat.check(rc, "ves_mlarm_step")
+            break
         self.last_result = res
         return from_vm(Xo), from_vm(to)
 

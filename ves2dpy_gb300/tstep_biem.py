@@ -69,6 +69,10 @@ class TStepBiem:
         _, self.area, self.length = Curve().geomProp(X)
         self._ctx = nat.context(self.N, self.device)
         self.last = None
+        # near-list capacities (candidates per vesicle, MATLAB entries; 0 =
+        # the library default); they grow when a step reports more
+        self._maxc = 32
+        self._maxe = 0
 
     def params(self) -> nat.StepParams:
         p = nat.StepParams()
@@ -88,8 +92,8 @@ class TStepBiem:
         p.near_scheme = nat.NEAR[self.near]
         p.farfield_precision = nat.PREC[self.farfield_precision]
         p.sl_precision = nat.PREC[self.sl_precision]
-        p.maxc = 64
-        p.max_entries = 0
+        p.maxc = self._maxc
+        p.max_entries = self._maxe
         p.repulsion = 1 if self.repulsion else 0
         p.rep_strength = self.repStrength
         p.min_dist = self.minDist
@@ -103,21 +107,37 @@ class TStepBiem:
     def step_device(self, Xv, sigv, Xout=None, sigout=None, ws=None):
         """One step on device-layout tensors Xv[nv][2N], sigv[nv][N] (float64,
         contiguous); returns (Xout, sigout, result)."""
-        p = self.params()
         ctx = self._ctx
-        nbytes = ctx.lib.ves_biem_step_workspace(ctx.handle, ctypes.byref(p), self.nv)
-        if ws is None:
-            ws = ctx.workspace(nbytes)
         Xout = torch.empty_like(Xv) if Xout is None else Xout
         sigout = torch.empty_like(sigv) if sigout is None else sigout
         res = nat.StepResult()
-        rc = ctx.lib.ves_biem_step(ctx.handle, ctypes.byref(p), self.nv, Xv.data_ptr(), sigv.data_ptr(),
-                                   Xout.data_ptr(), sigout.data_ptr(), ctypes.byref(res), ws.data_ptr(), ws.numel(),
-                                   nat.stream_ptr(self.device))
+        while True:
+            p = self.params()
+            nbytes = ctx.lib.ves_biem_step_workspace(ctx.handle, ctypes.byref(p), self.nv)
+            w = ws if ws is not None and ws.numel() >= nbytes else ctx.workspace(nbytes)
+            rc = ctx.lib.ves_biem_step(ctx.handle, ctypes.byref(p), self.nv, Xv.data_ptr(), sigv.data_ptr(),
+                                       Xout.data_ptr(), sigout.data_ptr(), ctypes.byref(res), w.data_ptr(),
+                                       w.numel(), nat.stream_ptr(self.device))
+            if rc == nat.VES_ERR_NEARLIST_OVERFLOW and self._grow(res):
+                continue  # the near lists are built before the solve reads them: re-run with room
+            break
         if rc not in (nat.VES_OK, nat.VES_ERR_GMRES_MAXIT):
             nat.check(rc, "time_step")
         self.last = res
         return Xout, sigout, res
+
+    def _grow(self, res) -> bool:
+        """After VES_ERR_NEARLIST_OVERFLOW: enlarge the capacity that ran out
+        (False if neither did, i.e. the overflow is not a capacity)."""
+        need = self._ctx.max_candidates()
+        if need > self._maxc:
+            self._maxc = nat.grow_capacity(need, self._maxc)
+            return True
+        maxe = self._maxe if self._maxe > 0 else max(1024, self.nv * self.N)
+        if self.near == "matlab" and res.n_near_entries > maxe:
+            self._maxe = nat.grow_capacity(res.n_near_entries, maxe)
+            return True
+        return False
 
     def time_step(self, Xstore, sigStore, etaStore=None, RSstore=None):
         """tstep_biem.py:181-428 -> (X, sigma, eta, RS, iter, iflag).
@@ -211,14 +231,29 @@ class TStepBiemMixed:
         def ptrs(ts):
             return ctypes.cast((ctypes.c_void_p * ng)(*[t.data_ptr() for t in ts]), ctypes.c_void_p)
 
-        nbytes = self.workspace_bytes()
-        if nbytes == 0:
-            nat.check(nat.VES_ERR_ARG, "time_step (mixed): workspace query")
-        ws = self.groups[0]._ctx.workspace(nbytes)
         res = nat.StepResult()
-        rc = lib.ves_biem_step_mixed(ng, ctypes.cast(ctxs, ctypes.c_void_p), ctypes.byref(p),
-                                     ctypes.cast(nvs, ctypes.c_void_p), ptrs(Xv), ptrs(sv), ptrs(Xo), ptrs(so),
-                                     ctypes.byref(res), ws.data_ptr(), ws.numel(), nat.stream_ptr(self.device))
+        while True:
+            p = self.groups[0].params()
+            nbytes = self.workspace_bytes()
+            if nbytes == 0:
+                nat.check(nat.VES_ERR_ARG, "time_step (mixed): workspace query")
+            ws = self.groups[0]._ctx.workspace(nbytes)
+            rc = lib.ves_biem_step_mixed(ng, ctypes.cast(ctxs, ctypes.c_void_p), ctypes.byref(p),
+                                         ctypes.cast(nvs, ctypes.c_void_p), ptrs(Xv), ptrs(sv), ptrs(Xo), ptrs(so),
+                                         ctypes.byref(res), ws.data_ptr(), ws.numel(), nat.stream_ptr(self.device))
+            if rc == nat.VES_ERR_NEARLIST_OVERFLOW:
+                need = max(g._ctx.max_candidates() for g in self.groups)
+                g0 = self.groups[0]
+                if need > g0._maxc:
+                    for g in self.groups:
+                        g._maxc = nat.grow_capacity(need, g0._maxc)
+                    continue
+                maxe = g0._maxe if g0._maxe > 0 else max(1024, max(g.nv * g.N for g in self.groups))
+                if res.n_near_entries > maxe:
+                    for g in self.groups:
+                        g._maxe = nat.grow_capacity(res.n_near_entries, maxe)
+                    continue
+            break
         if rc not in (nat.VES_OK, nat.VES_ERR_GMRES_MAXIT):
             nat.check(rc, "time_step (mixed)")
         self.last = res

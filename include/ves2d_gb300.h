@@ -444,6 +444,70 @@ VES_API int ves_mlarm_standardize(ves_ctx* ctx, int nv, const double* X, double*
                                   size_t ws_bytes, void* stream);
 VES_API size_t ves_mlarm_standardize_workspace(ves_ctx* ctx, int nv);
 
+/* ---- training the MLARM networks ------------------------------------------ */
+/* The reference loads trained TorchScript models (get_network_torch.py:29,
+ * 127, 224, 324, 410) whose weights, data and training code are not in its
+ * tree; the MATLAB ground-truth scripts (matlab/relaxation_solve.m,
+ * matlab/groundTruth_NearFieldStokesletData.m) generate data with the BIEM
+ * operators of one vesicle.  These entry points make that data on the device
+ * and train networks of the block template.
+ *
+ * Training targets for standardised shapes Xs[nv][2][N] (N = 128; the output
+ * of ves_mlarm_standardize), each output optional (NULL = skip):
+ *   relax_dx[nv][2][N]  X+ - Xs of the implicit step (tstep_biem.py:181-428) of
+ *                       the isolated vesicle without flow, time step dt
+ *   selften[nv][N]      A^-1 Div G fBend, A = Div G Ten (invTenMatOnSelfBend,
+ *                       wrapper_MLARM_batch_compile_N128.py:3672-3688)
+ *   advten[nv][254][N]  channel 2m + c: A^-1 Div b_{m+1,c}, b_{k,0} = (cos k th,
+ *                       sin k th)/N, b_{k,1} = (-sin k th, cos k th)/N
+ *                       (invTenMatOnVback :3632-3669)
+ *   adv[nv][254][2N]    channel 2m + c: G Ten A^-1 Div b_{m+1,c} (the M of
+ *                       translateVinfwTorch :3584-3620)
+ * sl_precision: VES_PREC_FP64 or VES_PREC_FP32C for the Alpert matrix. */
+VES_API int ves_mlarm_targets(ves_ctx* ctx, int nv, const double* Xs, double dt, double kappa, int sl_precision,
+                              double* relax_dx, double* selften, double* advten, double* adv, void* ws,
+                              size_t ws_bytes, void* stream);
+VES_API size_t ves_mlarm_targets_workspace(ves_ctx* ctx, int nv, int sl_precision);
+
+/* The implicit step of tstep_biem.py:181-428 for vesicles that do not
+ * interact (each solves its own self-interaction block directly):
+ * [I + dt k G Ben, -dt G Ten; Div, 0] [Xout; s] = [X + dt vinf; Div X],
+ * X, vinf (NULL: no flow), Xout [nv][2][N].  Evolves training shapes under a
+ * background flow; the relaxation target above is its vinf = NULL case. */
+VES_API int ves_isolated_step(ves_ctx* ctx, int nv, const double* X, const double* vinf, double dt, double kappa,
+                              int sl_precision, double* Xout, void* ws, size_t ws_bytes, void* stream);
+VES_API size_t ves_isolated_step_workspace(ves_ctx* ctx, int nv, int sl_precision);
+
+/* One channel group of a network of the block template in training
+ * (model_zoo/Net_ves_*.py), precision VES_NET_FP32 (training) or VES_NET_FP64
+ * (gradient checks): parameters, gradients, Adam moments and the activations
+ * of up to max_batch samples.  params: 30 float32 arrays per block in the
+ * order conv1_1.{weight,bias}, conv1_2, conv2_1, conv2_2, deconv1, deconv2,
+ * mix, then bn1..bn4.{weight, bias, running_mean, running_var} (the state-dict
+ * names of the reference modules); batch norm is trained as its
+ * evaluation-mode affine map (running statistics fixed). */
+typedef struct ves_trainer ves_trainer;
+VES_API int ves_trainer_create(int precision, int length, int nblocks, const ves_net_block* blocks,
+                               const float* const* params, int max_batch, ves_trainer** out);
+VES_API int ves_trainer_destroy(ves_trainer* t);
+VES_API long long ves_trainer_num_params(const ves_trainer* t);
+/* x[B][cin][L] -> y[B][cout][L] (y may be NULL); keeps the activations */
+VES_API int ves_trainer_forward(ves_trainer* t, int batch, const void* x, void* y, void* stream);
+/* loss = mean of w_b w_c (y - target)^2 over the last forward's batch
+ * (channel weights w_c[cout], sample weights w_b[batch]; NULL: all 1), its
+ * gradient through every layer into the parameter gradients (zeroed first);
+ * *loss (may be NULL) read back with one stream sync */
+VES_API int ves_trainer_backward_mse(ves_trainer* t, int batch, const void* target, const void* channel_weights,
+                                     const void* sample_weights, double* loss, void* stream);
+/* Adam (bias-corrected, step >= 1) on every trainable parameter */
+VES_API int ves_trainer_adam(ves_trainer* t, double lr, double beta1, double beta2, double eps, int step,
+                             void* stream);
+/* parameters / gradients out as float32 arrays in the order of _create (NULL entries skipped) */
+VES_API int ves_trainer_get_params(const ves_trainer* t, float* const* params, void* stream);
+VES_API int ves_trainer_get_grads(const ves_trainer* t, float* const* grads, void* stream);
+/* the FP64 trainer's gradients as one host array in the same order */
+VES_API int ves_trainer_get_grads_f64(const ves_trainer* t, double* out, void* stream);
+
 /* ---- all-pairs sum without allocation (no counterpart in the reference) ---- */
 /* The sum of ves_farfield (no near-pair lists) for callers that cannot allocate
  * device memory when they call: applications whose GPU memory is entirely

@@ -39,11 +39,18 @@ def net_forward(spec, sd, x, dtype=np.float64):
     state dict ``sd`` on input x (nv, rep*cin, L); numpy in/out in ``dtype``
     (float64 for parity, float32 to time the reference networks' precision)."""
     import torch
+    t = torch.from_numpy(np.asarray(x, dtype=dtype))
+    W = {k: torch.from_numpy(np.asarray(v, dtype=dtype)) for k, v in sd.items()}
+    return net_forward_t(spec, W, t).numpy()
+
+
+def net_forward_t(spec, W, t):
+    """net_forward on torch tensors (state dict W, input t): differentiable,
+    the reference for the training kernels' gradients."""
+    import torch
     import torch.nn.functional as F
 
     G = spec.rep
-    t = torch.from_numpy(np.asarray(x, dtype=dtype))
-    W = {k: torch.from_numpy(np.asarray(v, dtype=dtype)) for k, v in sd.items()}
     nv = t.shape[0]
 
     def conv(inp, name, pad, dil):
@@ -77,7 +84,7 @@ def net_forward(spec, sd, x, dtype=np.float64):
         if blk.npass:
             mm = torch.cat((mm, xs[:, :, blk.cin - blk.npass:]), dim=2)
         t = mm.reshape(nv, G * blk.cout, L)
-    return t.numpy()
+    return t
 
 
 # --------------------------------------------------------------------------
@@ -325,6 +332,55 @@ def bending_upsampled(X, kappa=1.0):
     Xup = O.interpft_vec(X, Nup)
     cup = O.Capsule(Xup, kappa)
     return O.interpft_vec(cup.bending_term(Xup), N)
+
+
+def exact_targets(Xs, dt=1e-5, kappa=1.0):
+    """Training targets of the four trained networks for standardised shapes
+    Xs (2N, nv), from the BIEM operators of each isolated vesicle (FP64):
+    relax (2N, nv) = X+ - Xs of the implicit step without flow
+    (tstep_biem.py:181-428 with one vesicle; its bending operator is the
+    fourth power of the matvec's arc derivative, capsules.py:62-68); selften (N, nv) =
+    A^-1 Div G fBend, A = Div G Ten; advten (nv, 254, N) and adv (nv, 254, 2N):
+    A^-1 Div b and G Ten A^-1 Div b for the Fourier basis velocities
+    b_{k,0} = (cos k th, sin k th)/N, b_{k,1} = (-sin k th, cos k th)/N,
+    channel 2(k-1) + c, k = 1..127."""
+    N, nv = Xs.shape[0] // 2, Xs.shape[1]
+    tab = O.PotenTables(N)
+    G = O.stokes_sl_matrix(Xs, tab)
+    cap = O.Capsule(Xs, kappa)
+    Ben, Ten, Div = cap.compute_derivs()
+    fB = bending_upsampled(Xs, kappa)
+    th = 2 * np.pi * np.arange(N) / N
+    Bm = np.zeros((2 * N, 254))
+    for m in range(127):
+        c, s_ = np.cos((m + 1) * th) / N, np.sin((m + 1) * th) / N
+        Bm[:N, 2 * m], Bm[N:, 2 * m] = c, s_
+        Bm[:N, 2 * m + 1], Bm[N:, 2 * m + 1] = -s_, c
+    relax = np.zeros((2 * N, nv))
+    selften = np.zeros((N, nv))
+    advten = np.zeros((nv, 254, N))
+    adv = np.zeros((nv, 254, 2 * N))
+    divx = cap.surface_div(Xs)
+    D1 = np.real(O.fourier_diff(N))
+    for k in range(nv):
+        # the matvec's bending operator: the fourth power of its arc derivative
+        Ar = cap.isa[:, k][:, None] * D1
+        D4 = np.linalg.matrix_power(Ar, 4)
+        Bk = np.zeros((2 * N, 2 * N))
+        Bk[:N, :N] = Bk[N:, N:] = D4
+        M = np.zeros((3 * N, 3 * N))
+        M[:2 * N, :2 * N] = np.eye(2 * N) + dt * kappa * G[:, :, k] @ Bk
+        M[:2 * N, 2 * N:] = -dt * G[:, :, k] @ Ten[:, :, k]
+        M[2 * N:, :2 * N] = Div[:, :, k]
+        sol = np.linalg.solve(M, np.concatenate([Xs[:, k], divx[:, k]]))
+        relax[:, k] = sol[:2 * N] - Xs[:, k]
+        GT = G[:, :, k] @ Ten[:, :, k]
+        A = Div[:, :, k] @ GT
+        selften[:, k] = np.linalg.solve(A, Div[:, :, k] @ (G[:, :, k] @ fB[:, k]))
+        Z = np.linalg.solve(A, Div[:, :, k] @ Bm)
+        advten[k] = Z.T
+        adv[k] = (GT @ Z).T
+    return {"relax": relax, "selften": selften, "advten": advten, "adv": adv}
 
 
 def far_field(X, f, excl=None):

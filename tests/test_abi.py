@@ -11,7 +11,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared():
     txt = open(os.path.join(ROOT, "include", "ves2d_gb300.h")).read()
-    return set(re.findall(r"VES_API\s+(?:int|size_t|const char\*)\s+(ves_\w+)\s*\(", txt))
+    return set(re.findall(r"VES_API\s+(?:int|size_t|long long|const char\*)\s+(ves_\w+)\s*\(", txt))
 
 
 def test_header_declares_api():

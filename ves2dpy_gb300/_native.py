@@ -228,6 +228,19 @@ SIGNATURES = {
     "ves_traj_append": (_I, [_P, _D, _P, _I, _P]),
     "ves_traj_flush": (_I, [_P, ctypes.POINTER(_LL)]),
     "ves_traj_close": (_I, [_P]),
+    "ves_mlarm_targets": (_I, [_P, _I, _P, ctypes.c_double, ctypes.c_double, _I, _P, _P, _P, _P, _P, _SZ, _P]),
+    "ves_mlarm_targets_workspace": (_SZ, [_P, _I, _I]),
+    "ves_isolated_step": (_I, [_P, _I, _P, _P, ctypes.c_double, ctypes.c_double, _I, _P, _P, _SZ, _P]),
+    "ves_isolated_step_workspace": (_SZ, [_P, _I, _I]),
+    "ves_trainer_create": (_I, [_I, _I, _I, _P, _P, _I, ctypes.POINTER(_P)]),
+    "ves_trainer_destroy": (_I, [_P]),
+    "ves_trainer_num_params": (ctypes.c_longlong, [_P]),
+    "ves_trainer_forward": (_I, [_P, _I, _P, _P, _P]),
+    "ves_trainer_backward_mse": (_I, [_P, _I, _P, _P, _P, ctypes.POINTER(ctypes.c_double), _P]),
+    "ves_trainer_adam": (_I, [_P, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, _I, _P]),
+    "ves_trainer_get_params": (_I, [_P, _P, _P]),
+    "ves_trainer_get_grads": (_I, [_P, _P, _P]),
+    "ves_trainer_get_grads_f64": (_I, [_P, _P, _P]),
 }
 
 _lib = None

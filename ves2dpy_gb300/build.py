@@ -20,7 +20,7 @@ LIB = os.path.join(LIBDIR, "libves2d_gb300.so")
 SOURCES = ["ves_ctx.cu", "ves_spectral.cu", "ves_blas.cu", "ves_alpert.cu", "ves_farfield.cu",
            "ves_farfield_mp.cu", "ves_near.cu", "ves_step.cu", "ves_capi.cu", "ves_noalloc.cu", "ves_post.cu",
            "ves_nets.cu", "ves_nets_tc.cu", "ves_mlarm.cu", "ves_traj.cu",
-           "ves_repulsion.cu", "ves_rbf.cu", "ves_dl.cu"]
+           "ves_repulsion.cu", "ves_rbf.cu", "ves_dl.cu", "ves_targets.cu", "ves_train.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
          "--expt-relaxed-constexpr", "-diag-suppress", "550"]

@@ -193,6 +193,9 @@ void launch_align_center_angle(ves_ctx* c, int nv, const double* Xorg, const dou
 int post_correct_area_length(ves_ctx* c, int nv, const double* X, const double* area0, const double* length0,
                              double* Xout, int* outer_iters, WsCarver& ws, cudaStream_t s);
 
+// bending force of the MLARM step: bending of the Nup-upsampled shape truncated to N modes
+int launch_bend_up(ves_ctx* c, int nv, const double* X, double kappa, double* fB, cudaStream_t s);
+
 // vector kernels (GMRES)
 void launch_dot_partials(long long n, const double* a, const double* b, double* partials,
                          cudaStream_t s);

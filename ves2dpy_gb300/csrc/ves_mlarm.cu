@@ -861,6 +861,26 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
   return rc;
 }
 
+}  // namespace
+
+// fBend of the step (bending of the Nup-upsampled shape, truncated to N modes)
+// for callers outside the step (the training targets of ves_targets.cu)
+int launch_bend_up(ves_ctx* c, int nv, const double* X, double kappa, double* fB, cudaStream_t s) {
+  const int N = c->N, Nup = c->Nup;
+  const size_t sh = (size_t)(5 * Nup + 2 * N) * sizeof(double);
+  if (sh > 48 * 1024) {
+    int rc = ves_cuda_status(cudaFuncSetAttribute(bend_up_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh),
+                             "bend smem");
+    if (rc) return rc;
+  }
+  if (nv <= 0) return VES_OK;
+  ves_count_launch();
+  bend_up_kernel<<<nv, 256, sh, s>>>(N, Nup, c->m, c->pc, c->pcd, c->cosU, c->sinU, kappa, X, fB);
+  return ves_launch_check("bend_up");
+}
+
+namespace {
+
 int mlarm_step_run(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double* X, const double* ten,
                    const double* vback, const double* area0, const double* len0, double* Xout, double* ten_out,
                    ves_mlarm_result* res, const ves_mlarm_trace* tr, WsCarver& ws, cudaStream_t s) {

@@ -517,8 +517,10 @@ VES_API int ves_trainer_get_grads_f64(const ves_trainer* t, double* out, void* s
  * VES_STATIC_SCRATCH_BYTES bytes that belongs to the library image (held on
  * every GPU that loads the library until the process exits), so it performs
  * no allocation and needs no ves_ctx.  The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress); make that first call before
- * any stream capture.  Sizes whose scratch exceeds the array return
+ * array's device address (cudaGetSymbolAddress) and keeps it for the life of
+ * the device's primary context; make that first call before any stream
+ * capture, and make no call after a cudaDeviceReset in the same process (the
+ * kept address would be stale).  Sizes whose scratch exceeds the array return
  * VES_ERR_WORKSPACE.  All calls share the one array: calls that overlap on the
  * GPU race and must be serialised by the caller.  Synchronises ``stream``. */
 #define VES_STATIC_SCRATCH_BYTES (64u << 20)

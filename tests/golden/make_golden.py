@@ -151,7 +151,7 @@ def job_step(promote, which):
     torch = R.torch
     if which == 'c1':
         X = config1_suspension(32, 0)
-        dt, speed, nsteps = 1e-4, 2.0, 2 if promote else 1
+        dt, speed, nsteps = 1e-4, 2.0, 10 if promote else 1   # the configuration's 10 steps
     else:
         patch_exact_stokes_sl(R)
         X = small_cluster(nv=4, N=16, seed=1)
@@ -324,7 +324,9 @@ def job_mlarm(precision):
         wrap(type(oc), nm)
     ten = torch.zeros((N, nv), dtype=torch.float64)  # entry :121
     out = {"X0": X0, "Xinit": _np(Xinit), "area0": _np(area0), "len0": _np(len0)}
-    for step in range(2):
+    nsteps = 10 if precision == "fp64" else 2
+    out["nsteps"] = nsteps
+    for step in range(nsteps):
         with torch.no_grad():
             X, ten = m.time_step_many_noinfo(X, ten, 3)
         out[f"X{step + 1}"] = _np(X)
@@ -615,7 +617,27 @@ def job_dl(promote):
     return out
 
 
+def job_bgflow(promote):
+    """bg_flow (mytorch/tstep_biem.py:849-952) for every unconfined kind, with
+    non-default speed, channel width and vortex size, on a lattice suspension."""
+    import ref_shim
+    from ves2dpy_gb300.suspension import lattice_suspension
+    R = ref_shim.load(promote=promote)
+    torch = R.torch
+    X = lattice_suspension(3, 32, spacing=3.0, jitter=0.2, min_gap=0.3, seed=4)
+    N, nv = X.shape[0] // 2, X.shape[1]
+    Xt = torch.tensor(X, dtype=torch.float64)
+    prams, options = make_prams(R, N, nv, 1e-4, 1.0)
+    tt = R.tstep_biem.TStepBiem(Xt, None, options, prams)
+    out = {"X": X, "kinds": np.array(["relaxation", "extensional", "parabolic", "taylorGreen", "vortex", "shear"])}
+    for kind in out["kinds"]:
+        v = tt.bg_flow(Xt, None, str(kind), Speed=1.7, chanWidth=2.3, vortexSize=1.9)
+        out[f"v_{kind}"] = _np(v)
+    return out
+
+
 JOBS = {
+    'bgflow_fp64': (job_bgflow, True, ()),
     'dl_fp64': (job_dl, True, ()),
     'io_fp64': (job_io, True, ()),
     'step_rep_fp64': (job_step_rep, True, ()),

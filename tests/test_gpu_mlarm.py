@@ -94,7 +94,8 @@ def test_standardization_matches_reference(golden):
 
 
 def test_mlarm_step_fp64_matches_reference(golden):
-    """FP64 networks and far field: every stage and two steps at 1e-10."""
+    """FP64 networks and far field: every stage of the first step and each of
+    the recorded steps (10) at 1e-10."""
     g = golden("mlarm_fp64")
     m = _mlarm("fp64", "fp64")
     m.area0 = torch.from_numpy(g["area0"])
@@ -106,9 +107,29 @@ def test_mlarm_step_fp64_matches_reference(golden):
         assert rel(t[k], g[k]) < 1e-10, (k, rel(t[k], g[k]))
     assert rel(t["X"], g["X1"]) < 1e-10
     assert rel(t["ten"], g["ten1"]) < 1e-10
-    X2, t2 = m.time_step_many_noinfo(t["X"], t["ten"], 3)
-    assert rel(X2, g["X2"]) < 1e-10
-    assert rel(t2, g["ten2"]) < 1e-10
+    X, ten = t["X"], t["ten"]
+    nsteps = int(g["nsteps"]) if "nsteps" in g.files else 2
+    for step in range(2, nsteps + 1):
+        X, ten = m.time_step_many_noinfo(X, ten, 3)
+        assert rel(X, g[f"X{step}"]) < 1e-10, (step, rel(X, g[f"X{step}"]))
+        assert rel(ten, g[f"ten{step}"]) < 1e-10, (step, rel(ten, g[f"ten{step}"]))
+
+
+def test_autotuned_launch_shapes_give_the_fixed_rule_outputs():
+    """The autotuner (ves_net_set_autotune) only picks among launch shapes of
+    the same arithmetic: its outputs equal the fixed rule's bit for bit, on
+    the timing pass and after it."""
+    from ves2dpy_gb300.mlarm import Network
+    from ves2dpy_gb300.mlarm_weights import net_test_input
+    for name in ("adv", "near"):
+        sd = _state_dicts()[name]
+        x = torch.from_numpy(net_test_input(name, nv=48, seed=21))
+        y0 = Network(name, sd, "bf16", DEV, autotune=False)(x)
+        tuned = Network(name, sd, "bf16", DEV, autotune=True)
+        y1 = tuned(x)
+        y2 = tuned(x)
+        assert torch.equal(y0, y1), name
+        assert torch.equal(y0, y2), name
 
 
 def test_mlarm_step_fp32_networks(golden):

@@ -141,9 +141,12 @@ def _step(X, dt, speed, near="py_hh", ff="fp64", sl="fp64", sig=None):
 
 
 def test_time_step_config1_fp64(golden):
+    """The configuration's 10 steps, each against the reference's."""
     g = golden("step_c1_fp64")
     X, sig = g["X0"], None
-    for s in (1, 2):
+    nsteps = sum(1 for k in g.files if k.startswith("iter"))
+    assert nsteps == 10
+    for s in range(1, nsteps + 1):
         Xn, sn, _, _, it, iflag = _step(X, float(g["dt"]), float(g["speed"]), sig=sig)
         assert not iflag
         assert it == int(g[f"iter{s}"])
@@ -261,3 +264,17 @@ def test_time_step_with_repulsion_fp64(golden):
     assert not iflag and it == int(g["iter1"])
     assert rel(Xn, g["X1"]) < FP64_TOL, rel(Xn, g["X1"])
     assert rel(sn, g["sig1"]) < 1e-8, rel(sn, g["sig1"])
+
+
+def test_bg_flow(golden):
+    """ves_bg_flow against the reference's bg_flow (mytorch/tstep_biem.py:849-952)
+    for every unconfined kind, with non-default speed, width and vortex size."""
+    from ves2dpy_gb300.tstep_biem import TStepBiem
+    g = golden("bgflow_fp64")
+    X = g["X"]
+    N, nv = X.shape[0] // 2, X.shape[1]
+    prams = dict(dt=1e-4, kappa=1.0, gmresTol=1e-10, gmresMaxIter=100, farFieldSpeed=1.0, viscCont=[1.0] * nv)
+    tt = TStepBiem(T(X), None, dict(farField="shear", usePreco=True), prams)
+    for kind in g["kinds"]:
+        v = tt.bg_flow(T(X), None, str(kind), Speed=1.7, chanWidth=2.3, vortexSize=1.9)
+        assert rel(v, g[f"v_{kind}"]) < 1e-14, kind

@@ -105,7 +105,7 @@ def test_time_step(golden, fixture):
     prm = O.StepParams(dt=float(g["dt"]), speed=float(g["speed"]), gmres_tol=1e-10, gmres_maxiter=200)
     tab = O.PotenTables(N)
     sig = np.zeros((N, nv))
-    nsteps = 2 if "X2" in g.files else 1
+    nsteps = sum(1 for k in g.files if k.startswith("iter"))   # config 1: its 10 steps
     for s in range(1, nsteps + 1):
         res = O.time_step(X, sig, prm, tab)
         assert res.iters == int(g[f"iter{s}"])
@@ -141,3 +141,11 @@ def test_post_step_conditioning(golden, tag):
     assert rel(O.align_center_angle(X, g[f"redist5_{tag}"]), g[f"align_{tag}"]) < 1e-10
     Xc = O.correct_area_length(g[f"pert_{tag}"], g[f"a0_{tag}"], g[f"l0_{tag}"])
     assert rel(Xc, g[f"corrected_{tag}"]) < 1e-9
+
+
+def test_bg_flow(golden):
+    """bg_flow (mytorch/tstep_biem.py:849-952), every unconfined kind."""
+    g = golden("bgflow_fp64")
+    for kind in g["kinds"]:
+        v = O.bg_flow(g["X"], str(kind), speed=1.7, chan_width=2.3, vortex_size=1.9)
+        assert rel(v, g[f"v_{kind}"]) < 1e-14, kind

@@ -6,9 +6,11 @@ host calling in from a runtime where cudaMalloc would synchronise the device):
 its scratch is a fixed array inside the library image instead of a workspace
 the caller allocates.  The test calls it through the C ABI twice in a row and
 checks both results against the workspace-based ``ves_farfield`` at the same
-tolerances as the other parity tests, for FP64 and FP32C, and checks that a
-size whose scratch does not fit is rejected.  The file name makes pytest
-collect it last.
+tolerances as the other parity tests, for FP64, FP32C and FP32M (the
+multipole path), checks that the second call changes neither the device's
+free memory nor the caching allocator's reservation, and checks that a size
+whose scratch does not fit is rejected.  The file name makes pytest collect
+it last.
 """
 import ctypes
 
@@ -18,7 +20,7 @@ import torch
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp64": 1e-10, "fp32c": 1e-5}
+TOL = {"fp64": 1e-10, "fp32c": 1e-5, "fp32m": 1e-5}
 
 
 def _inputs(dev):
@@ -33,7 +35,7 @@ def _inputs(dev):
     return Xv, dv, self_idx, N, nv
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32c", "fp32m"])
 def test_static_scratch_matches_workspace_entry_twice(precision):
     from ves2dpy_gb300 import _native as nat
     dev = torch.device("cuda:0")
@@ -50,12 +52,18 @@ def test_static_scratch_matches_workspace_entry_twice(precision):
     refn = ref.cpu().numpy()
     scale = np.abs(refn).max()
     assert scale > 0
+    outs = [torch.full((nv, 2 * N), float("nan"), dtype=torch.float64, device=dev) for _ in range(2)]
     for call in range(2):
-        out = torch.full((nv, 2 * N), float("nan"), dtype=torch.float64, device=dev)
+        torch.cuda.synchronize(dev)
+        free0, reserved0 = torch.cuda.mem_get_info(dev)[0], torch.cuda.memory_reserved(dev)
         rc = lib.ves_farfield_static_scratch(prec, nv, N, Xv.data_ptr(), dv.data_ptr(), nv, N, Xv.data_ptr(),
-                                             self_idx.data_ptr(), out.data_ptr(), stream)
+                                             self_idx.data_ptr(), outs[call].data_ptr(), stream)
         nat.check(rc, f"static scratch call {call}")
-        err = np.abs(out.cpu().numpy() - refn).max() / scale
+        torch.cuda.synchronize(dev)
+        if call == 1:  # the first call may load the kernels; the second allocates nothing
+            assert torch.cuda.mem_get_info(dev)[0] == free0
+            assert torch.cuda.memory_reserved(dev) == reserved0
+        err = np.abs(outs[call].cpu().numpy() - refn).max() / scale
         assert err < TOL[precision], (precision, call, err)
 
 

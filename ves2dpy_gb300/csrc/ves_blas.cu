@@ -200,14 +200,16 @@ void launch_bgemv_f64(int nv, int m, int n, const double* A, const double* x, lo
 // piv[j] = row exchanged with row j at step j (LAPACK ipiv, 0-based).
 constexpr int LU_NB = 32;
 
-__global__ void __launch_bounds__(256) lu_factor_kernel(int n, double* __restrict__ A, int* __restrict__ piv,
+template <typename T>
+__global__ void __launch_bounds__(256) lu_factor_kernel(int n, T* __restrict__ A, int* __restrict__ piv,
                                                         VesDeviceStatus* st) {
-  extern __shared__ double sh[];
+  extern __shared__ __align__(16) unsigned char lu_sh[];
+  T* sh = (T*)lu_sh;
   const int k = blockIdx.x;
-  double* a = A + (long long)k * n * n;
+  T* a = A + (long long)k * n * n;
   int* pv = piv + (long long)k * n;
-  double* panel = sh;                 // [n][LU_NB]
-  double* U12 = sh + n * LU_NB;       // [LU_NB][n]
+  T* panel = sh;                 // [n][LU_NB]
+  T* U12 = sh + n * LU_NB;       // [LU_NB][n]
   __shared__ double red_v[256];
   __shared__ int red_i[256];
   __shared__ int s_piv;
@@ -226,7 +228,7 @@ __global__ void __launch_bounds__(256) lu_factor_kernel(int n, double* __restric
       double best = -1.0;
       int bi = n;
       for (int i = j + tid; i < rows; i += nt) {
-        const double v = fabs(panel[i * LU_NB + j]);
+        const double v = fabs((double)panel[i * LU_NB + j]);
         if (v > best) {
           best = v;
           bi = i;
@@ -255,14 +257,14 @@ __global__ void __launch_bounds__(256) lu_factor_kernel(int n, double* __restric
       const int ip = s_piv;
       if (ip != j) {
         for (int jj = tid; jj < nb; jj += nt) {
-          const double t = panel[j * LU_NB + jj];
+          const T t = panel[j * LU_NB + jj];
           panel[j * LU_NB + jj] = panel[ip * LU_NB + jj];
           panel[ip * LU_NB + jj] = t;
         }
       }
       __syncthreads();
-      const double d = panel[j * LU_NB + j];
-      const double rcp = (d != 0.0) ? 1.0 / d : 0.0;
+      const T d = panel[j * LU_NB + j];
+      const T rcp = (d != T(0)) ? T(1) / d : T(0);
       for (int i = j + 1 + tid; i < rows; i += nt) panel[i * LU_NB + j] *= rcp;
       __syncthreads();
       const int rem = nb - j - 1;
@@ -285,7 +287,7 @@ __global__ void __launch_bounds__(256) lu_factor_kernel(int n, double* __restric
       if (r2 != r1) {
         for (int c = tid; c < n; c += nt) {
           if (c >= p0 && c < p0 + nb) continue;
-          const double t = a[(long long)r1 * n + c];
+          const T t = a[(long long)r1 * n + c];
           a[(long long)r1 * n + c] = a[(long long)r2 * n + c];
           a[(long long)r2 * n + c] = t;
         }
@@ -296,14 +298,14 @@ __global__ void __launch_bounds__(256) lu_factor_kernel(int n, double* __restric
     if (ncol > 0) {
       // U12 = L11^{-1} A12 (unit lower triangular), one thread per column
       for (int c = tid; c < ncol; c += nt) {
-        double col[LU_NB];
+        T col[LU_NB];
 #pragma unroll
         for (int j = 0; j < LU_NB; ++j)
           if (j < nb) col[j] = a[(long long)(p0 + j) * n + p0 + nb + c];
 #pragma unroll
         for (int j = 0; j < LU_NB; ++j) {
           if (j >= nb) break;
-          const double v = col[j];
+          const T v = col[j];
           for (int i = j + 1; i < nb; ++i) col[i] = fma(-panel[i * LU_NB + j], v, col[i]);
         }
 #pragma unroll
@@ -318,8 +320,8 @@ __global__ void __launch_bounds__(256) lu_factor_kernel(int n, double* __restric
       const int m2 = rows - nb;
       for (long long idx = tid; idx < (long long)m2 * ncol; idx += nt) {
         const int i = (int)(idx / ncol), c = (int)(idx % ncol);
-        double s = a[(long long)(p0 + nb + i) * n + p0 + nb + c];
-        const double* l = panel + (nb + i) * LU_NB;
+        T s = a[(long long)(p0 + nb + i) * n + p0 + nb + c];
+        const T* l = panel + (nb + i) * LU_NB;
 #pragma unroll 8
         for (int j = 0; j < nb; ++j) s = fma(-l[j], U12[j * n + c], s);
         a[(long long)(p0 + nb + i) * n + p0 + nb + c] = s;
@@ -329,32 +331,42 @@ __global__ void __launch_bounds__(256) lu_factor_kernel(int n, double* __restric
   }
 }
 
-int launch_lu_factor(ves_ctx* c, int nv, int n, double* A, int* piv, cudaStream_t s) {
+template <typename T>
+static int lu_factor_t(ves_ctx* c, int nv, int n, T* A, int* piv, cudaStream_t s) {
   if (nv <= 0) return VES_OK;
-  const size_t sh = (size_t)(n * LU_NB + LU_NB * n) * sizeof(double);
+  const size_t sh = (size_t)(n * LU_NB + LU_NB * n) * sizeof(T);
   if (sh > 220 * 1024) {
     ves_record_error(VES_ERR_SHAPE, "lu_factor: n=%d too large", n);
     return VES_ERR_SHAPE;
   }
   if (sh > 32 * 1024) {  // dynamic + static shared memory must fit the opt-in limit
     int rc = ves_cuda_status(
-        cudaFuncSetAttribute(lu_factor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh),
+        cudaFuncSetAttribute(lu_factor_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sh),
         "lu_factor smem attribute");
     if (rc) return rc;
   }
   ves_count_launch();
-  lu_factor_kernel<<<nv, 256, sh, s>>>(n, A, piv, c->status);
+  lu_factor_kernel<T><<<nv, 256, sh, s>>>(n, A, piv, c->status);
   return ves_launch_check("lu_factor");
+}
+
+int launch_lu_factor(ves_ctx* c, int nv, int n, double* A, int* piv, cudaStream_t s) {
+  return lu_factor_t<double>(c, nv, n, A, piv, s);
+}
+
+int launch_lu_factor_f32(ves_ctx* c, int nv, int n, float* A, int* piv, cudaStream_t s) {
+  return lu_factor_t<float>(c, nv, n, A, piv, s);
 }
 
 // x = LU^{-1} P b per vesicle.  Blocks of 32 rows: the off-diagonal part is a
 // warp-parallel GEMV, the 32x32 diagonal block is solved by one warp.
-__global__ void __launch_bounds__(256) lu_solve_kernel(int n, const double* __restrict__ LU,
+template <typename T>
+__global__ void __launch_bounds__(256) lu_solve_kernel(int n, const T* __restrict__ LU,
                                                        const int* __restrict__ piv,
                                                        const double* __restrict__ b, double* __restrict__ x) {
   extern __shared__ double xs[];
   const int k = blockIdx.x;
-  const double* a = LU + (long long)k * n * n;
+  const T* a = LU + (long long)k * n * n;
   const int* pv = piv + (long long)k * n;
   const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32, nw = blockDim.x / 32;
   for (int i = tid; i < n; i += blockDim.x) xs[i] = b[(long long)k * n + i];
@@ -375,7 +387,7 @@ __global__ void __launch_bounds__(256) lu_solve_kernel(int n, const double* __re
     const int nr = min(32, n - r0);
     for (int r = warp; r < nr; r += nw) {
       double s = 0.0;
-      for (int c = lane; c < r0; c += 32) s = fma(a[(long long)(r0 + r) * n + c], xs[c], s);
+      for (int c = lane; c < r0; c += 32) s = fma((double)a[(long long)(r0 + r) * n + c], xs[c], s);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
       if (lane == 0) xs[r0 + r] -= s;
@@ -385,7 +397,7 @@ __global__ void __launch_bounds__(256) lu_solve_kernel(int n, const double* __re
       double v = (lane < nr) ? xs[r0 + lane] : 0.0;
       for (int j = 0; j < nr; ++j) {
         const double xj = __shfl_sync(0xffffffffu, v, j);
-        if (lane > j && lane < nr) v = fma(-a[(long long)(r0 + lane) * n + r0 + j], xj, v);
+        if (lane > j && lane < nr) v = fma(-(double)a[(long long)(r0 + lane) * n + r0 + j], xj, v);
       }
       if (lane < nr) xs[r0 + lane] = v;
     }
@@ -396,7 +408,7 @@ __global__ void __launch_bounds__(256) lu_solve_kernel(int n, const double* __re
     const int r0 = max(0, r1 - 32), nr = r1 - r0;
     for (int r = warp; r < nr; r += nw) {
       double s = 0.0;
-      for (int c = r1 + lane; c < n; c += 32) s = fma(a[(long long)(r0 + r) * n + c], xs[c], s);
+      for (int c = r1 + lane; c < n; c += 32) s = fma((double)a[(long long)(r0 + r) * n + c], xs[c], s);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
       if (lane == 0) xs[r0 + r] -= s;
@@ -407,10 +419,10 @@ __global__ void __launch_bounds__(256) lu_solve_kernel(int n, const double* __re
       for (int j = nr - 1; j >= 0; --j) {
         double vj = __shfl_sync(0xffffffffu, v, j);
         if (lane == j) {
-          v = v / a[(long long)(r0 + j) * n + r0 + j];
+          v = v / (double)a[(long long)(r0 + j) * n + r0 + j];
         }
         vj = __shfl_sync(0xffffffffu, v, j);
-        if (lane < j) v = fma(-a[(long long)(r0 + lane) * n + r0 + j], vj, v);
+        if (lane < j) v = fma(-(double)a[(long long)(r0 + lane) * n + r0 + j], vj, v);
       }
       if (lane < nr) xs[r0 + lane] = v;
     }
@@ -423,7 +435,15 @@ void launch_lu_solve(int nv, int n, const double* LU, const int* piv, const doub
                      cudaStream_t s) {
   if (nv <= 0) return;
   ves_count_launch();
-  lu_solve_kernel<<<nv, 256, (size_t)n * sizeof(double), s>>>(n, LU, piv, b, x);
+  lu_solve_kernel<double><<<nv, 256, (size_t)n * sizeof(double), s>>>(n, LU, piv, b, x);
+}
+
+// the same solve with an FP32 factorisation (FP64 right-hand side, FP64 sums)
+void launch_lu_solve_f32(int nv, int n, const float* LU, const int* piv, const double* b, double* x,
+                         cudaStream_t s) {
+  if (nv <= 0) return;
+  ves_count_launch();
+  lu_solve_kernel<float><<<nv, 256, (size_t)n * sizeof(double), s>>>(n, LU, piv, b, x);
 }
 
 // ----------------------------------------------------------------------------

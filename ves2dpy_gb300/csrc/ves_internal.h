@@ -112,6 +112,10 @@ void launch_density(int nv, int ns, const double* f, const double* sa, double* d
 int derivs_and_precond(ves_ctx* c, int nv, const double* isa, const double* tang, const double* G,
                        double dt, double kappa, double* Ben, double* Ten, double* Div, double* M,
                        WsCarver& ws, cudaStream_t s, const double* Dm = nullptr, const double* alpha = nullptr);
+// the block-diagonal preconditioner of derivs_and_precond built with FP32
+// products into M32 [nv][3N][3N] (no viscosity contrast)
+int precond_f32(ves_ctx* c, int nv, const double* isa, const double* tang, const double* G, double dt, double kappa,
+                float* M32, WsCarver& ws, cudaStream_t s);
 
 // dense per-vesicle algebra
 void launch_bgemm_f64(int batch, int M, int N, int K, double alpha, const double* A, int lda,
@@ -125,6 +129,10 @@ void launch_bgemv_f64(int nv, int m, int n, const double* A, const double* x, lo
 int launch_lu_factor(ves_ctx* c, int nv, int n, double* A, int* piv, cudaStream_t s);
 void launch_lu_solve(int nv, int n, const double* LU, const int* piv, const double* b, double* x,
                      cudaStream_t s);
+// FP32 factorisation / solve with it (FP64 vectors)
+int launch_lu_factor_f32(ves_ctx* c, int nv, int n, float* A, int* piv, cudaStream_t s);
+void launch_lu_solve_f32(int nv, int n, const float* LU, const int* piv, const double* b, double* x,
+                         cudaStream_t s);
 
 // Alpert
 int alpert_sl_matrix(ves_ctx* c, int nv, const double* X, int precision, double* G, WsCarver& ws,

@@ -10,8 +10,10 @@
 //   library holds it until the process exits.
 // * Host code cannot use the array's name as a device address.  The first
 //   call on each device resolves the address with cudaGetSymbolAddress (with
-//   that device current) and caches it; make that first call before any stream
-//   capture.
+//   that device current) and caches it for the life of the device's primary
+//   context; make that first call before any stream capture, and make no call
+//   after a cudaDeviceReset in the same process (the cached address would be
+//   stale).
 // * Every call shares the array and leaves its contents behind; the status
 //   word is cleared at the start of each call and every other byte a call
 //   reads is written earlier in the same call.  Calls that overlap on the GPU

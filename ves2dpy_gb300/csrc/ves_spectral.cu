@@ -554,6 +554,56 @@ __global__ void assemble_precond_kernel(int N, double dt, double kappa, const do
   }
 }
 
+__global__ void arc_deriv_matrix_f32_kernel(int N, const double* __restrict__ dstencil,
+                                            const double* __restrict__ isa, float* __restrict__ Are,
+                                            float* __restrict__ Aim) {
+  const int k = blockIdx.y;
+  const long long base = (long long)k * N * N;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < N * N; idx += gridDim.x * blockDim.x) {
+    const int j = idx / N, l = idx % N;
+    const double is = isa[(long long)k * N + j];
+    const int r = ((j - l) % N + N) % N;
+    Are[base + idx] = (float)(is * dstencil[r]);
+    Aim[base + idx] = (float)(is * (((j - l) & 1) ? 0.5 : -0.5));
+  }
+}
+
+__global__ void ten_div_f32_kernel(int N, const float* __restrict__ Are, const double* __restrict__ tang,
+                                   float* __restrict__ Ten, float* __restrict__ Div) {
+  const int k = blockIdx.y;
+  const long long tb = (long long)k * 2 * N;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < N * N; idx += gridDim.x * blockDim.x) {
+    const int j = idx / N, l = idx % N;
+    const float a = Are[(long long)k * N * N + idx];
+    Ten[(long long)k * 2 * N * N + (long long)j * N + l] = a * (float)tang[tb + l];
+    Ten[(long long)k * 2 * N * N + (long long)(N + j) * N + l] = a * (float)tang[tb + N + l];
+    Div[(long long)k * N * 2 * N + (long long)j * 2 * N + l] = (float)tang[tb + j] * a;
+    Div[(long long)k * N * 2 * N + (long long)j * 2 * N + N + l] = (float)tang[tb + N + j] * a;
+  }
+}
+
+__global__ void to_f32_kernel(long long n, const double* __restrict__ a, float* __restrict__ b) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = (float)a[i];
+}
+
+__global__ void assemble_precond_f32_kernel(int N, float dt, float kappa, const float* __restrict__ GB,
+                                            const float* __restrict__ GT, const float* __restrict__ Div,
+                                            float* __restrict__ M) {
+  const int k = blockIdx.y;
+  const int n3 = 3 * N, n2 = 2 * N;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n3 * n3; idx += gridDim.x * blockDim.x) {
+    const int r = idx / n3, cc = idx % n3;
+    float v;
+    if (r < n2)
+      v = cc < n2 ? (r == cc ? 1.0f : 0.0f) + dt * kappa * GB[(long long)k * n2 * n2 + (long long)r * n2 + cc]
+                  : -dt * GT[(long long)k * n2 * N + (long long)r * N + (cc - n2)];
+    else
+      v = (cc < n2) ? Div[(long long)k * N * n2 + (long long)(r - n2) * n2 + cc] : 0.0f;
+    M[(long long)k * n3 * n3 + idx] = v;
+  }
+}
+
 // D4 = Re(C*C) with C = A*A, complex A = Are + i Aim, via real products:
 // C = (Are Are - Aim Aim) + i (Are Aim + Aim Are); D4 = Cr Cr - Ci Ci.
 int derivs_and_precond(ves_ctx* c, int nv, const double* isa, const double* tang, const double* G,
@@ -606,4 +656,49 @@ int derivs_and_precond(ves_ctx* c, int nv, const double* isa, const double* tang
     assemble_precond_kernel<<<g3, 256, 0, s>>>(N, dt, kappa, GB, GT, Div, Dm, alpha, M);
   }
   return ves_launch_check("derivs_and_precond");
+}
+
+// The preconditioner of derivs_and_precond (tstep_biem.py:653-711) with every
+// product in FP32: [I + dt k G Ben, -dt G Ten; Div, 0] in FP32, for an FP32
+// factorisation (GMRES only needs an approximate inverse).
+int precond_f32(ves_ctx* c, int nv, const double* isa, const double* tang, const double* G, double dt, double kappa,
+                float* M32, WsCarver& ws, cudaStream_t s) {
+  const int N = c->N;
+  const size_t NN = (size_t)N * N;
+  float* Are = ws.take<float>(NN * nv);
+  float* Aim = ws.take<float>(NN * nv);
+  float* Cr = ws.take<float>(NN * nv);
+  float* Ci = ws.take<float>(NN * nv);
+  float* D4 = ws.take<float>(NN * nv);
+  float* Ten = ws.take<float>(2 * NN * nv);
+  float* Div = ws.take<float>(2 * NN * nv);
+  float* G32 = ws.take<float>(4 * NN * nv);
+  float* GB = ws.take<float>(4 * NN * nv);
+  float* GT = ws.take<float>(2 * NN * nv);
+  if (ws.sizing) return VES_OK;
+  if (!ws.ok()) {
+    ves_record_error(VES_ERR_WORKSPACE, "precond_f32: workspace too small");
+    return VES_ERR_WORKSPACE;
+  }
+  if (nv <= 0) return VES_OK;
+  dim3 grid(ceil_div(NN, 256), nv);
+  ves_count_launch(3);
+  arc_deriv_matrix_f32_kernel<<<grid, 256, 0, s>>>(N, c->d1N, isa, Are, Aim);
+  ten_div_f32_kernel<<<grid, 256, 0, s>>>(N, Are, tang, Ten, Div);
+  to_f32_kernel<<<ceil_div((long long)4 * NN * nv, 256), 256, 0, s>>>((long long)4 * NN * nv, G, G32);
+  const long long sN = (long long)NN;
+  launch_bgemm_f32(nv, N, N, N, 1.0f, Are, N, sN, Are, N, sN, 0.0f, Cr, N, sN, s);
+  launch_bgemm_f32(nv, N, N, N, -1.0f, Aim, N, sN, Aim, N, sN, 1.0f, Cr, N, sN, s);
+  launch_bgemm_f32(nv, N, N, N, 1.0f, Are, N, sN, Aim, N, sN, 0.0f, Ci, N, sN, s);
+  launch_bgemm_f32(nv, N, N, N, 1.0f, Aim, N, sN, Are, N, sN, 1.0f, Ci, N, sN, s);
+  launch_bgemm_f32(nv, N, N, N, 1.0f, Cr, N, sN, Cr, N, sN, 0.0f, D4, N, sN, s);
+  launch_bgemm_f32(nv, N, N, N, -1.0f, Ci, N, sN, Ci, N, sN, 1.0f, D4, N, sN, s);
+  const long long sG = 4 * sN;
+  launch_bgemm_f32(nv, 2 * N, N, N, 1.0f, G32, 2 * N, sG, D4, N, sN, 0.0f, GB, 2 * N, sG, s);
+  launch_bgemm_f32(nv, 2 * N, N, N, 1.0f, G32 + N, 2 * N, sG, D4, N, sN, 0.0f, GB + N, 2 * N, sG, s);
+  launch_bgemm_f32(nv, 2 * N, N, 2 * N, 1.0f, G32, 2 * N, sG, Ten, N, 2 * sN, 0.0f, GT, N, 2 * sN, s);
+  dim3 g3(ceil_div(9 * NN, 256), nv);
+  ves_count_launch();
+  assemble_precond_f32_kernel<<<g3, 256, 0, s>>>(N, (float)dt, (float)kappa, GB, GT, Div, M32);
+  return ves_launch_check("precond_f32");
 }

@@ -65,6 +65,10 @@ def parse():
                     help="fixed launch shapes for the network kernels (no timing of the shapes on the first step)")
     ap.add_argument("--only-net", default=None, help="time one network's forward pass at --nv and exit "
                     "(relax, adv, near, selften, advten)")
+    ap.add_argument("--synthetic-weights", action="store_true",
+                    help="seeded synthetic networks instead of the trained ones in ves2dpy_gb300/trained")
+    ap.add_argument("--biem-precond", default="fp32", choices=["fp32", "fp64"],
+                    help="precision of the BIEM step's block-diagonal preconditioner (GMRES solves the FP64 system)")
     return ap.parse_args()
 
 
@@ -216,9 +220,30 @@ def _events():
     return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
 
-def run_mlarm(a, dev, X0, state_dicts):
+def networks(a):
+    """(state dicts, normalisation arrays, description): the trained networks
+    of ves2dpy_gb300/trained (ves2dpy_gb300.train_surrogate) unless
+    --synthetic-weights or none are present."""
+    from ves2dpy_gb300 import training as TR
+    from ves2dpy_gb300.mlarm_weights import NETS, synthetic_norms, synthetic_state_dict
+    if not a.synthetic_weights and TR.have_trained():
+        sds, norms = TR.load()
+        log = {}
+        try:
+            log = json.load(open(os.path.join(TR.TRAINED_DIR, "train_log.json")))
+        except Exception:
+            pass
+        val = {k: v.get("validation_rel_error") for k, v in log.get("nets", {}).items()}
+        return sds, norms, {"weights": "trained on BIEM-generated data (ves2dpy_gb300/trained)",
+                            "validation_rel_error_vs_biem": val, "training_shapes": log.get("shapes")}
+    return ({n: synthetic_state_dict(n, 0) for n in NETS}, synthetic_norms(0),
+            {"weights": "seeded synthetic (untrained)"})
+
+
+def run_mlarm(a, dev, X0, state_dicts, norms=None):
     """Timed MLARM steps on the device (inputs resident), then one end-to-end
     step through MLARM_manyfree_py with pinned host buffers."""
+    import numpy as np
     import torch
     from ves2dpy_gb300 import _native as nat
     from ves2dpy_gb300.curve import Curve
@@ -227,7 +252,7 @@ def run_mlarm(a, dev, X0, state_dicts):
     from ves2dpy_gb300.replicas import barrier
 
     N, nv = a.N, a.nv
-    nrm = {k: torch.from_numpy(v) for k, v in synthetic_norms(0).items()}
+    nrm = {k: torch.from_numpy(np.asarray(v, dtype=np.float64)) for k, v in (norms or synthetic_norms(0)).items()}
 
     def vinf(X):  # shear, rate 2 (entry_driver_manyfreeSpaceVesicle_N128.py:53)
         n = X.shape[0] // 2
@@ -324,7 +349,7 @@ def run_biem(a, dev, X0):
     prams = dict(STEP, viscCont=[1.0] * nv, gmresTol=a.biem_tol)
     Xd = torch.tensor(X0, dtype=torch.float64, device=dev)
     tt = TStepBiem(Xd, None, options, prams, near="py_hh", farfield_precision=a.precision,
-                   sl_precision="fp64" if a.precision == "fp64" else "fp32c")
+                   sl_precision="fp64" if a.precision == "fp64" else "fp32c", precond_precision=a.biem_precond)
     ctx = nat.context(N, dev)
     ws = ctx.workspace(tt.workspace_bytes())
     Xv = to_vm(Xd)
@@ -385,8 +410,8 @@ def run_gb300(a, rank, world):
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
     X0 = workload(a.nv, a.N, a.area_fraction, seed=rank)
-    sds = {n: synthetic_state_dict(n, 0) for n in NETS}
-    r = run_mlarm(a, dev, X0, sds)
+    sds, norms, net_info = networks(a)
+    r = run_mlarm(a, dev, X0, sds, norms)
     t_max, value = aggregate(r["ms"], float(a.nv * a.steps), dev)
     ms_per_step = t_max / a.steps
     b = None if a.no_biem else run_biem(a, dev, r["Xw"])
@@ -467,13 +492,15 @@ def run_gb300(a, rank, world):
                   ("multipole series for separated vesicle pairs, compensated direct sums for close pairs"
                    if a.precision == "fp32m" else "compensated direct sums" if a.precision == "fp32c" else "f64") +
                   ") + f64 geometry"),
-        "data": "synthetic (seeded suspension generator and seeded network weights of the reference "
-                "architectures; the reference's trained weights and initial conditions are absent)",
+        "data": "synthetic (seeded suspension generator; networks of the reference architectures "
+                + ("trained here on BIEM-generated shapes and targets" if "trained" in net_info["weights"]
+                   else "with seeded synthetic weights") +
+                "; the reference's trained weights and initial conditions are absent)",
         "config": {
             "workload": f"MLARM step (time_step_many_noinfo, nlayers=3) vs plain BIEM step (TStepBiem.time_step), "
                         f"nv={a.nv}, N={a.N}, Nup=1536, unit-length vesicles of reduced area 0.65, area fraction "
                         f"{a.area_fraction}, shear rate 2, dt=1e-5",
-            "networks": a.nets, "farfield_precision": a.precision,
+            "networks": a.nets, "network_weights": net_info, "farfield_precision": a.precision,
             "network_autotune": not a.no_autotune,
             "l2": "inputs larger than L2 (network activations 11 GB, upsampled sources 50 MB x 2 + near lists, "
                   "per step)",
@@ -498,6 +525,7 @@ def run_gb300(a, rank, world):
     }
     if b is not None:
         out["config"]["biem"] = {"value": vb, "unit": "vesicle-steps/s", "ms_per_step": tb / a.biem_steps,
+                                 "preconditioner": a.biem_precond,
                                  "steps": a.biem_steps, "warmup": a.biem_warmup, "matvecs_per_step": b["matvecs"],
                                  "gmres_info_resid": b["info"], "gmres_tol": a.biem_tol,
                                  "note": "the context, kernels and workspace are warm from the MLARM run; same "
@@ -511,8 +539,10 @@ def run_gb300(a, rank, world):
                 raise ValueError("no end-to-end step")
             out["config"]["centroid_velocity_error_vs_biem"] = centroid_velocity_error(
                 r["Xw"], r["X1"], b["X1"], STEP["dt"], dev)
-            out["config"]["velocity_error_note"] = ("networks carry synthetic untrained weights, so the surrogate "
-                                                    "velocity is not a physical prediction")
+            out["config"]["velocity_error_note"] = (
+                "relative 2-norm over vesicles of the physical-centre velocity of one MLARM step against one BIEM "
+                "step from the same state (the timed steps' starting state)" +
+                ("" if "trained" in net_info["weights"] else "; synthetic untrained weights: not a physical prediction"))
         except Exception:
             pass
     return out, sds, (b["matvecs"] if b is not None else None)

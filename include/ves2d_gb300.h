@@ -250,7 +250,10 @@ typedef struct ves_step_params {
   double gmres_tol;      /* relative tolerance (scipy rtol) */
   int gmres_maxiter;     /* outer restart cycles (scipy maxiter) */
   int gmres_restart;     /* 20 = scipy default */
-  int use_preco;         /* block-diagonal LU preconditioner (tstep_biem.py:653-711) */
+  int use_preco;         /* block-diagonal LU preconditioner (tstep_biem.py:653-711):
+                            0 none, 1 FP64, 2 built and factored in FP32 (FP64
+                            vectors; GMRES absorbs the difference; FP64 when a
+                            viscosity contrast is present) */
   int flow;              /* VES_FLOW_* */
   double speed, chan_width, vortex_size;
   int near_scheme;       /* VES_NEAR_* */
@@ -577,8 +580,10 @@ typedef struct ves_stats {
 VES_API int ves_ctx_set_timing(ves_ctx* ctx, int on);
 /* Read (and with reset != 0 clear) the counters; synchronises pending events. */
 VES_API int ves_ctx_stats(ves_ctx* ctx, ves_stats* out, int reset);
-/* Measured MUFU throughput of this GPU: lg2.approx + rcp.approx operations
- * per second over all SMs (a ~0.1 s probe on ``stream``). */
+/* Measurement hook (not part of any step): the MUFU throughput of this GPU,
+ * lg2.approx + rcp.approx operations per second over all SMs (a ~0.1 s probe
+ * on ``stream``); the denominator of the direct all-pairs kernel's roofline,
+ * which no vendor figure gives. */
 VES_API int ves_probe_sfu_peak(double* ops_per_second, void* stream);
 /* Failure-path check: a kernel waits on an mbarrier that nothing completes,
  * with the bounded wait of the tensor-core kernels (2^20 polls with sleeps:

@@ -278,3 +278,26 @@ def test_bg_flow(golden):
     for kind in g["kinds"]:
         v = tt.bg_flow(T(X), None, str(kind), Speed=1.7, chanWidth=2.3, vortexSize=1.9)
         assert rel(v, g[f"v_{kind}"]) < 1e-14, kind
+
+
+@pytest.mark.parametrize("ff", ["fp64", "fp32m"])
+def test_fp32_preconditioner_gives_the_fp64_preconditioned_step(golden, ff):
+    """The block-diagonal preconditioner built and factored in FP32 (the FP64
+    system is still what GMRES solves): the step's result within GMRES's
+    tolerance of the FP64-preconditioned step's, at most two more matvecs."""
+    from ves2dpy_gb300.tstep_biem import TStepBiem
+    g = golden("step_c1_fp64")
+    X = g["X0"]
+    N, nv = X.shape[0] // 2, X.shape[1]
+    tol = 1e-10 if ff == "fp64" else 1e-8
+    prams = dict(dt=float(g["dt"]), kappa=1.0, gmresTol=tol, gmresMaxIter=200, farFieldSpeed=float(g["speed"]),
+                 viscCont=[1.0] * nv)
+    out = {}
+    for pp in ("fp64", "fp32"):
+        tt = TStepBiem(T(X), None, dict(farField="shear", usePreco=True), prams, farfield_precision=ff,
+                       sl_precision="fp64" if ff == "fp64" else "fp32c", precond_precision=pp)
+        Xn, sn, _, _, it, iflag = tt.time_step(T(X), torch.zeros(N, nv, dtype=torch.float64, device=dev()))
+        assert not iflag
+        out[pp] = (Xn.cpu().numpy(), it)
+    assert rel(out["fp32"][0], out["fp64"][0]) < 10 * tol
+    assert out["fp32"][1] <= out["fp64"][1] + 2, (out["fp32"][1], out["fp64"][1])

@@ -236,11 +236,18 @@ int matvec(StepState& S, const double* v, double* out) {
   return ves_launch_check("matvec");
 }
 
+// use_preco == 2: the block-diagonal preconditioner built and factored in
+// FP32 (no viscosity contrast); otherwise FP64
+static bool precond_is_f32(const ves_step_params* prm) { return prm->use_preco == 2 && prm->visc_cont == nullptr; }
+
 int psolve(StepState& S, const double* z, double* out) {
   if (!S.prm->use_preco) {
     return ves_cuda_status(cudaMemcpyAsync(out, z, S.n * sizeof(double), cudaMemcpyDeviceToDevice, S.s), "psolve copy");
   }
-  launch_lu_solve(S.nv, 3 * S.N, S.LU, S.piv, z, out, S.s);
+  if (precond_is_f32(S.prm))
+    launch_lu_solve_f32(S.nv, 3 * S.N, (const float*)S.LU, S.piv, z, out, S.s);
+  else
+    launch_lu_solve(S.nv, 3 * S.N, S.LU, S.piv, z, out, S.s);
   return ves_launch_check("psolve");
 }
 
@@ -333,8 +340,13 @@ int psolve(MixedState& M, const double* z, double* out) {
     return ves_cuda_status(cudaMemcpyAsync(out, z, M.n * sizeof(double), cudaMemcpyDeviceToDevice, M.s),
                            "psolve copy");
   }
-  for (int g = 0; g < M.ng; ++g)
-    launch_lu_solve(M.g[g].nv, 3 * M.g[g].N, M.g[g].LU, M.g[g].piv, z + M.off[g], out + M.off[g], M.s);
+  for (int g = 0; g < M.ng; ++g) {
+    if (precond_is_f32(M.prm))
+      launch_lu_solve_f32(M.g[g].nv, 3 * M.g[g].N, (const float*)M.g[g].LU, M.g[g].piv, z + M.off[g],
+                          out + M.off[g], M.s);
+    else
+      launch_lu_solve(M.g[g].nv, 3 * M.g[g].N, M.g[g].LU, M.g[g].piv, z + M.off[g], out + M.off[g], M.s);
+  }
   return ves_launch_check("psolve mixed");
 }
 
@@ -570,6 +582,9 @@ static int biem_step_impl(ves_ctx* c, const ves_step_params* prm, int nv, const 
     w.take<double>((size_t)nv * 2 * N * N);  // Ten
     w.take<double>((size_t)nv * 2 * N * N);  // Div
     scratch = std::max(scratch, w.off);
+    WsCarver w2(nullptr, 0);
+    precond_f32(c, nv, nullptr, nullptr, nullptr, 0, 0, nullptr, w2, s);
+    scratch = std::max(scratch, w2.off);
   }
   {
     WsCarver w(nullptr, 0);
@@ -707,7 +722,11 @@ static int biem_step_impl(ves_ctx* c, const ves_step_params* prm, int nv, const 
     if ((rc = ves_cuda_status(cudaMemsetAsync(B.x, 0, n * sizeof(double), s), "x0"))) goto done;
   }
   // preconditioner
-  if (prm->use_preco) {
+  if (prm->use_preco && precond_is_f32(prm)) {
+    WsCarver sub(S.scratch, S.scratch_bytes);
+    if ((rc = precond_f32(c, nv, S.isa, S.tang, S.G, prm->dt, prm->kappa, (float*)S.LU, sub, s))) goto done;
+    if ((rc = launch_lu_factor_f32(c, nv, 3 * N, (float*)S.LU, S.piv, s))) goto done;
+  } else if (prm->use_preco) {
     WsCarver sub(S.scratch, S.scratch_bytes);
     double* Ben = nullptr;
     double* Ten = sub.take<double>((size_t)nv * 2 * N * N);
@@ -870,6 +889,9 @@ static int biem_step_mixed_impl(int ng, ves_ctx* const* ctx, const ves_step_para
       w.take<double>((size_t)nv * 2 * N * N);  // Ten
       w.take<double>((size_t)nv * 2 * N * N);  // Div
       scratch = std::max(scratch, w.off);
+      WsCarver w2(nullptr, 0);
+      precond_f32(c, nv, nullptr, nullptr, nullptr, 0, 0, nullptr, w2, s);
+      scratch = std::max(scratch, w2.off);
     }
     {
       WsCarver w(nullptr, 0);
@@ -971,11 +993,17 @@ static int biem_step_mixed_impl(int ng, ves_ctx* const* ctx, const ves_step_para
       ves_count_launch();
       pack_kernel<<<ceil_div(S.n, 256), 256, 0, s>>>(nv, N, S.X, sigma[g], B.x + M.off[g]);
       WsCarver sub(M.scratch, M.scratch_bytes);
-      double* Ten = sub.take<double>((size_t)nv * 2 * N * N);
-      double* Div = sub.take<double>((size_t)nv * 2 * N * N);
-      if ((rc = derivs_and_precond(S.c, nv, S.isa, S.tang, S.G, prm->dt, prm->kappa, nullptr, Ten, Div, S.LU, sub, s)))
-        return rc;
-      if ((rc = launch_lu_factor(S.c, nv, 3 * N, S.LU, S.piv, s))) return rc;
+      if (precond_is_f32(prm)) {
+        if ((rc = precond_f32(S.c, nv, S.isa, S.tang, S.G, prm->dt, prm->kappa, (float*)S.LU, sub, s))) return rc;
+        if ((rc = launch_lu_factor_f32(S.c, nv, 3 * N, (float*)S.LU, S.piv, s))) return rc;
+      } else {
+        double* Ten = sub.take<double>((size_t)nv * 2 * N * N);
+        double* Div = sub.take<double>((size_t)nv * 2 * N * N);
+        if ((rc = derivs_and_precond(S.c, nv, S.isa, S.tang, S.G, prm->dt, prm->kappa, nullptr, Ten, Div, S.LU, sub,
+                                     s)))
+          return rc;
+        if ((rc = launch_lu_factor(S.c, nv, 3 * N, S.LU, S.piv, s))) return rc;
+      }
     }
   }
   if (!prm->use_preco && n > 0)

@@ -31,7 +31,7 @@ class TStepBiem:
     """
 
     def __init__(self, X, Xwalls, options, prams, near: str = "py_hh", farfield_precision: str = "fp32c",
-                 sl_precision: str = "fp32c", device=None):
+                 sl_precision: str = "fp32c", device=None, precond_precision: str = "fp64"):
         if Xwalls is not None:
             raise NotImplementedError("confined flows (walls) are not supported by the device stepper")
         X = as_device_f64(X, device)
@@ -61,6 +61,9 @@ class TStepBiem:
         if self.repulsion and near not in ("py_hh", "py_rbf"):
             raise NotImplementedError("repulsion needs near='py_hh' or 'py_rbf' (naiveNearZoneInfo lists)")
         self.near = near
+        if precond_precision not in ("fp64", "fp32"):
+            raise ValueError("precond_precision: 'fp64' or 'fp32'")
+        self.precond_precision = precond_precision
         self.farfield_precision = farfield_precision
         self.sl_precision = sl_precision
         from .poten import Poten
@@ -81,7 +84,7 @@ class TStepBiem:
         p.gmres_tol = self.gmresTol
         p.gmres_maxiter = self.gmresMaxIter
         p.gmres_restart = 20
-        p.use_preco = 1 if self.usePreco else 0
+        p.use_preco = (2 if self.precond_precision == "fp32" else 1) if self.usePreco else 0
         flow = self.options.get("farField", "shear")
         if flow not in nat.FLOW:
             raise ValueError("Unknown or missing flow type in bg_flow.")
@@ -185,7 +188,7 @@ class TStepBiemMixed:
     """
 
     def __init__(self, Xs, options, prams, near: str = "matlab", farfield_precision: str = "fp32c",
-                 sl_precision: str = "fp32c", device=None):
+                 sl_precision: str = "fp32c", device=None, precond_precision: str = "fp64"):
         if near not in ("matlab", "none"):
             raise NotImplementedError("TStepBiemMixed: near must be 'matlab' or 'none'")
         if not 1 <= len(Xs) <= 4:
@@ -193,7 +196,8 @@ class TStepBiemMixed:
         if options.get("repulsion", False):
             raise NotImplementedError("TStepBiemMixed: no repulsion between groups")
         self.groups = [TStepBiem(X, None, options, prams, near=near, farfield_precision=farfield_precision,
-                                 sl_precision=sl_precision, device=device) for X in Xs]
+                                 sl_precision=sl_precision, device=device, precond_precision=precond_precision)
+                       for X in Xs]
         if any(g._visc is not None for g in self.groups):
             raise NotImplementedError("TStepBiemMixed: no viscosity contrast")
         if any(g.nv < 1 for g in self.groups):

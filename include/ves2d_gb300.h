@@ -415,10 +415,20 @@ typedef struct ves_mlarm_params {
                                  does (:1034); its velocities enter the step only
                                  through the repulsion force, zero here          */
   int maxc;                   /* near-pair candidate capacity per vesicle (0: 64) */
+  double judge_tol;           /* > 0: the plain BIEM step judges the surrogate and
+                                 stands in for it.  A vesicle whose surrogate step
+                                 (advection network + relaxation network) changes
+                                 its area or its length by more than judge_tol
+                                 (relative) takes instead the implicit BIEM step
+                                 of the isolated vesicle (tstep_biem.py:181-428
+                                 self block) with the step's explicit velocity
+                                 vinf + filtered far field; 0: the reference's
+                                 step (no judge)                                  */
 } ves_mlarm_params;
 typedef struct ves_mlarm_result {
   int n_near_pairs;           /* excluded (target point, source vesicle) pairs   */
   int auglag_iters;           /* augmented-Lagrangian updates of the correction  */
+  int n_fallback;             /* vesicles that took the BIEM step (judge_tol > 0) */
 } ves_mlarm_result;
 /* Optional device buffers receiving stage outputs of the step (NULL = skip):
  * the standardised shape and its values (:4119-4138), the two far fields

@@ -139,11 +139,12 @@ class MlarmParams(ctypes.Structure):
         ("farfield_precision", ctypes.c_int),
         ("eval_near_net", ctypes.c_int),
         ("maxc", ctypes.c_int),
+        ("judge_tol", ctypes.c_double),
     ]
 
 
 class MlarmResult(ctypes.Structure):
-    _fields_ = [("n_near_pairs", ctypes.c_int), ("auglag_iters", ctypes.c_int)]
+    _fields_ = [("n_near_pairs", ctypes.c_int), ("auglag_iters", ctypes.c_int), ("n_fallback", ctypes.c_int)]
 
 
 class MlarmTrace(ctypes.Structure):

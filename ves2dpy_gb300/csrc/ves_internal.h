@@ -204,6 +204,11 @@ int post_correct_area_length(ves_ctx* c, int nv, const double* X, const double* 
 // bending force of the MLARM step: bending of the Nup-upsampled shape truncated to N modes
 int launch_bend_up(ves_ctx* c, int nv, const double* X, double kappa, double* fB, cudaStream_t s);
 
+// dx = X+ - X of the implicit BIEM step of non-interacting vesicles (ves_targets.cu);
+// dx NULL sizes the workspace only
+int isolated_step_run(ves_ctx* c, int nv, const double* X, const double* vinf, double dt, double kappa, int slp,
+                      double* dx, WsCarver& ws, cudaStream_t s);
+
 // vector kernels (GMRES)
 void launch_dot_partials(long long n, const double* a, const double* b, double* partials,
                          cudaStream_t s);

@@ -514,6 +514,35 @@ __global__ void relax_post_kernel(int N, double dt, const double* __restrict__ X
   }
 }
 
+// judge: vesicles whose area or length moved by more than tol (relative) in
+// the surrogate step are listed for the BIEM fallback
+__global__ void judge_kernel(int nv, double tol, const double* __restrict__ a0, const double* __restrict__ l0,
+                             const double* __restrict__ a1, const double* __restrict__ l1, int* __restrict__ idx,
+                             int* __restrict__ count) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nv) return;
+  const double ea = fabs(a1[k] - a0[k]) / fabs(a0[k]), el = fabs(l1[k] - l0[k]) / fabs(l0[k]);
+  if (!(ea <= tol && el <= tol)) idx[atomicAdd(count, 1)] = k;  // NaN counts as a failure
+}
+
+__global__ void fb_gather_kernel(int cnt, int N, const int* __restrict__ idx, const double* __restrict__ X,
+                                 const double* __restrict__ v, double* __restrict__ Xg, double* __restrict__ vg) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)cnt * 2 * N) return;
+  const long long j = i / (2 * N);
+  const long long src = (long long)idx[j] * 2 * N + i % (2 * N);
+  Xg[i] = X[src];
+  vg[i] = v[src];
+}
+
+__global__ void fb_scatter_kernel(int cnt, int N, const int* __restrict__ idx, const double* __restrict__ Xg,
+                                  const double* __restrict__ dx, double* __restrict__ Xout) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)cnt * 2 * N) return;
+  const long long j = i / (2 * N);
+  Xout[(long long)idx[j] * 2 * N + i % (2 * N)] = Xg[i] + dx[i];
+}
+
 __global__ void count_excl_kernel(long long nwords, const uint32_t* __restrict__ mask, const int* __restrict__ cand_count,
                                   int maxc, int nwords_N, int* __restrict__ total) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -638,6 +667,15 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
   double* fup = ws.take<double>((size_t)nv * 2 * Nup);
   double* den = ws.take<double>((size_t)nv * 2 * Nup);
   int* selfidx = ws.take<int>((size_t)nv);
+  // judge and fallback (judge_tol > 0): areas and lengths before and after the
+  // surrogate step, the listed vesicles, and chunks of their isolated BIEM step
+  const bool judge = prm->judge_tol > 0.0;
+  const int kFb = std::max(1, std::min(nv, 512));
+  double* jgeo = judge ? ws.take<double>((size_t)4 * nv) : nullptr;
+  int* fb_idx = judge ? ws.take<int>((size_t)nv + 1) : nullptr;
+  double* fbX = judge ? ws.take<double>((size_t)kFb * 2 * N) : nullptr;
+  double* fbV = judge ? ws.take<double>((size_t)kFb * 2 * N) : nullptr;
+  double* fbD = judge ? ws.take<double>((size_t)kFb * 2 * N) : nullptr;
   ves_near_lists nl;
   memset(&nl, 0, sizeof(nl));
   nl.maxc = maxc;
@@ -676,6 +714,11 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
     WsCarver w5(nullptr, 0);
     post_redistribute(c, nv, nullptr, nullptr, nullptr, w5, s);
     scratch = std::max(scratch, w5.off);
+    if (judge) {
+      WsCarver w6(nullptr, 0);
+      isolated_step_run(c, kFb, nullptr, nullptr, prm->dt, prm->kappa, VES_PREC_FP32C, nullptr, w6, s);
+      scratch = std::max(scratch, w6.off);
+    }
   }
   char* scr = ws.take<char>(scratch + 1024);
   const size_t scr_bytes = scratch + 1024;
@@ -812,6 +855,34 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
   }
   ves_count_launch();
   relax_post_kernel<Real><<<nv, 128, 0, s>>>(N, prm->dt, Xs2, nout, m->relax_out, scal2, rot2, rotc2, trn2, sidx2, Xa);
+  // the plain BIEM step as judge and fallback of the surrogate: vesicles whose
+  // area or length the surrogate moved by more than judge_tol take the implicit
+  // step of the isolated vesicle with the same explicit velocity vsum
+  int nfb = 0;
+  if (judge) {
+    launch_geom_prop(c, nv, X, nullptr, jgeo, jgeo + nv, s);
+    launch_geom_prop(c, nv, Xa, nullptr, jgeo + 2 * nv, jgeo + 3 * nv, s);
+    rc = ves_cuda_status(cudaMemsetAsync(fb_idx + nv, 0, sizeof(int), s), "judge count");
+    if (rc) return rc;
+    ves_count_launch();
+    judge_kernel<<<ceil_div(nv, 256), 256, 0, s>>>(nv, prm->judge_tol, jgeo, jgeo + nv, jgeo + 2 * nv, jgeo + 3 * nv,
+                                                   fb_idx, fb_idx + nv);
+    rc = ves_cuda_status(cudaMemcpyAsync(c->h_ints + 1, fb_idx + nv, sizeof(int), cudaMemcpyDeviceToHost, s),
+                         "judge count read");
+    if (!rc) rc = ves_cuda_status(cudaStreamSynchronize(s), "judge sync");
+    if (rc) return rc;
+    nfb = c->h_ints[1];
+    for (int a = 0; a < nfb; a += kFb) {
+      const int cnt = std::min(kFb, nfb - a);
+      const long long ne = (long long)cnt * 2 * N;
+      ves_count_launch();
+      fb_gather_kernel<<<ceil_div(ne, 256), 256, 0, s>>>(cnt, N, fb_idx + a, X, vsum, fbX, fbV);
+      WsCarver w = sub();
+      if ((rc = isolated_step_run(c, cnt, fbX, fbV, prm->dt, prm->kappa, VES_PREC_FP32C, fbD, w, s))) return rc;
+      ves_count_launch();
+      fb_scatter_kernel<<<ceil_div(ne, 256), 256, 0, s>>>(cnt, N, fb_idx + a, fbX, fbD, Xa);
+    }
+  }
   if (tr && tr->Xrelax) cudaMemcpyAsync(tr->Xrelax, Xa, n2 * sizeof(double), cudaMemcpyDeviceToDevice, s);
   // up to five redistribution passes (stopping once nothing moves is the
   // same as running all five), alignment, area/length correction, filter (:1165-1198)
@@ -857,6 +928,7 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
   if (res) {
     res->n_near_pairs = npairs;
     res->auglag_iters = iters;
+    res->n_fallback = nfb;
   }
   return rc;
 }

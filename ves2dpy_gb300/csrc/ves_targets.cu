@@ -204,11 +204,13 @@ int targets_run(ves_ctx* c, int nv, const double* Xs, const double* vinf, double
   double* v3 = ws.take<double>((size_t)nv * 3 * N);
   double* x3 = ws.take<double>((size_t)nv * 3 * N);
   double* GT = ws.take<double>((size_t)nv * 2 * NN);
-  double* A = ws.take<double>((size_t)nv * NN);
-  double* Ai = ws.take<double>((size_t)nv * NN);
-  double* Bm = ws.take<double>((size_t)2 * N * nc);
-  double* DB = ws.take<double>((size_t)nv * N * nc);
-  double* Z = ws.take<double>((size_t)nv * N * nc);
+  const bool tens = selften || advten || adv;  // the tension operator A = Div G Ten is needed
+  const bool modes = advten || adv;
+  double* A = tens ? ws.take<double>((size_t)nv * NN) : nullptr;
+  double* Ai = tens ? ws.take<double>((size_t)nv * NN) : nullptr;
+  double* Bm = modes ? ws.take<double>((size_t)2 * N * nc) : nullptr;
+  double* DB = modes ? ws.take<double>((size_t)nv * N * nc) : nullptr;
+  double* Z = modes ? ws.take<double>((size_t)nv * N * nc) : nullptr;
   double* W = adv ? ws.take<double>((size_t)nv * 2 * N * nc) : nullptr;
   // scratch of the Alpert build and the derivative matrices
   size_t scr = 0;
@@ -302,6 +304,14 @@ int targets_run(ves_ctx* c, int nv, const double* Xs, const double* vinf, double
 }
 
 }  // namespace
+
+// dx = X+ - X of the implicit step of non-interacting vesicles with background
+// velocity vinf (NULL: none), for callers inside the library (the MLARM
+// step's fallback); no status reset, no synchronisation
+int isolated_step_run(ves_ctx* c, int nv, const double* X, const double* vinf, double dt, double kappa, int slp,
+                      double* dx, WsCarver& ws, cudaStream_t s) {
+  return targets_run(c, nv, X, vinf, dt, kappa, slp, dx ? dx : (double*)1, nullptr, nullptr, nullptr, ws, s);
+}
 
 extern "C" size_t ves_mlarm_targets_workspace(ves_ctx* c, int nv, int sl_precision) {
   if (!c || nv < 0) return 0;

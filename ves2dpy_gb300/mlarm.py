@@ -104,7 +104,12 @@ class MLARM_manyfree_py:
     ("fp32c" or "fp64"), ``eval_near_net`` (evaluate the near-field
     network as the reference does; its output enters the step only through
     the repulsion force) and ``autotune`` (launch shapes of the BF16 network
-    kernels timed on the first step at each vesicle count).
+    kernels timed on the first step at each vesicle count), ``judge_tol``
+    (> 0: the plain BIEM step judges every vesicle's surrogate step and
+    replaces it where it moved the vesicle's area or length by more than
+    ``judge_tol``, relative: the implicit step of the isolated vesicle with
+    the step's explicit velocity; ``last_result.n_fallback`` counts them; 0,
+    the default, is the reference's step).
     """
 
     def __init__(self, dt, vinf, oc, use_repulsion, repStrength, rbf_upsample: int,
@@ -112,7 +117,8 @@ class MLARM_manyfree_py:
                  nearNetInputNorm, nearNetOutputNorm, tenSelfNetInputNorm, tenSelfNetOutputNorm,
                  tenAdvNetInputNorm, tenAdvNetOutputNorm, device, logger=None, *, state_dicts=None,
                  model_dir: str = "../trained/torch_script_models", net_precision: str = "fp32",
-                 farfield_precision: str = "fp32c", eval_near_net: bool = True, autotune: bool = True):
+                 farfield_precision: str = "fp32c", eval_near_net: bool = True, autotune: bool = True,
+                 judge_tol: float = 0.0):
         if use_repulsion:
             raise NotImplementedError("MLARM_manyfree_py: repulsion is not supported")
         self.dt = float(dt)
@@ -128,6 +134,7 @@ class MLARM_manyfree_py:
         self.rbf_upsample = rbf_upsample
         self.farfield_precision = farfield_precision
         self.eval_near_net = bool(eval_near_net)
+        self.judge_tol = float(judge_tol)
         self.area0 = None
         self.len0 = None
         self._norms = {
@@ -166,7 +173,8 @@ class MLARM_manyfree_py:
 
     def _params(self):
         return nat.MlarmParams(self.dt, self.kappa, nat.FLOW["shear"], 0.0, 0.0, 0.0,
-                               nat.PREC[self.farfield_precision], 1 if self.eval_near_net else 0, self._maxc)
+                               nat.PREC[self.farfield_precision], 1 if self.eval_near_net else 0, self._maxc,
+                               self.judge_tol)
 
     def _step(self, Xold, tenOld, trace=None):
         X = as_device_f64(Xold, self.device)

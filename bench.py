@@ -43,8 +43,8 @@ MIN_GAP = 0.05 / 7.79              # the 0.05 gap of radius-1 vesicles (length 7
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--nv", type=int, default=4096)
     ap.add_argument("--N", type=int, default=128)
@@ -67,6 +67,9 @@ def parse():
                     "(relax, adv, near, selften, advten)")
     ap.add_argument("--synthetic-weights", action="store_true",
                     help="seeded synthetic networks instead of the trained ones in ves2dpy_gb300/trained")
+    ap.add_argument("--judge-tol", type=float, default=0.0,
+                    help="> 0: the BIEM step judges each vesicle's surrogate step and stands in where it moved the "
+                         "area or length by more than this (relative)")
     ap.add_argument("--biem-precond", default="fp32", choices=["fp32", "fp64"],
                     help="precision of the BIEM step's block-diagonal preconditioner (GMRES solves the FP64 system)")
     return ap.parse_args()
@@ -261,7 +264,8 @@ def run_mlarm(a, dev, X0, state_dicts, norms=None):
     m = MLARM_manyfree_py(STEP["dt"], vinf, Curve(), False, 1e2, -1, nrm["adv_in"], nrm["adv_out"],
                           nrm["relax_in"], nrm["relax_out"], nrm["near_in"], nrm["near_out"], nrm["selften_in"],
                           nrm["selften_out"], nrm["advten_in"], nrm["advten_out"], dev, state_dicts=state_dicts,
-                          net_precision=a.nets, farfield_precision=a.precision, autotune=not a.no_autotune)
+                          net_precision=a.nets, farfield_precision=a.precision, autotune=not a.no_autotune,
+                          judge_tol=a.judge_tol)
     Xd = torch.tensor(X0, dtype=torch.float64, device=dev)
     _, area0, len0 = Curve().geomProp(Xd)
     m.area0, m.len0 = area0, len0
@@ -281,10 +285,12 @@ def run_mlarm(a, dev, X0, state_dicts, norms=None):
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream(dev)
     e0, e1 = _events()
+    nfb = 0
     with Clocks(dev.index) as clk:
         e0.record(stream)
         for _ in range(a.steps):
             X, t = m.time_step_many_noinfo(X, t, 3)
+            nfb += m.last_result.n_fallback
         e1.record(stream)
         torch.cuda.synchronize()
     barrier()
@@ -334,7 +340,7 @@ def run_mlarm(a, dev, X0, state_dicts, norms=None):
     Xs1, _ = m.time_step_many_noinfo(Xw.to(dev), tw.to(dev), 3)
     return dict(ms=ms, stats=st, launches=launches, clocks=clk.summary(), net_ms=net_ms, e2e_s=e2e_s, io=io,
                 e2e_steps=e2e_steps, drift=drift, near_pairs=near_pairs, Xw=Xw.numpy().copy(), tw=tw,
-                X1=Xs1.cpu(), nets=m.nets)
+                X1=Xs1.cpu(), nets=m.nets, fallbacks=nfb)
 
 
 def run_biem(a, dev, X0):
@@ -506,11 +512,12 @@ def run_gb300(a, rank, world):
                   "per step)",
             "parallelism": "replicas only" if world > 1 else "single GPU",
             "mlarm": {"ms_per_step": ms_per_step, "near_pairs_excluded": r["near_pairs"],
+                      "judge_tol": a.judge_tol, "biem_fallbacks_per_step": r["fallbacks"] / max(a.steps, 1),
                       "area_length_drift": r["drift"],
                       "drift_note": "max over vesicles of the relative area and length change after the warm-up "
-                                    "and timed steps; the correction (correctAreaAndLengthAugLag) aims at the "
-                                    "reference's areaLenTol 1e-2 within its capped iterations, and the untrained "
-                                    "synthetic networks move some shapes further than it recovers",
+                                    "and timed steps against the initial shapes; the step's correction "
+                                    "(correctAreaAndLengthAugLag) acts only beyond 1e-2 (its tolerance), so the "
+                                    "drift below that is the networks' own",
                       "network_ms": r["net_ms"],
                       "network_tflops": net_tflops,
                       "farfield_ms_per_eval": ff_ms, "farfield_evals_per_step": st.farfield_launches / a.steps},

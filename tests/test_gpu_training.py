@@ -143,7 +143,7 @@ def test_training_lowers_the_loss():
     from ves2dpy_gb300 import training as T
     Xs = T.standardize(torch.tensor(_shapes(512, 13), dtype=torch.float64, device=DEV))
     data = T.Dataset(Xs, chunk=512)
-    idx = torch.arange(Xs.shape[0], device=DEV)
+    idx = torch.arange(data.n, device=DEV)   # the shapes the dataset kept
     tr, info = T.train_network("relax", data, idx, seconds=15.0, batch=128)
     first = T.evaluate("relax", T.Trainer(T.group_spec("relax"), T.init_state_dict(T.group_spec("relax"), 0),
                                           "fp32", 256, DEV), data, idx[:256])

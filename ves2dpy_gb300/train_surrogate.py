@@ -41,11 +41,13 @@ def main(argv=None):
     Xs = T.shape_dataset(a.shapes, a.seed, dev)
     log(f"{Xs.shape[0]} standardised shapes")
     data = T.Dataset(Xs)
-    log("BIEM targets done")
-    perm = torch.randperm(Xs.shape[0], device=dev, generator=torch.Generator(dev).manual_seed(a.seed))
-    nval = max(256, Xs.shape[0] // 20)
+    log(f"BIEM targets done; {data.n} shapes kept, {data.dropped} dropped as outliers")
+    # indices into the kept shapes (the dataset drops outliers)
+    perm = torch.randperm(data.n, device=dev, generator=torch.Generator(dev).manual_seed(a.seed))
+    nval = max(256, data.n // 20)
     val, train = perm[:nval], perm[nval:]
-    nets, meta = {}, {"shapes": Xs.shape[0], "validation_shapes": nval, "modes": list(T.TRAIN_MODES), "nets": {}}
+    nets, meta = {}, {"shapes": data.n, "dropped": data.dropped, "validation_shapes": nval,
+                      "modes": list(T.TRAIN_MODES), "nets": {}}
     for name, sec in budget.items():
         tr, info = T.train_network(name, data, train, sec, batch=a.batch, lr=a.lr, seed=a.seed, log=log)
         err = T.evaluate(name, tr, data, val)

@@ -443,6 +443,8 @@ def train_network(name: str, data: Dataset, train_idx: torch.Tensor, seconds: fl
     """Train the one-group network ``name`` for about ``seconds`` of wall
     clock (cosine schedule over the steps the first ones' rate allows)."""
     spec = group_spec(name)
+    if train_idx.numel() == 0 or int(train_idx.min()) < 0 or int(train_idx.max()) >= data.n:
+        raise IndexError(f"train_network: sample indices outside the {data.n} shapes of the dataset")
     tr = Trainer(spec, init_state_dict(spec, seed), "fp32", batch, data.device)
     gen = torch.Generator(data.device).manual_seed(seed + 1)
     nmodes = len(data.modes)
@@ -484,6 +486,8 @@ def train_network(name: str, data: Dataset, train_idx: torch.Tensor, seconds: fl
 def evaluate(name: str, tr: Trainer, data: Dataset, idx: torch.Tensor, batch: int = 256):
     """Relative error (2-norm over the samples) of the de-normalised network
     outputs against the BIEM targets on samples ``idx`` (all kept modes)."""
+    if idx.numel() == 0 or int(idx.min()) < 0 or int(idx.max()) >= data.n:
+        raise IndexError(f"evaluate: sample indices outside the {data.n} shapes of the dataset")
     num = den = 0.0
     batch = min(batch, tr.max_batch)
     for a in range(0, idx.numel(), batch):

@@ -435,7 +435,9 @@ def run_gb300(a, rank, world):
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
-    bf16_peak = peaks.get("bf16_tflops", 1900.0)
+    # the network kernels are timed inside a step of about a second: the
+    # sustained BF16 figure is their denominator
+    bf16_peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops", 1700.0))
     flops = {n: net_flops(NETS[n]) * a.nv for n in NETS}
     net_total_ms = sum(r["net_ms"].values())
     net_tflops = sum(flops.values()) / (net_total_ms * 1e-3) / 1e12 if net_total_ms > 0 else None
@@ -451,7 +453,8 @@ def run_gb300(a, rank, world):
                                 "written and read once; no re-reads), at most 20% of the DRAM peak",
                 "flops_per_step": st.networks_flops / a.steps, "ms_per_step": st.networks_ms / a.steps,
                 "passes_per_step": st.networks_launches / a.steps,
-                "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured",
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (cuBLAS BF16 GEMM looped for seconds "
+                               "under the power cap), of measured",
                 "share_of_step": st.networks_ms / r["ms"] if r["ms"] else None}
     # all-pairs sums
     sm_mhz = (r["clocks"] or {}).get("sm_max_mhz") or 2070.0

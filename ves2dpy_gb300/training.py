@@ -39,7 +39,7 @@ import numpy as np
 import torch
 
 from . import _native as nat
-from .mlarm_weights import NETS, BlockSpec, NetSpec, param_shapes
+from .mlarm_weights import NETS, NetSpec, param_shapes
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 TRAINED_DIR = os.path.join(PKG, "trained")

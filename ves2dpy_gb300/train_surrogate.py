@@ -3,7 +3,7 @@ directory that ``training.load`` (and ``MLARM_manyfree_py.from_trained``)
 reads.
 
     python -m ves2dpy_gb300.train_surrogate --out DIR [--shapes 60000]
-           [--seconds relax=480,selften=300,adv=600,advten=600] [--seed 0]
+           [--seconds relax=900,selften=600,adv=420,advten=300] [--seed 0]
 
 Every stage runs on the current CUDA device: shape generation and evolution
 (``ves_isolated_step``), standardisation, the BIEM targets
@@ -26,9 +26,9 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
     ap.add_argument("--shapes", type=int, default=60000)
-    ap.add_argument("--seconds", default="relax=480,selften=300,adv=600,advten=600")
+    ap.add_argument("--seconds", default="relax=900,selften=600,adv=420,advten=300")
     ap.add_argument("--batch", type=int, default=256)
-    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--lr", type=float, default=5e-4)
     ap.add_argument("--seed", type=int, default=0)
     a = ap.parse_args(argv)
     dev = torch.device("cuda", torch.cuda.current_device())

@@ -338,9 +338,14 @@ def run_mlarm(a, dev, X0, state_dicts, norms=None):
     # one step from the timed steps' starting state: the surrogate velocity
     # the accuracy check compares with the BIEM step's from the same state
     Xs1, _ = m.time_step_many_noinfo(Xw.to(dev), tw.to(dev), 3)
+    # the BIEM operators as the judge of each network on that state (512 vesicles)
+    from ves2dpy_gb300 import training as TR
+    from ves2dpy_gb300.layout import to_vm
+    sub = to_vm(Xw.to(dev))[: min(nv, 512)].contiguous()
+    judge = TR.surrogate_errors(m.nets, norms or synthetic_norms(0), TR.standardize(sub))
     return dict(ms=ms, stats=st, launches=launches, clocks=clk.summary(), net_ms=net_ms, e2e_s=e2e_s, io=io,
                 e2e_steps=e2e_steps, drift=drift, near_pairs=near_pairs, Xw=Xw.numpy().copy(), tw=tw,
-                X1=Xs1.cpu(), nets=m.nets, fallbacks=nfb)
+                X1=Xs1.cpu(), nets=m.nets, fallbacks=nfb, judge=judge)
 
 
 def run_biem(a, dev, X0):
@@ -516,6 +521,10 @@ def run_gb300(a, rank, world):
             "parallelism": "replicas only" if world > 1 else "single GPU",
             "mlarm": {"ms_per_step": ms_per_step, "near_pairs_excluded": r["near_pairs"],
                       "judge_tol": a.judge_tol, "biem_fallbacks_per_step": r["fallbacks"] / max(a.steps, 1),
+                      "network_errors_vs_biem_operators": r["judge"],
+                      "network_errors_note": "relative 2-norm error of each network (as the step runs it) against "
+                                             "the BIEM operator it stands for, on 512 vesicles of the timed steps' "
+                                             "starting state (ves_mlarm_targets; merged networks on |k| <= 16)",
                       "area_length_drift": r["drift"],
                       "drift_note": "max over vesicles of the relative area and length change after the warm-up "
                                     "and timed steps against the initial shapes; the step's correction "

@@ -163,34 +163,41 @@ def test_mlarm_step_bf16_networks(golden, farfield):
     assert rel(t["ten"], g["ten1"]) < 5e-2, rel(t["ten"], g["ten1"])
 
 
-def test_biem_fallback_matches_the_biem_step():
-    """judge_tol: with a tolerance nothing meets, every vesicle takes the
-    implicit BIEM step of the isolated vesicle with the step's explicit
-    velocity, and the vesicle velocities (physical centres) agree with the
-    plain BIEM step's from the same state; with a tolerance everything meets,
-    the step is the surrogate's, bit for bit."""
-    import math
+def test_biem_fallback_is_the_biem_step_of_the_vesicle():
+    """judge_tol: with a tolerance nothing meets, a vesicle takes the implicit
+    BIEM step of the isolated vesicle with the step's explicit velocity.  A
+    single vesicle has no far field, so that velocity is the background flow
+    and the vesicle moves as the plain BIEM step moves it (physical centre,
+    1e-5 of its velocity), whatever the networks predict; with a tolerance
+    everything meets, the step is the surrogate's, bit for bit."""
     from ves2dpy_gb300.curve import Curve
-    from ves2dpy_gb300.suspension import random_suspension
+    from ves2dpy_gb300.training import random_shapes
     from ves2dpy_gb300.tstep_biem import TStepBiem
-    X0 = random_suspension(24, 128, 0.05, min_gap=0.1, area=0.65 / (4 * math.pi), seed=5)
-    nv = X0.shape[1]
-    X = torch.from_numpy(X0).to(DEV)
-    ten = torch.zeros(128, nv, dtype=torch.float64, device=DEV)
+    x = random_shapes(1, 21, reduced_area=(0.65, 0.65), amp=(0.02, 0.02))[0]
+    # modes above 16 removed, as the step's last filter does, and moved off the
+    # shear flow's zero line
+    z = np.fft.fft(x[:128] + 1j * x[128:])
+    k = np.fft.fftfreq(128, 1.0 / 128)
+    z[np.abs(k) > 16] = 0.0
+    w = np.fft.ifft(z)
+    X = torch.from_numpy(np.concatenate([w.real, w.imag + 3.0])[:, None].copy()).to(DEV)
+    ten = torch.zeros(128, 1, dtype=torch.float64, device=DEV)
     m = _mlarm("bf16", "fp32m")
     _, a0, l0 = Curve().geomProp(X)
     m.area0, m.len0 = a0, l0
-    m.judge_tol = 0.0
-    Xs, _ = m.time_step_many_noinfo(X, ten, 3)
-    m.judge_tol = 1e10
-    Xj, _ = m.time_step_many_noinfo(X, ten, 3)
-    assert m.last_result.n_fallback == 0
-    assert torch.equal(Xs, Xj)
-    m.judge_tol = 1e-300
-    Xf, _ = m.time_step_many_noinfo(X, ten, 3)
-    m.judge_tol = 0.0
-    assert m.last_result.n_fallback == nv
-    prams = dict(dt=1e-5, kappa=1.0, gmresTol=1e-10, gmresMaxIter=100, farFieldSpeed=2.0, viscCont=[1.0] * nv)
+    try:
+        m.judge_tol = 0.0
+        Xs, _ = m.time_step_many_noinfo(X, ten, 3)
+        m.judge_tol = 1e10
+        Xj, _ = m.time_step_many_noinfo(X, ten, 3)
+        assert m.last_result.n_fallback == 0
+        assert torch.equal(Xs, Xj)
+        m.judge_tol = 1e-300
+        Xf, _ = m.time_step_many_noinfo(X, ten, 3)
+        assert m.last_result.n_fallback == 1
+    finally:
+        m.judge_tol = 0.0
+    prams = dict(dt=1e-5, kappa=1.0, gmresTol=1e-12, gmresMaxIter=100, farFieldSpeed=2.0, viscCont=[1.0])
     tt = TStepBiem(X, None, dict(farField="shear", usePreco=True), prams, near="py_hh", farfield_precision="fp32m",
                    sl_precision="fp32c")
     Xb, *_ = tt.time_step(X, ten)
@@ -199,4 +206,4 @@ def test_biem_fallback_matches_the_biem_step():
     vb = (cv.getPhysicalCenter(Xb).double() - c0) / 1e-5
     vf = (cv.getPhysicalCenter(Xf).double() - c0) / 1e-5
     err = float(torch.linalg.norm(vf - vb) / torch.linalg.norm(vb))
-    assert err < 1e-3, err
+    assert err < 1e-5, err

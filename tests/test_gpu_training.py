@@ -150,3 +150,22 @@ def test_training_lowers_the_loss():
     last = T.evaluate("relax", tr, data, idx[:256])
     assert info["steps"] >= 40
     assert last < 0.5 * first, (first, last, info["losses"])
+
+
+def test_surrogate_errors_of_the_trained_networks():
+    """The BIEM operators judging the trained networks as the step runs them
+    (merged, BF16 tensor cores, the step's normalisation): each relative
+    error is finite and below 1 on the benchmark generator's shapes."""
+    import math
+    from ves2dpy_gb300 import training as T
+    from ves2dpy_gb300.mlarm import Network
+    from ves2dpy_gb300.suspension import random_suspension
+    if not T.have_trained():
+        pytest.skip("no trained networks in the package")
+    sds, norms = T.load()
+    nets = {n: Network(n, sds[n], "bf16", DEV) for n in ("relax", "selften", "adv", "advten")}
+    X = random_suspension(64, 128, 0.15, min_gap=0.05 / 7.79, area=0.65 / (4 * math.pi), seed=3)
+    Xs = T.standardize(torch.tensor(X.T.copy(), dtype=torch.float64, device=DEV))
+    err = T.surrogate_errors(nets, norms, Xs)
+    for name, e in err.items():
+        assert np.isfinite(e) and e < 1.0, (name, e)

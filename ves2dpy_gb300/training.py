@@ -559,3 +559,59 @@ def load(model_dir: str = TRAINED_DIR):
 
 def have_trained(model_dir: str = TRAINED_DIR) -> bool:
     return os.path.exists(os.path.join(model_dir, "norms.npz"))
+
+
+def surrogate_errors(nets: dict, norms: dict, Xs: torch.Tensor, modes=TRAIN_MODES, dt: float = 1e-5):
+    """The plain BIEM operators as the judge of the surrogate: relative errors
+    (2-norm over the vesicles and points) of the merged networks ``nets``
+    (mlarm.Network objects, as the step runs them) against ves_mlarm_targets
+    on standardised shapes Xs[nv][2N] (device).  The networks' inputs and
+    outputs are normalised and de-normalised as the step does
+    (get_network_torch.py pre/post-processing); the merged networks are
+    compared on the Fourier modes ``modes``."""
+    dev = Xs.device
+    nv = Xs.shape[0]
+    t = targets(Xs, dt)
+    x, y = Xs[:, :N], Xs[:, N:]
+
+    def q(name):
+        return torch.as_tensor(np.asarray(norms[name], dtype=np.float64), device=dev)
+
+    def rel(a, b):
+        return float(torch.linalg.norm((a - b).reshape(-1)) / torch.linalg.norm(b.reshape(-1)))
+
+    out = {}
+    p, o = q("relax_in"), q("relax_out")
+    inp = torch.stack([(x - p[0]) / p[1], (y - p[2]) / p[3]], 1)
+    r = nets["relax"](inp).double()
+    dx = torch.cat([r[:, 0] * o[1] + o[0], r[:, 1] * o[3] + o[2]], 1) * (dt / 1e-5)
+    out["relax"] = rel(dx, t["relax"])
+    p, o = q("selften_in"), q("selften_out")
+    inp = torch.stack([(x - p[0]) / p[1], (y - p[2]) / p[3]], 1)
+    out["selften"] = rel(nets["selften"](inp).double()[:, 0] * o[1] + o[0], t["selften"])
+    km = torch.tensor(modes, dtype=torch.long, device=dev)
+    # advection-tension: channel 2k + c is coordinate c normalised with mode k's statistics
+    p, o = q("advten_in"), q("advten_out")
+    inp = torch.stack([(x[:, None, :] - p[None, :, 0, None]) / p[None, :, 1, None],
+                       (y[:, None, :] - p[None, :, 2, None]) / p[None, :, 3, None]], 2).reshape(nv, 2 * MODES, N)
+    z = nets["advten"](inp).double().reshape(nv, MODES, 2, N)
+    z = torch.stack([z[:, :, 0] * o[None, :, 1, None] + o[None, :, 0, None],
+                     z[:, :, 1] * o[None, :, 3, None] + o[None, :, 2, None]], 2)
+    out["advten"] = rel(z[:, km], t["advten"].reshape(nv, MODES, 2, N)[:, km])
+    # advection: channel 2k = [x ++ y] normalised (mode 63: unit std), 2k + 1 = the mode's basis
+    p, o = q("adv_in"), q("adv_out")
+    sx = p[:, 1].clone()
+    sy = p[:, 3].clone()
+    sx[NYQUIST] = 1.0
+    sy[NYQUIST] = 1.0
+    coords = torch.cat([(x[:, None, :] - p[None, :, 0, None]) / sx[None, :, None],
+                        (y[:, None, :] - p[None, :, 2, None]) / sy[None, :, None]], 2)
+    th = torch.arange(N, dtype=torch.float64, device=dev) * (2 * math.pi / N)
+    kk = torch.arange(1, MODES + 1, dtype=torch.float64, device=dev)[:, None]
+    basis = torch.cat([torch.cos(kk * th), torch.sin(kk * th)], 1) / N
+    inp = torch.stack([coords, basis[None].expand(nv, -1, -1)], 2).reshape(nv, 2 * MODES, 2 * N)
+    w = nets["adv"](inp).double().reshape(nv, MODES, 2, 2 * N)
+    w = torch.stack([w[:, :, 0] * o[None, :, 1, None] + o[None, :, 0, None],
+                     w[:, :, 1] * o[None, :, 3, None] + o[None, :, 2, None]], 2)
+    out["adv"] = rel(w[:, km], t["adv"].reshape(nv, MODES, 2, 2 * N)[:, km])
+    return out

@@ -424,6 +424,12 @@ typedef struct ves_mlarm_params {
                                  self block) with the step's explicit velocity
                                  vinf + filtered far field; 0: the reference's
                                  step (no judge)                                  */
+  int conserve;               /* 1: the advection displacement and the relaxation
+                                 network's displacement are made area- and
+                                 length-preserving to first order (their
+                                 components along n and kappa n removed), as the
+                                 exact incompressible, inextensible dynamics is;
+                                 0: the reference's step                           */
 } ves_mlarm_params;
 typedef struct ves_mlarm_result {
   int n_near_pairs;           /* excluded (target point, source vesicle) pairs   */

@@ -207,3 +207,31 @@ def test_biem_fallback_is_the_biem_step_of_the_vesicle():
     vf = (cv.getPhysicalCenter(Xf).double() - c0) / 1e-5
     err = float(torch.linalg.norm(vf - vb) / torch.linalg.norm(vb))
     assert err < 1e-5, err
+
+
+def test_conserve_keeps_area_and_length():
+    """conserve: the advection and relaxation displacements lose their
+    first-order area and length changes; with the seeded (untrained)
+    networks, whose displacements change both, one step's change of area and
+    length falls by more than ten times and below 1e-3."""
+    import math
+    from ves2dpy_gb300.curve import Curve
+    from ves2dpy_gb300.suspension import random_suspension
+    X0 = random_suspension(16, 128, 0.05, min_gap=0.1, area=0.65 / (4 * math.pi), seed=6)
+    X = torch.from_numpy(X0).to(DEV)
+    ten = torch.zeros(128, 16, dtype=torch.float64, device=DEV)
+    m = _mlarm("bf16", "fp32m")
+    cv = Curve()
+    _, a0, l0 = cv.geomProp(X)
+    m.area0, m.len0 = a0, l0
+    change = {}
+    try:
+        for flag in (False, True):
+            m.conserve = flag
+            Xn, _ = m.time_step_many_noinfo(X, ten, 3)
+            _, a, l = cv.geomProp(Xn)
+            change[flag] = max(float(((a - a0) / a0).abs().max()), float(((l - l0) / l0).abs().max()))
+    finally:
+        m.conserve = False
+    assert change[True] < 0.1 * change[False], change
+    assert change[True] < 1e-3, change

@@ -140,6 +140,7 @@ class MlarmParams(ctypes.Structure):
         ("eval_near_net", ctypes.c_int),
         ("maxc", ctypes.c_int),
         ("judge_tol", ctypes.c_double),
+        ("conserve", ctypes.c_int),
     ]
 
 

@@ -484,23 +484,117 @@ __global__ void translate_kernel(int N, double dt, const double* __restrict__ Xo
   }
 }
 
-// RelaxNetwork.forward post-processing (:59-80) and destandardize (:4154-4177)
+// First-order conservation of a displacement (dx, dy) of the curve (x, y)
+// (shared memory, N points, blockDim a power of two): removes the components
+// along n and kappa n that change the enclosed area (d A = int n . d X ds) and
+// the length (d L = int kappa n . d X ds), so that a surrogate's displacement
+// keeps both to first order, as the exact (incompressible, inextensible)
+// dynamics does.  tmp: 3N doubles, red: blockDim doubles.
+__device__ void conserve_area_length(int N, const double* __restrict__ d1, const double* x, const double* y,
+                                     double* dx, double* dy, double* tmp, double* red) {
+  double* xp = tmp;
+  double* yp = tmp + N;
+  double* kap = tmp + 2 * N;
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    xp[j] = circ(d1, x, N, j);
+    yp[j] = circ(d1, y, N, j);
+  }
+  __syncthreads();
+  double m11 = 0, m12 = 0, m22 = 0, r1 = 0, r2 = 0;
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    const double xpp = circ(d1, xp, N, j), ypp = circ(d1, yp, N, j);
+    const double jac = sqrt(xp[j] * xp[j] + yp[j] * yp[j]);
+    const double kp = (xp[j] * ypp - yp[j] * xpp) / (jac * jac * jac);
+    const double nx = yp[j] / jac, ny = -xp[j] / jac;
+    const double dn = nx * dx[j] + ny * dy[j];
+    kap[j] = kp;
+    m11 += jac;
+    m12 += kp * jac;
+    m22 += kp * kp * jac;
+    r1 += dn * jac;
+    r2 += kp * dn * jac;
+  }
+  m11 = bsum(m11, red);
+  m12 = bsum(m12, red);
+  m22 = bsum(m22, red);
+  r1 = bsum(r1, red);
+  r2 = bsum(r2, red);
+  const double det = m11 * m22 - m12 * m12;
+  double a, b;
+  if (det > 1e-12 * m11 * m22) {  // area and length variations independent (not a circle)
+    a = (m22 * r1 - m12 * r2) / det;
+    b = (m11 * r2 - m12 * r1) / det;
+  } else {
+    a = r1 / m11;
+    b = 0.0;
+  }
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    const double jac = sqrt(xp[j] * xp[j] + yp[j] * yp[j]);
+    const double nx = yp[j] / jac, ny = -xp[j] / jac;
+    const double c = a + b * kap[j];
+    dx[j] -= c * nx;
+    dy[j] -= c * ny;
+  }
+  __syncthreads();
+}
+
+// advection displacement Xa - X made first-order area- and length-preserving (in place)
+__global__ void conserve_kernel(int N, const double* __restrict__ d1, const double* __restrict__ X,
+                                double* __restrict__ Xa) {
+  __shared__ double x[kN], y[kN], dx[kN], dy[kN], tmp[3 * kN], red[128];
+  const int k = blockIdx.x;
+  const long long o = (long long)k * 2 * N;
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    x[j] = X[o + j];
+    y[j] = X[o + N + j];
+    dx[j] = Xa[o + j] - x[j];
+    dy[j] = Xa[o + N + j] - y[j];
+  }
+  __syncthreads();
+  conserve_area_length(N, d1, x, y, dx, dy, tmp, red);
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    Xa[o + j] = x[j] + dx[j];
+    Xa[o + N + j] = y[j] + dy[j];
+  }
+}
+
+// RelaxNetwork.forward post-processing (:59-80) and destandardize (:4154-4177);
+// d1 non-null: the displacement is first made area- and length-preserving to
+// first order in the standardised frame (destandardize is a similarity)
 template <typename Real>
 __global__ void relax_post_kernel(int N, double dt, const double* __restrict__ Xin, const Real* __restrict__ pred,
                                   const double* __restrict__ q, const double* __restrict__ scaling,
                                   const double* __restrict__ rotate, const double* __restrict__ rot_center,
                                   const double* __restrict__ trans, const int* __restrict__ sort_idx,
-                                  double* __restrict__ Xout) {
+                                  double* __restrict__ Xout, const double* __restrict__ d1) {
   __shared__ double ux[kN], uy[kN];
   const int k = blockIdx.x;
   const double sc = scaling[k];
-  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+  if (d1) {
+    __shared__ double x[kN], y[kN], dx[kN], dy[kN], tmp[3 * kN], red[128];
     const long long o = (long long)k * 2 * N;
-    const double dxs = ((double)pred[o + j] * q[1] + q[0]) / 1e-5 * dt;
-    const double dys = ((double)pred[o + N + j] * q[3] + q[2]) / 1e-5 * dt;
-    const int dst = sort_idx[(long long)k * N + j];
-    ux[dst] = (Xin[o + j] + dxs) / sc;
-    uy[dst] = (Xin[o + N + j] + dys) / sc;
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+      x[j] = Xin[o + j];
+      y[j] = Xin[o + N + j];
+      dx[j] = ((double)pred[o + j] * q[1] + q[0]) / 1e-5 * dt;
+      dy[j] = ((double)pred[o + N + j] * q[3] + q[2]) / 1e-5 * dt;
+    }
+    __syncthreads();
+    conserve_area_length(N, d1, x, y, dx, dy, tmp, red);
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+      const int dst = sort_idx[(long long)k * N + j];
+      ux[dst] = (x[j] + dx[j]) / sc;
+      uy[dst] = (y[j] + dy[j]) / sc;
+    }
+  } else {
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+      const long long o = (long long)k * 2 * N;
+      const double dxs = ((double)pred[o + j] * q[1] + q[0]) / 1e-5 * dt;
+      const double dys = ((double)pred[o + N + j] * q[3] + q[2]) / 1e-5 * dt;
+      const int dst = sort_idx[(long long)k * N + j];
+      ux[dst] = (Xin[o + j] + dxs) / sc;
+      uy[dst] = (Xin[o + N + j] + dys) / sc;
+    }
   }
   __syncthreads();
   const double cx = rot_center[2 * k], cy = rot_center[2 * k + 1];
@@ -837,6 +931,10 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
   ves_count_launch();
   translate_kernel<Real><<<nv, 128, (size_t)6 * N * sizeof(double), s>>>(N, prm->dt, X, vsum, rot, sidx, nout,
                                                                           m->adv_out, m->tw, Xa);
+  if (prm->conserve) {
+    ves_count_launch();
+    conserve_kernel<<<nv, 128, 0, s>>>(N, c->d1N, X, Xa);
+  }
   if (tr && tr->Xadv) cudaMemcpyAsync(tr->Xadv, Xa, n2 * sizeof(double), cudaMemcpyDeviceToDevice, s);
   ves_count_launch();
   filter_kernel<<<nv, 128, shf, s>>>(N, m->filt, Xa, nullptr, Xb);
@@ -854,7 +952,8 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
     ves_net_timing_end(c, s, net_flops_per_vesicle(m->relax) * nv);
   }
   ves_count_launch();
-  relax_post_kernel<Real><<<nv, 128, 0, s>>>(N, prm->dt, Xs2, nout, m->relax_out, scal2, rot2, rotc2, trn2, sidx2, Xa);
+  relax_post_kernel<Real><<<nv, 128, 0, s>>>(N, prm->dt, Xs2, nout, m->relax_out, scal2, rot2, rotc2, trn2, sidx2, Xa,
+                                             prm->conserve ? c->d1N : nullptr);
   // the plain BIEM step as judge and fallback of the surrogate: vesicles whose
   // area or length the surrogate moved by more than judge_tol take the implicit
   // step of the isolated vesicle with the same explicit velocity vsum

@@ -67,6 +67,13 @@ def parse():
                     "(relax, adv, near, selften, advten)")
     ap.add_argument("--synthetic-weights", action="store_true",
                     help="seeded synthetic networks instead of the trained ones in ves2dpy_gb300/trained")
+    ap.add_argument("--accuracy-steps", type=int, default=0,
+                    help="after the timed steps, continue the MLARM trajectory this many steps and compare with the "
+                         "BIEM step every --accuracy-every steps (velocity error, drift)")
+    ap.add_argument("--accuracy-every", type=int, default=25)
+    ap.add_argument("--conserve", action="store_true",
+                    help="MLARM option: advection and relaxation displacements area- and length-preserving to first "
+                         "order")
     ap.add_argument("--judge-tol", type=float, default=0.0,
                     help="> 0: the BIEM step judges each vesicle's surrogate step and stands in where it moved the "
                          "area or length by more than this (relative)")
@@ -265,7 +272,7 @@ def run_mlarm(a, dev, X0, state_dicts, norms=None):
                           nrm["relax_in"], nrm["relax_out"], nrm["near_in"], nrm["near_out"], nrm["selften_in"],
                           nrm["selften_out"], nrm["advten_in"], nrm["advten_out"], dev, state_dicts=state_dicts,
                           net_precision=a.nets, farfield_precision=a.precision, autotune=not a.no_autotune,
-                          judge_tol=a.judge_tol)
+                          judge_tol=a.judge_tol, conserve=a.conserve)
     Xd = torch.tensor(X0, dtype=torch.float64, device=dev)
     _, area0, len0 = Curve().geomProp(Xd)
     m.area0, m.len0 = area0, len0
@@ -343,9 +350,40 @@ def run_mlarm(a, dev, X0, state_dicts, norms=None):
     from ves2dpy_gb300.layout import to_vm
     sub = to_vm(Xw.to(dev))[: min(nv, 512)].contiguous()
     judge = TR.surrogate_errors(m.nets, norms or synthetic_norms(0), TR.standardize(sub))
+    accuracy = accuracy_leg(a, dev, m, X, t, area0, len0) if a.accuracy_steps > 0 else None
     return dict(ms=ms, stats=st, launches=launches, clocks=clk.summary(), net_ms=net_ms, e2e_s=e2e_s, io=io,
                 e2e_steps=e2e_steps, drift=drift, near_pairs=near_pairs, Xw=Xw.numpy().copy(), tw=tw,
-                X1=Xs1.cpu(), nets=m.nets, fallbacks=nfb, judge=judge)
+                X1=Xs1.cpu(), nets=m.nets, fallbacks=nfb, judge=judge, accuracy=accuracy)
+
+
+def accuracy_leg(a, dev, m, X, t, area0, len0):
+    """The MLARM trajectory continued from the timed steps' end for
+    --accuracy-steps steps; every --accuracy-every steps, one MLARM step and
+    one BIEM step from the same state give the velocity error, and the drift
+    of area and length since the start is recorded.  A failure ends the leg
+    and is reported with its step."""
+    import torch
+    from ves2dpy_gb300.curve import Curve
+    from ves2dpy_gb300.tstep_biem import TStepBiem
+    nv = X.shape[1]
+    prams = dict(STEP, viscCont=[1.0] * nv, gmresTol=a.biem_tol)
+    rows = []
+    try:
+        for k in range(a.accuracy_steps + 1):
+            if k % a.accuracy_every == 0:
+                tt = TStepBiem(X, None, dict(farField="shear", usePreco=True), prams, near="py_hh",
+                               farfield_precision=a.precision, sl_precision="fp32c", precond_precision=a.biem_precond)
+                Xb, *_ = tt.time_step(X, t)
+                Xm, _ = m.time_step_many_noinfo(X, t, 3)
+                _, ar, ln = Curve().geomProp(X)
+                drift = max(float(((ar - area0).abs() / area0).max()), float(((ln - len0).abs() / len0).max()))
+                rows.append({"step": k, "velocity_error": centroid_velocity_error(X, Xm, Xb, STEP["dt"], dev),
+                             "drift": drift})
+            if k < a.accuracy_steps:
+                X, t = m.time_step_many_noinfo(X, t, 3)
+    except Exception as e:  # the trajectory ended (e.g. a non-finite shape): report where
+        rows.append({"failed_at_step": k, "error": str(e)[:200]})
+    return rows
 
 
 def run_biem(a, dev, X0):
@@ -522,6 +560,8 @@ def run_gb300(a, rank, world):
             "mlarm": {"ms_per_step": ms_per_step, "near_pairs_excluded": r["near_pairs"],
                       "judge_tol": a.judge_tol, "biem_fallbacks_per_step": r["fallbacks"] / max(a.steps, 1),
                       "network_errors_vs_biem_operators": r["judge"],
+                      "conserve": a.conserve,
+                      "accuracy_along_trajectory": r["accuracy"],
                       "network_errors_note": "relative 2-norm error of each network (as the step runs it) against "
                                              "the BIEM operator it stands for, on 512 vesicles of the timed steps' "
                                              "starting state (ves_mlarm_targets; merged networks on |k| <= 16)",

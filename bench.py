@@ -230,6 +230,21 @@ def _events():
     return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
 
+def prepare_initial(X):
+    """The reference MLARM driver's preparation of the initial shapes
+    (entry_driver_manyfreeSpaceVesicle_N128.py:157-167): the reference area
+    and length first, then up to 10 equal-arclength passes.  Returns
+    (X, area0, len0)."""
+    from ves2dpy_gb300.curve import Curve
+    cv = Curve()
+    _, area0, len0 = cv.geomProp(X)
+    for _ in range(10):
+        X, good = cv.redistributeArcLength(X)
+        if good:
+            break
+    return X, area0, len0
+
+
 def networks(a):
     """(state dicts, normalisation arrays, description): the trained networks
     of ves2dpy_gb300/trained (ves2dpy_gb300.train_surrogate) unless
@@ -274,7 +289,7 @@ def run_mlarm(a, dev, X0, state_dicts, norms=None):
                           net_precision=a.nets, farfield_precision=a.precision, autotune=not a.no_autotune,
                           judge_tol=a.judge_tol, conserve=a.conserve)
     Xd = torch.tensor(X0, dtype=torch.float64, device=dev)
-    _, area0, len0 = Curve().geomProp(Xd)
+    Xd, area0, len0 = prepare_initial(Xd)
     m.area0, m.len0 = area0, len0
     ten = torch.zeros(N, nv, dtype=torch.float64, device=dev)
     X, t = Xd, ten

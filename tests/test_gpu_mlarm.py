@@ -167,20 +167,15 @@ def test_biem_fallback_is_the_biem_step_of_the_vesicle():
     """judge_tol: with a tolerance nothing meets, a vesicle takes the implicit
     BIEM step of the isolated vesicle with the step's explicit velocity.  A
     single vesicle has no far field, so that velocity is the background flow
-    and the vesicle moves as the plain BIEM step moves it (physical centre,
-    1e-5 of its velocity), whatever the networks predict; with a tolerance
-    everything meets, the step is the surrogate's, bit for bit."""
+    and the fallback shape (the step's relaxed shape before the
+    re-parametrisation and conditioning) is the plain BIEM step's result,
+    whatever the networks predict; with a tolerance everything meets, the
+    step is the surrogate's, bit for bit."""
     from ves2dpy_gb300.curve import Curve
     from ves2dpy_gb300.training import random_shapes
     from ves2dpy_gb300.tstep_biem import TStepBiem
     x = random_shapes(1, 21, reduced_area=(0.65, 0.65), amp=(0.02, 0.02))[0]
-    # modes above 16 removed, as the step's last filter does, and moved off the
-    # shear flow's zero line
-    z = np.fft.fft(x[:128] + 1j * x[128:])
-    k = np.fft.fftfreq(128, 1.0 / 128)
-    z[np.abs(k) > 16] = 0.0
-    w = np.fft.ifft(z)
-    X = torch.from_numpy(np.concatenate([w.real, w.imag + 3.0])[:, None].copy()).to(DEV)
+    X = torch.from_numpy(np.concatenate([x[:128], x[128:] + 3.0])[:, None].copy()).to(DEV)
     ten = torch.zeros(128, 1, dtype=torch.float64, device=DEV)
     m = _mlarm("bf16", "fp32m")
     _, a0, l0 = Curve().geomProp(X)
@@ -193,27 +188,22 @@ def test_biem_fallback_is_the_biem_step_of_the_vesicle():
         assert m.last_result.n_fallback == 0
         assert torch.equal(Xs, Xj)
         m.judge_tol = 1e-300
-        Xf, _ = m.time_step_many_noinfo(X, ten, 3)
+        tr = m.time_step_trace(X, ten)
         assert m.last_result.n_fallback == 1
     finally:
         m.judge_tol = 0.0
-    prams = dict(dt=1e-5, kappa=1.0, gmresTol=1e-12, gmresMaxIter=100, farFieldSpeed=2.0, viscCont=[1.0])
+    prams = dict(dt=1e-5, kappa=1.0, gmresTol=1e-13, gmresMaxIter=100, farFieldSpeed=2.0, viscCont=[1.0])
     tt = TStepBiem(X, None, dict(farField="shear", usePreco=True), prams, near="py_hh", farfield_precision="fp32m",
                    sl_precision="fp32c")
     Xb, *_ = tt.time_step(X, ten)
-    cv = Curve()
-    c0 = cv.getPhysicalCenter(X).double()
-    vb = (cv.getPhysicalCenter(Xb).double() - c0) / 1e-5
-    vf = (cv.getPhysicalCenter(Xf).double() - c0) / 1e-5
-    err = float(torch.linalg.norm(vf - vb) / torch.linalg.norm(vb))
-    assert err < 1e-5, err
+    assert rel(tr["Xrelax"], Xb) < 1e-10
 
 
 def test_conserve_keeps_area_and_length():
-    """conserve: the advection and relaxation displacements lose their
-    first-order area and length changes; with the seeded (untrained)
-    networks, whose displacements change both, one step's change of area and
-    length falls by more than ten times and below 1e-3."""
+    """conserve: the advection displacement loses its first-order area and
+    length changes.  In shear flow the seeded networks' inextensibility
+    correction is tiny, so the advected shape stretches at first order in dt;
+    with conserve on, only the second-order change is left."""
     import math
     from ves2dpy_gb300.curve import Curve
     from ves2dpy_gb300.suspension import random_suspension
@@ -228,10 +218,9 @@ def test_conserve_keeps_area_and_length():
     try:
         for flag in (False, True):
             m.conserve = flag
-            Xn, _ = m.time_step_many_noinfo(X, ten, 3)
-            _, a, l = cv.geomProp(Xn)
+            Xadv = m.time_step_trace(X, ten)["Xadv"]
+            _, a, l = cv.geomProp(Xadv)
             change[flag] = max(float(((a - a0) / a0).abs().max()), float(((l - l0) / l0).abs().max()))
     finally:
         m.conserve = False
-    assert change[True] < 0.1 * change[False], change
-    assert change[True] < 1e-3, change
+    assert change[True] < 1e-2 * change[False], change

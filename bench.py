@@ -74,6 +74,8 @@ def parse():
     ap.add_argument("--conserve", action="store_true",
                     help="MLARM option: advection and relaxation displacements area- and length-preserving to first "
                          "order")
+    ap.add_argument("--area-len-tol", type=float, default=0.0,
+                    help="tolerance of the MLARM step's area/length correction (0: the reference's 1e-2)")
     ap.add_argument("--judge-tol", type=float, default=0.0,
                     help="> 0: the BIEM step judges each vesicle's surrogate step and stands in where it moved the "
                          "area or length by more than this (relative)")
@@ -287,7 +289,7 @@ def run_mlarm(a, dev, X0, state_dicts, norms=None):
                           nrm["relax_in"], nrm["relax_out"], nrm["near_in"], nrm["near_out"], nrm["selften_in"],
                           nrm["selften_out"], nrm["advten_in"], nrm["advten_out"], dev, state_dicts=state_dicts,
                           net_precision=a.nets, farfield_precision=a.precision, autotune=not a.no_autotune,
-                          judge_tol=a.judge_tol, conserve=a.conserve)
+                          judge_tol=a.judge_tol, conserve=a.conserve, area_len_tol=a.area_len_tol)
     Xd = torch.tensor(X0, dtype=torch.float64, device=dev)
     Xd, area0, len0 = prepare_initial(Xd)
     m.area0, m.len0 = area0, len0
@@ -575,7 +577,7 @@ def run_gb300(a, rank, world):
             "mlarm": {"ms_per_step": ms_per_step, "near_pairs_excluded": r["near_pairs"],
                       "judge_tol": a.judge_tol, "biem_fallbacks_per_step": r["fallbacks"] / max(a.steps, 1),
                       "network_errors_vs_biem_operators": r["judge"],
-                      "conserve": a.conserve,
+                      "conserve": a.conserve, "area_len_tol": a.area_len_tol or 1e-2,
                       "accuracy_along_trajectory": r["accuracy"],
                       "network_errors_note": "relative 2-norm error of each network (as the step runs it) against "
                                              "the BIEM operator it stands for, on 512 vesicles of the timed steps' "

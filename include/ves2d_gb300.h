@@ -430,6 +430,11 @@ typedef struct ves_mlarm_params {
                                  components along n and kappa n removed), as the
                                  exact incompressible, inextensible dynamics is;
                                  0: the reference's step                           */
+  double area_len_tol;        /* relative area/length error beyond which the
+                                 step's correction acts and down to which it
+                                 corrects (correctAreaAndLengthAugLag's
+                                 tolConstraint, curve_batch_compile.py:603);
+                                 0: the reference's 1e-2                          */
 } ves_mlarm_params;
 typedef struct ves_mlarm_result {
   int n_near_pairs;           /* excluded (target point, source vesicle) pairs   */

@@ -141,6 +141,7 @@ class MlarmParams(ctypes.Structure):
         ("maxc", ctypes.c_int),
         ("judge_tol", ctypes.c_double),
         ("conserve", ctypes.c_int),
+        ("area_len_tol", ctypes.c_double),
     ]
 
 

@@ -198,8 +198,10 @@ int post_redistribute(ves_ctx* c, int nv, const double* X, double* Xout, int* fl
                       cudaStream_t s);
 void launch_align_center_angle(ves_ctx* c, int nv, const double* Xorg, const double* X, double* Xout,
                                double* center, double* angle, cudaStream_t s);
+// tol_constraint <= 0: the reference's 1e-2
 int post_correct_area_length(ves_ctx* c, int nv, const double* X, const double* area0, const double* length0,
-                             double* Xout, int* outer_iters, WsCarver& ws, cudaStream_t s);
+                             double* Xout, int* outer_iters, WsCarver& ws, cudaStream_t s,
+                             double tol_constraint = 0.0);
 
 // bending force of the MLARM step: bending of the Nup-upsampled shape truncated to N modes
 int launch_bend_up(ves_ctx* c, int nv, const double* X, double kappa, double* fB, cudaStream_t s);

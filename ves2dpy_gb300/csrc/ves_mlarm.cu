@@ -996,7 +996,7 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
   int iters = 0;
   {
     WsCarver w = sub();
-    if ((rc = post_correct_area_length(c, nv, Xc, area0, len0, Xb, &iters, w, s))) return rc;
+    if ((rc = post_correct_area_length(c, nv, Xc, area0, len0, Xb, &iters, w, s, prm->area_len_tol))) return rc;
   }
   if (tr && tr->Xcorr) cudaMemcpyAsync(tr->Xcorr, Xb, n2 * sizeof(double), cudaMemcpyDeviceToDevice, s);
   ves_count_launch();

@@ -542,7 +542,7 @@ void launch_align_center_angle(ves_ctx* c, int nv, const double* Xorg, const dou
 }
 
 int post_correct_area_length(ves_ctx* c, int nv, const double* X, const double* area0, const double* length0,
-                             double* Xout, int* outer_iters, WsCarver& ws, cudaStream_t s) {
+                             double* Xout, int* outer_iters, WsCarver& ws, cudaStream_t s, double tol_constraint) {
   const int N = c->N;
   const size_t n2 = (size_t)nv * 2 * N;
   double* z = ws.take<double>(n2);
@@ -567,7 +567,7 @@ int post_correct_area_length(ves_ctx* c, int nv, const double* X, const double* 
   if (nv <= 0) return VES_OK;
   int rc = ves_cuda_status(cudaMemcpyAsync(Xout, X, n2 * sizeof(double), cudaMemcpyDeviceToDevice, s), "copy");
   if (rc) return rc;
-  // current area and length; which vesicles violate the 1e-2 tolerance
+  // current area and length; which vesicles violate the tolerance
   launch_geom_prop(c, nv, X, nullptr, a, l, s);
   std::vector<double> ha(nv), hl(nv), ha0(nv), hl0(nv);
   rc = ves_cuda_status(cudaMemcpyAsync(ha.data(), a, nv * sizeof(double), cudaMemcpyDeviceToHost, s), "a");
@@ -576,7 +576,9 @@ int post_correct_area_length(ves_ctx* c, int nv, const double* X, const double* 
   if (!rc) rc = ves_cuda_status(cudaMemcpyAsync(hl0.data(), length0, nv * sizeof(double), cudaMemcpyDeviceToHost, s), "l0");
   if (!rc) rc = ves_cuda_status(cudaStreamSynchronize(s), "sync");
   if (rc) return rc;
-  const double tol_c = 1e-2, tol_f = 1e-2, lr = 3e-5;
+  // tolConstraint and tolFunctional (curve_batch_compile.py:603-604); the
+  // constraint tolerance may be tightened by the caller
+  const double tol_c = tol_constraint > 0 ? tol_constraint : 1e-2, tol_f = 1e-2, lr = 3e-5;
   std::vector<int> hidx;
   double ea = 0, el = 0;
   for (int k = 0; k < nv; ++k) {

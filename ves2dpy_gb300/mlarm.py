@@ -111,7 +111,9 @@ class MLARM_manyfree_py:
     the step's explicit velocity; ``last_result.n_fallback`` counts them; 0,
     the default, is the reference's step) and ``conserve`` (the advection and
     relaxation displacements made area- and length-preserving to first order,
-    as the exact dynamics is; off: the reference's step).
+    as the exact dynamics is; off: the reference's step) and
+    ``area_len_tol`` (the area/length correction's tolerance; 0: the
+    reference's 1e-2).
     """
 
     def __init__(self, dt, vinf, oc, use_repulsion, repStrength, rbf_upsample: int,
@@ -120,7 +122,7 @@ class MLARM_manyfree_py:
                  tenAdvNetInputNorm, tenAdvNetOutputNorm, device, logger=None, *, state_dicts=None,
                  model_dir: str = "../trained/torch_script_models", net_precision: str = "fp32",
                  farfield_precision: str = "fp32c", eval_near_net: bool = True, autotune: bool = True,
-                 judge_tol: float = 0.0, conserve: bool = False):
+                 judge_tol: float = 0.0, conserve: bool = False, area_len_tol: float = 0.0):
         if use_repulsion:
             raise NotImplementedError("MLARM_manyfree_py: repulsion is not supported")
         self.dt = float(dt)
@@ -138,6 +140,7 @@ class MLARM_manyfree_py:
         self.eval_near_net = bool(eval_near_net)
         self.judge_tol = float(judge_tol)
         self.conserve = bool(conserve)
+        self.area_len_tol = float(area_len_tol)
         self.area0 = None
         self.len0 = None
         self._norms = {
@@ -177,7 +180,7 @@ class MLARM_manyfree_py:
     def _params(self):
         return nat.MlarmParams(self.dt, self.kappa, nat.FLOW["shear"], 0.0, 0.0, 0.0,
                                nat.PREC[self.farfield_precision], 1 if self.eval_near_net else 0, self._maxc,
-                               self.judge_tol, 1 if self.conserve else 0)
+                               self.judge_tol, 1 if self.conserve else 0, self.area_len_tol)
 
     def _step(self, Xold, tenOld, trace=None):
         X = as_device_f64(Xold, self.device)

@@ -283,7 +283,8 @@ int net_forward_t(const ves_net* net, int nv, const Real* in, Real* out, WsCarve
   Real* p0 = nb > 1 ? ws.take<Real>(buf) : nullptr;
   Real* p1 = nb > 2 ? ws.take<Real>(buf) : nullptr;
   const bool tc = net->precision == VES_NET_BF16;
-  unsigned char* mid = tc ? ws.take<unsigned char>((size_t)nv * net->groups * net->mid_max) : nullptr;
+  // the tensor-core intermediates: nv rounded up to whole tiles of 4 vesicles
+  unsigned char* mid = tc ? ws.take<unsigned char>((size_t)((nv + 3) / 4 * 4) * net->groups * net->mid_max) : nullptr;
   if (ws.sizing) return VES_OK;
   if (!ws.ok()) {
     ves_record_error(VES_ERR_WORKSPACE, "net_forward: workspace too small (%zu needed)", ws.off);

@@ -24,7 +24,11 @@
 //
 // Three kernels per block: "down" (conv pair 1, conv pair 2), "up1"
 // (transposed conv 1) and "up2" (transposed conv 2, mix, residual and
-// pass-through).  The block input and output stay FP32 in global memory
+// pass-through).  up1 works on tiles of V1 = 128 / (L/4) vesicles of one
+// group whose rows are interleaved (row q*V1 + j holds position q of the
+// tile's vesicle j), so that its MMAs use all 128 rows: a shift of the input
+// by u positions is a shift by u*V1 rows, and every row still only meets
+// rows of its own vesicle.  down writes the intermediate in that layout.  The block input and output stay FP32 in global memory
 // ([nv][groups*channels][L]); the intermediates between the kernels are BF16
 // in the K-major layout.  Kernels are persistent: each CTA walks a contiguous
 // range of (group, vesicle) items, loading a group's weight image into shared
@@ -77,9 +81,10 @@ struct Geo {
   // arrays of warp group 0: cs [kcd][L/2+4][16B], ds [kcd][L+2][16B] (at least
   // cin*L*4 bytes: it first receives the block input)
   int u2merge, u2w, u2wm, u2cst, u2size, u2cs, u2ds, u2grp;
-  // per (vesicle, group) item in the workspace: down -> up1 [kcd][L/4][16B],
-  // then up1 -> up2 [kcd][L/2][16B]
+  // down -> up1 per tile of v1 vesicles: [kcd][L/4][v1][16B] (mid_bytes per
+  // vesicle); up1 -> up2 per (vesicle, group) item: [kcd][L/2][16B]
   int mid_bytes, mid2_bytes, mid_stride;
+  int v1;  // vesicles per up1 tile (v1 * L/4 = 128 rows)
 };
 
 constexpr int kMaxSmem = 227 * 1024 - 256;  // dynamic shared memory available next to the static part
@@ -147,7 +152,8 @@ inline Geo make_geo(const ves_net_block& b, int L) {
   g.u1cst = g.u1merge ? 5 * g.kcd * 2 * g.kcd * 8 * 16 : dec_unmerged;
   g.u1size = g.u1cst + 7 * 128 * 4;
   g.u1bs = g.u1size;
-  g.u1grp = g.kcd * (L / 4 + 4) * 16;
+  g.v1 = 128 / (L / 4);
+  g.u1grp = g.kcd * (L / 4 + 4) * g.v1 * 16;
   // up2: merged (one MMA of N = 2*Nd per tap) when the conv is not M-split
   // and the image still leaves room for three warp groups
   g.u2grp = g.kcd * (L / 2 + 4) * 16 + std::max(g.kcd * (L + 2) * 16, rup(g.cin * L * 4, 16));
@@ -176,7 +182,9 @@ struct KArgs {
   const unsigned char* img;  // group 0 image of this block; group stride = image size
   const float* x;            // block input [nv][G*cin][L]
   float* out;                // block output [nv][G*cout][L]
-  unsigned char* mid;        // [nv][G][mid_bytes]
+  unsigned char* mid;        // down -> up1: [ntiles][G][v1 * mid_bytes]
+  unsigned char* mid2;       // up1 -> up2: [nv][G][mid2_bytes]
+  int per_grp;               // items per channel group (nv, or up1 tiles)
   VesDeviceStatus* st;
 };
 
@@ -234,13 +242,13 @@ __device__ __forceinline__ void issue_conv(uint32_t d, uint64_t a0, uint64_t b0,
     for (int j = 0; j < NK; ++j) tc_mma_bf16(d, ad + j * stepA, bd + j * stepB, idesc, (oi | j) ? 1u : 0u);
   }
 }
-// transposed conv, one output parity: 5 taps u (A rows 4 - u) x NK K steps.
+// transposed conv, one output parity: 5 taps u (A rows (4 - u) * tapRows) x NK K steps.
 template <int NK>
 __device__ __forceinline__ void issue_deconv(uint32_t d, uint64_t a0, uint64_t b0, uint32_t bTap, uint32_t stepA,
-                                             uint32_t stepB, uint32_t idesc) {
+                                             uint32_t stepB, uint32_t idesc, uint32_t tapRows = 1) {
 #pragma unroll
   for (int u = 0; u < 5; ++u) {
-    const uint64_t ad = a0 + (uint32_t)(4 - u), bd = b0 + (uint32_t)u * bTap;
+    const uint64_t ad = a0 + (uint32_t)(4 - u) * tapRows, bd = b0 + (uint32_t)u * bTap;
 #pragma unroll
     for (int j = 0; j < NK; ++j) tc_mma_bf16(d, ad + j * stepA, bd + j * stepB, idesc, (u | j) ? 1u : 0u);
   }
@@ -515,10 +523,13 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
       phase ^= 1;
       tc_fence_after_sync();
       if (acc_row0(M2, qd) < L4) {
-        // the intermediate [kcd][L/4][16B] goes straight to global memory (coalesced 16-byte rows)
+        // the intermediate goes straight to global memory, row (kc, p) of
+        // vesicle j = v % v1 of its up1 tile at ((kc * L/4 + p) * v1 + j)
         const int p = acc_row(M2, qd, lane);
         const bool own = p >= 0 && p < L4;
-        uint4* gmid = reinterpret_cast<uint4*>(a.mid + ((size_t)v * a.G + sg.grp) * g.mid_stride);
+        const int V1 = g.v1;
+        uint4* gmid = reinterpret_cast<uint4*>(a.mid + ((size_t)(v / V1) * a.G + sg.grp) * (size_t)V1 * g.mid_bytes) +
+                      (v % V1);
 #pragma unroll
         for (int k0 = 0; k0 < kcd; k0 += 4) {
           float vv[32];
@@ -526,7 +537,8 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
           if (own) {
 #pragma unroll
             for (int k = 0; k < 4; ++k)
-              if (k0 + k < kcd) gmid[(size_t)(k0 + k) * L4 + p] = act8(vv + 8 * k, cst, k0 + k, g.d, 384, 512, 640);
+              if (k0 + k < kcd)
+                gmid[((size_t)(k0 + k) * L4 + p) * V1] = act8(vv + 8 * k, cst, k0 + k, g.d, 384, 512, 640);
           }
         }
       }
@@ -565,13 +577,14 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
 template <int KCD>
 __device__ __forceinline__ void deconv_issue(uint32_t dt, uint32_t sbase, uint32_t a_off, uint32_t lboA, int npos,
                                              int Nd, int kcd, bool merged, uint32_t w0, uint32_t w1, uint32_t bTap,
-                                             uint32_t lboB, bool allow_split = true, int Mrows = 128) {
+                                             uint32_t lboB, bool allow_split = true, int Mrows = 128,
+                                             uint32_t tapRows = 1) {
   const bool msplit = allow_split && 2 * npos <= 128;
   const uint32_t stepA = (2 * lboA) >> 4;
   if (merged && !msplit) {
     const uint32_t idesc = tc_idesc_bf16(Mrows, 2 * Nd);
     const uint64_t a0 = tc_desc(sbase + a_off, lboA, 128), b0 = tc_desc(sbase + w0, lboB, 128);
-#define VES_DEC(NK) issue_deconv<NK>(dt, a0, b0, bTap, stepA, (2 * lboB) >> 4, idesc)
+#define VES_DEC(NK) issue_deconv<NK>(dt, a0, b0, bTap, stepA, (2 * lboB) >> 4, idesc, tapRows)
     VES_TC_NK_SWITCH(kcd / 2, VES_DEC)
 #undef VES_DEC
   } else {
@@ -580,7 +593,7 @@ __device__ __forceinline__ void deconv_issue(uint32_t dt, uint32_t sbase, uint32
       const int lift = msplit ? r * npos * 16 : 0;
       const uint64_t a0 = tc_desc(sbase + a_off - lift, lboA, 128);
       const uint64_t b0 = tc_desc(sbase + (r ? w1 : w0), lboB, 128);
-#define VES_DEC(NK) issue_deconv<NK>(dt + r * Nd, a0, b0, bTap, stepA, (2 * lboB) >> 4, idesc)
+#define VES_DEC(NK) issue_deconv<NK>(dt + r * Nd, a0, b0, bTap, stepA, (2 * lboB) >> 4, idesc, tapRows)
       VES_TC_NK_SWITCH(kcd / 2, VES_DEC)
 #undef VES_DEC
     }
@@ -622,8 +635,11 @@ __device__ __forceinline__ void deconv_epilogue(uint32_t dt, int qd, int lane, i
   }
 }
 
-// up1: KCD compile-time K chunk count (0: from the geometry); NG warp groups
-// (TMEM columns [128*wg, 128*wg + 2*Nd) each).
+// up1: transposed conv 1 on tiles of v1 vesicles with interleaved rows
+// (M = v1 * L/4 = 128), both output parities in one MMA of N = 2*Nd (merged
+// image) or two MMAs on the same lanes.  KCD compile-time K chunk count (0:
+// from the geometry); NG warp groups (TMEM columns [128*wg, 128*wg + 2*Nd)
+// each).  Items are (group, tile) pairs, a.per_grp tiles per group.
 template <int KCD, int NG>
 __global__ void __launch_bounds__(NG * kGroupThreads, 1) up1_kernel(KArgs a) {
   extern __shared__ __align__(128) unsigned char sm[];
@@ -632,7 +648,8 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) up1_kernel(KArgs a) {
   __shared__ int fail[NG];
   const Geo& g = a.g;
   const int kcd = KCD ? KCD : g.kcd;
-  const int L = g.L, L2 = L / 2, L4 = L / 4;
+  const int L = g.L, L2 = L / 2, L4 = L / 4, V1 = g.v1;
+  const int ntiles = a.per_grp;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int wg = tid / kGroupThreads, gt = tid % kGroupThreads;
   const int qd = warp & 3;
@@ -656,36 +673,38 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) up1_kernel(KArgs a) {
   const uint32_t dt = tbase + 128 * wg;
   const uint32_t sbase = tc_smem_u32(sm);
   const float* cst = reinterpret_cast<const float*>(sm + g.u1cst);
-  const int PB = L4 + 4;
+  const int PB = (L4 + 4) * V1;  // rows per K chunk: 2*v1 zero rows, the tile's L4*v1 rows, 2*v1 zero rows
   const int Nd = kcd * 8;
+  const uint32_t chunk = (uint32_t)(L4 * V1 * 16);  // bytes of one K chunk of a tile
   uint4* bs = reinterpret_cast<uint4*>(sm + g.u1bs + wg * g.u1grp);
   const uint32_t bTap = (uint32_t)((g.u1merge ? 2 * Nd : g.d) * kcd * 16) >> 4;
   const uint32_t lboB1 = (uint32_t)((g.u1merge ? 2 * Nd : g.d) * 16);
-  const int M1 = (a.m64 && g.u1merge && L4 <= 64) ? 64 : 128;  // rows of the merged MMA
   const uint32_t w1 = g.u1merge ? (uint32_t)(g.u1w + Nd * 16) : (uint32_t)(g.u1w + 5 * kcd * g.d * 16);
+  // this thread's accumulator row: position q of the tile's vesicle j
+  const int row = 32 * qd + lane, q = row / V1, j = row % V1;
   unsigned phase = 0, mphase = 0;
   bool mpend = false;  // a bulk copy into bs is in flight
-  // intermediate [kcd][L/4][16B] of an item -> bs rows 2 .. L/4+1 of each chunk
+  // intermediate of a tile [kcd][L/4 * v1][16B] -> bs rows 2*v1 .. (L/4 + 2)*v1 - 1 of each chunk
   auto fetch_mid = [&](long long item) {
     if (gt == 0) {
-      const int grp = (int)(item / a.nv);
-      const long long v = item % a.nv;
-      const unsigned char* src = a.mid + ((size_t)v * a.G + grp) * g.mid_stride;
-      tc_expect_tx(&mbar[wg], (uint32_t)g.mid_bytes);
-      for (int kc = 0; kc < kcd; ++kc) tc_bulk_g2s(bs + kc * PB + 2, src + kc * L4 * 16, L4 * 16, &mbar[wg]);
+      const int grp = (int)(item / ntiles);
+      const long long t = item % ntiles;
+      const unsigned char* src = a.mid + ((size_t)t * a.G + grp) * (size_t)V1 * g.mid_bytes;
+      tc_expect_tx(&mbar[wg], chunk * (uint32_t)kcd);
+      for (int kc = 0; kc < kcd; ++kc) tc_bulk_g2s(bs + kc * PB + 2 * V1, src + (size_t)kc * chunk, chunk, &mbar[wg]);
     }
     mpend = true;
   };
   bool failed = false, stuck = false;
   for (long long lo = rg.lo; lo < rg.hi && !failed;) {
-    const Seg sg = next_seg(lo, rg.hi, a.nv);
+    const Seg sg = next_seg(lo, rg.hi, ntiles);
     __syncthreads();
     copy16(sm, a.img + (size_t)sg.grp * g.u1size, g.u1size);
     tc_fence_async_smem();
     __syncthreads();
     if (sg.lo + wg < sg.hi) fetch_mid(sg.lo + wg);
     for (long long it = sg.lo + wg; it < sg.hi; it += NG) {
-      const long long v = it % a.nv;
+      const long long t = it % ntiles;
       if (!group_wait_one(&mbar[wg], mphase, a.st, 26, wg, gt, &fail[wg])) {
         failed = true;
         break;
@@ -694,8 +713,8 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) up1_kernel(KArgs a) {
       mpend = false;
       tc_fence_after_sync();
       if (gt == 0) {
-        deconv_issue<KCD>(dt, sbase, g.u1bs + wg * g.u1grp, PB * 16, L4, Nd, kcd, g.u1merge != 0, g.u1w, w1, bTap,
-                          lboB1, g.u1merge == 0, M1);
+        deconv_issue<KCD>(dt, sbase, g.u1bs + wg * g.u1grp, PB * 16, 128, Nd, kcd, g.u1merge != 0, g.u1w, w1, bTap,
+                          lboB1, false, 128, (uint32_t)V1);
         tc_commit(&bar[wg]);
       }
       if (!group_wait_one(&bar[wg], phase, a.st, 23, wg, gt, &fail[wg])) {
@@ -706,8 +725,25 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) up1_kernel(KArgs a) {
       tc_fence_after_sync();
       // bs is free once the MMAs have completed: this group's next item
       if (it + NG < sg.hi) fetch_mid(it + NG);
-      uint4* dst = reinterpret_cast<uint4*>(a.mid + ((size_t)v * a.G + sg.grp) * g.mid_stride + g.mid_bytes);
-      deconv_epilogue<KCD>(dt, qd, lane, L4, Nd, kcd, g.d, cst, 0, 128, 256, dst, L2, 0, g.u1merge == 0, M1);
+      // output positions 2q + r of vesicle t*v1 + j -> its up1 -> up2 record
+      const long long v = t * V1 + j;
+      const bool own = v < a.nv;
+      uint4* dst = reinterpret_cast<uint4*>(a.mid2 + ((size_t)(own ? v : 0) * a.G + sg.grp) * g.mid2_bytes);
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+#pragma unroll
+        for (int k0 = 0; k0 < (KCD ? KCD : 8); k0 += 4) {
+          if (k0 >= kcd) break;
+          float vv[32];
+          tc_ld32(dt + ((uint32_t)(32 * qd) << 16) + r * Nd + 8 * k0, vv);
+          if (own) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+              if (k0 + k < kcd)
+                dst[(size_t)(k0 + k) * L2 + 2 * q + r] = act8(vv + 8 * k, cst, k0 + k, g.d, 0, 128, 256);
+          }
+        }
+      }
       tc_fence_before_sync();
       group_sync(wg);  // every TMEM read done before the next item's MMAs
     }
@@ -777,7 +813,7 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) up2_kernel(KArgs a) {
     if (gt == 0) {
       const int grp = (int)(item / a.nv);
       const long long v = item % a.nv;
-      const unsigned char* src = a.mid + ((size_t)v * a.G + grp) * g.mid_stride + g.mid_bytes;
+      const unsigned char* src = a.mid2 + ((size_t)v * a.G + grp) * g.mid2_bytes;
       tc_expect_tx(&mbar[wg], (uint32_t)g.mid2_bytes);
       for (int kc = 0; kc < kcd; ++kc) tc_bulk_g2s(cs + kc * PC + 2, src + kc * L2 * 16, L2 * 16, &mbar[wg]);
     }
@@ -1122,7 +1158,10 @@ int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_dow
   a.items = (long long)G * nv;
   a.x = x;
   a.out = out;
+  a.per_grp = nv;
+  const int ntiles = (nv + g.v1 - 1) / g.v1;
   a.mid = mid;
+  a.mid2 = mid + (size_t)ntiles * G * g.v1 * g.mid_bytes;
   a.st = st;
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
@@ -1143,6 +1182,7 @@ int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_dow
     b.m64 = m64;
     void (*fn)(KArgs);
     int smem;
+    int nblk = grid;
     if (which == 0) {
       fn = pick_down(kc1, kcd, ng);
       smem = std::max(g.dxs + ng * g.dgrp + kTail, kMinSmem);
@@ -1151,6 +1191,9 @@ int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_dow
       fn = pick_up1(kcd, ng);
       smem = std::max(g.u1size + ng * g.u1grp + kTail, kMinSmem);
       b.img = d_up1;
+      b.per_grp = ntiles;  // items: (group, tile)
+      b.items = (long long)G * ntiles;
+      nblk = (int)std::min<long long>(b.items, (long long)nsm);
     } else {
       fn = pick_up2(kcd, ng);
       smem = std::max(g.u2size + ng * g.u2grp + kTail, kMinSmem);
@@ -1160,7 +1203,7 @@ int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_dow
                              "tc smem attribute");
     if (rc) return rc;
     ves_count_launch();
-    fn<<<grid, ng * kGroupThreads, smem, s>>>(b);
+    fn<<<nblk, ng * kGroupThreads, smem, s>>>(b);
     return ves_launch_check("tc net block");
   };
   // the fixed rule: the most warp groups that fit, M = 64 MMAs where allowed
@@ -1207,7 +1250,7 @@ int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_dow
     best = 1e30f;
     for (int ng = 2; ng <= 4 && !rc; ng += 2) {
       if (ng == 4 && !u14) continue;
-      for (int m = 0; m < 2 && !rc; ++m) {
+      for (int m = 0; m < 1 && !rc; ++m) {
         if ((rc = timed(1, ng, m, t))) break;
         if (t < best) best = t, plan.ng_up1 = ng, plan.m64_up1 = m;
       }

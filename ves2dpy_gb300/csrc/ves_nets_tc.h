@@ -25,7 +25,8 @@ struct TcBlock {
 // arrays, see ves_net_create) for sequence length L.
 int tcnet_pack(const ves_net_block& b, int G, int L, const float* const* params, std::vector<unsigned char>& down,
                std::vector<unsigned char>& up1, std::vector<unsigned char>& up2, TcBlock& out);
-// One block: x [nv][G*cin][L] -> out [nv][G*cout][L] (FP32), mid = scratch of nv*G*mid_bytes.
+// One block: x [nv][G*cin][L] -> out [nv][G*cout][L] (FP32), mid = scratch of
+// (nv rounded up to a multiple of 4)*G*mid_bytes.
 // autotune: on the first call for a vesicle count, time every launch shape
 // that fits (warp groups per CTA, M = 64 MMAs on or off) of each kernel on
 // this input and keep the fastest for later calls with that count (the

@@ -154,10 +154,10 @@ inline Geo make_geo(const ves_net_block& b, int L) {
   g.u1bs = g.u1size;
   g.v1 = 128 / (L / 4);
   g.u1grp = g.kcd * (L / 4 + 4) * g.v1 * 16;
-  // up2: merged (one MMA of N = 2*Nd per tap) when the conv is not M-split
-  // and the image still leaves room for three warp groups
+  // up2: merged image (both parities in one operand of N = 2*Nd rows) when it
+  // still leaves room for three warp groups
   g.u2grp = g.kcd * (L / 2 + 4) * 16 + std::max(g.kcd * (L + 2) * 16, rup(g.cin * L * 4, 16));
-  for (g.u2merge = (2 * (L / 2) > 128) ? 1 : 0; g.u2merge >= 0; --g.u2merge) {
+  for (g.u2merge = 1; g.u2merge >= 0; --g.u2merge) {
     const int dbytes = g.u2merge ? 5 * g.kcd * 2 * g.kcd * 8 * 16 : dec_unmerged;
     g.u2w = 0;
     g.u2wm = dbytes;
@@ -483,7 +483,25 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
       }
       phase ^= 1;
       tc_fence_after_sync();
-      if (acc_row0(M1, qd) < L2) {  // uniform per warp: the TMEM loads are warp-wide
+      if (KC1 != 0 && M1 == 64) {
+        // M = 64: threads 0-15 and 16-31 of a warp take the two halves of the
+        // channel chunks of the same 16 rows (16x32bx2 loads)
+        const int p = 16 * qd + (lane & 15), par = p & 1, q = p >> 1;
+        const int kb = (lane >> 4) * (KC1 / 2);
+        float vv[32];
+        tc_ld16x2_32<4 * KC1>(d1 + ((uint32_t)(32 * qd) << 16), vv);
+        if (p < L2) {
+#pragma unroll
+          for (int k = 0; k < KC1 / 2; ++k) {
+            const int kc = kb + k;
+            const uint4 val = act8(vv + 8 * k, cst, kc, g.n1, 0, 128, 256);
+            uint4* base = as + (size_t)(par * kc1 + kc) * P2;
+            base[q + 3] = val;
+            if (q >= L4 - 3) base[q + 3 - L4] = val;
+            if (q < 3) base[q + 3 + L4] = val;
+          }
+        }
+      } else if (acc_row0(M1, qd) < L2) {  // uniform per warp: the TMEM loads are warp-wide
         const int p = acc_row(M1, qd, lane);
         const bool own = p >= 0 && p < L2;
         const int par = p & 1, q = p >> 1;
@@ -522,7 +540,22 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
       }
       phase ^= 1;
       tc_fence_after_sync();
-      if (acc_row0(M2, qd) < L4) {
+      if (KCD != 0 && M2 == 64) {
+        // M = 64, the two halves of the chunks on the two half-warps, as above
+        if (16 * qd < L4) {  // uniform per warp
+          const int p = 16 * qd + (lane & 15);
+          const int V1 = g.v1, kb = (lane >> 4) * (KCD / 2);
+          uint4* gmid = reinterpret_cast<uint4*>(a.mid + ((size_t)(v / V1) * a.G + sg.grp) * (size_t)V1 * g.mid_bytes) +
+                        (v % V1);
+          float vv[32];
+          tc_ld16x2_32<4 * KCD>(d2 + ((uint32_t)(32 * qd) << 16), vv);
+          if (p < L4) {
+#pragma unroll
+            for (int k = 0; k < KCD / 2; ++k)
+              gmid[((size_t)(kb + k) * L4 + p) * V1] = act8(vv + 8 * k, cst, kb + k, g.d, 384, 512, 640);
+          }
+        }
+      } else if (acc_row0(M2, qd) < L4) {
         // the intermediate goes straight to global memory, row (kc, p) of
         // vesicle j = v % v1 of its up1 tile at ((kc * L/4 + p) * v1 + j)
         const int p = acc_row(M2, qd, lane);
@@ -802,6 +835,9 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) up2_kernel(KArgs a) {
   uint4* ds = reinterpret_cast<uint4*>(sm + g.u2ds + goff);
   const float* xf = reinterpret_cast<const float*>(ds);  // block input while it sits in ds
   const bool need_x = g.residual || g.npass > 0;
+  // transposed conv of at most 64 input positions on the merged image: one
+  // M = 64 MMA per (tap, K step) with both parities on N
+  const bool m64dec = KCD != 0 && g.u2merge && L2 <= 64;
   const uint32_t xbytes = (uint32_t)(g.cin * L * 4);
   const uint32_t bTap = (uint32_t)((g.u2merge ? 2 * Nd : g.d) * kcd * 16) >> 4;
   const uint32_t lboB = (uint32_t)((g.u2merge ? 2 * Nd : g.d) * 16);
@@ -878,7 +914,8 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) up2_kernel(KArgs a) {
       mpend = false;
       group_sync_for_mma(wg);  // also: every read of the block input in ds is done
       if (gt == 0) {
-        deconv_issue<KCD>(dt, sbase, g.u2cs + goff, PC * 16, L2, Nd, kcd, g.u2merge != 0, g.u2w, w1, bTap, lboB);
+        deconv_issue<KCD>(dt, sbase, g.u2cs + goff, PC * 16, L2, Nd, kcd, g.u2merge != 0, g.u2w, w1, bTap, lboB,
+                          !m64dec, m64dec ? 64 : 128);
         tc_commit(&bar[wg]);
       }
       if (!group_wait_one(&bar[wg], phase, a.st, 24, wg, gt, &fail[wg])) {
@@ -889,7 +926,20 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) up2_kernel(KArgs a) {
       tc_fence_after_sync();
       // cs is free once the transposed conv has completed: this group's next item
       if (it + NG < sg.hi) fetch_mid(it + NG);
-      deconv_epilogue<KCD>(dt, qd, lane, L2, Nd, kcd, g.d, cst, 384, 512, 640, ds, PD, 1);
+      if (m64dec) {
+        // M = 64 rows (input positions q), parity r = lane / 16 at TMEM columns r*Nd (16x32bx2 loads)
+        const int q = 16 * qd + (lane & 15), r = lane >> 4;
+#pragma unroll
+        for (int k0 = 0; k0 < (KCD ? KCD : 8); k0 += 4) {
+          float vv[32];
+          tc_ld16x2_32<(KCD ? KCD : 8) * 8>(dt + ((uint32_t)(32 * qd) << 16) + 8 * k0, vv);
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            if (k0 + k < kcd) ds[(size_t)(k0 + k) * PD + 2 * q + r + 1] = act8(vv + 8 * k, cst, k0 + k, g.d, 384, 512, 640);
+        }
+      } else {
+        deconv_epilogue<KCD>(dt, qd, lane, L2, Nd, kcd, g.d, cst, 384, 512, 640, ds, PD, 1);
+      }
       // the halo rows of ds (zero padding of the mix) held block input
       if (gt < 2 * kcd) ds[(gt >> 1) * PD + ((gt & 1) ? L + 1 : 0)] = make_uint4(0, 0, 0, 0);
       group_sync_for_mma(wg);

@@ -28,7 +28,9 @@
 // group whose rows are interleaved (row q*V1 + j holds position q of the
 // tile's vesicle j), so that its MMAs use all 128 rows: a shift of the input
 // by u positions is a shift by u*V1 rows, and every row still only meets
-// rows of its own vesicle.  down writes the intermediate in that layout.  The block input and output stay FP32 in global memory
+// rows of its own vesicle.  down writes the intermediate in that layout.
+// down itself works on tiles of vd = 2 vesicles at L = 128 (conv pair 1
+// then fills 128 rows, conv pair 2 64), one vesicle at L = 256.  The block input and output stay FP32 in global memory
 // ([nv][groups*channels][L]); the intermediates between the kernels are BF16
 // in the K-major layout.  Kernels are persistent: each CTA walks a contiguous
 // range of (group, vesicle) items, loading a group's weight image into shared
@@ -85,6 +87,8 @@ struct Geo {
   // vesicle); up1 -> up2 per (vesicle, group) item: [kcd][L/2][16B]
   int mid_bytes, mid2_bytes, mid_stride;
   int v1;  // vesicles per up1 tile (v1 * L/4 = 128 rows)
+  int vd;  // vesicles per down tile (2 at L = 128: the block input is read
+           // from global memory (L2-prefetched) with no FP32 staging copy)
 };
 
 constexpr int kMaxSmem = 227 * 1024 - 256;  // dynamic shared memory available next to the static part
@@ -137,12 +141,13 @@ inline Geo make_geo(const ves_net_block& b, int L) {
   g.dcst = o;
   o += 6 * 128 * 4;
   g.dsize = o;
+  g.vd = (L / 2 <= 64) ? 2 : 1;
   g.dxs = o;
-  o += 2 * g.kcin * (L / 2 + 6) * 16;
+  o += 2 * g.kcin * (L / 2 + 6) * g.vd * 16;
   g.das = o;
-  o += 2 * g.kc1 * (L / 4 + 6) * 16;
+  o += 2 * g.kc1 * (L / 4 + 6) * g.vd * 16;
   g.dxf = o;
-  o += rup(g.cin * L * 4, 16);
+  o += g.vd == 1 ? rup(g.cin * L * 4, 16) : 0;
   g.dgrp = o - g.dxs;
   const int dec_unmerged = 10 * g.kcd * g.d * 16;
   // up1: both parities in one MMA of N = 2*Nd (u1merge, fewer and larger MMAs,
@@ -228,15 +233,16 @@ __device__ __forceinline__ bool group_wait_one(uint64_t* bar, unsigned phase, Ve
 // MMA).  Descriptors advance by adds: the start address is the low 14 bits of
 // a descriptor, in 16-byte units.
 
-// conv pair: 11 input shifts x NK K steps.  A at a0 + par*aPar + row,
-// B at b0 + oi*bOi; K steps at stepA / stepB.
+// conv pair: 11 input shifts x NK K steps.  A at a0 + par*aPar + row*rowMul
+// (rowMul: vesicles per tile, rows interleaved), B at b0 + oi*bOi; K steps at
+// stepA / stepB.
 template <int NK>
 __device__ __forceinline__ void issue_conv(uint32_t d, uint64_t a0, uint64_t b0, uint32_t aPar, uint32_t bOi,
-                                           uint32_t stepA, uint32_t stepB, uint32_t idesc) {
+                                           uint32_t stepA, uint32_t stepB, uint32_t idesc, uint32_t rowMul = 1) {
 #pragma unroll
   for (int oi = 0; oi < kOffsets; ++oi) {
     const int s = shift_of(oi);
-    const uint64_t ad = a0 + (uint32_t)((s & 1) * aPar + 3 + (s >> 1));
+    const uint64_t ad = a0 + (uint32_t)((s & 1) * aPar + (3 + (s >> 1)) * rowMul);
     const uint64_t bd = b0 + (uint32_t)oi * bOi;
 #pragma unroll
     for (int j = 0; j < NK; ++j) tc_mma_bf16(d, ad + j * stepA, bd + j * stepB, idesc, (oi | j) ? 1u : 0u);
@@ -375,6 +381,8 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
   const Geo& g = a.g;
   const int kc1 = KC1 ? KC1 : g.kc1, kcd = KCD ? KCD : g.kcd;
   const int L = g.L, L2 = L / 2, L4 = L / 4;
+  const int VD = g.vd;          // vesicles per item (tile), rows interleaved
+  const int ntl = a.per_grp;    // tiles per channel group
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int wg = tid / kGroupThreads, gt = tid % kGroupThreads;  // warp group, thread within it
   const int qd = warp & 3;                                       // TMEM lane quarter = position block
@@ -401,78 +409,96 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
   const uint32_t sbase = tc_smem_u32(sm);
   const int goff = wg * g.dgrp;
   const float* cst = reinterpret_cast<const float*>(sm + g.dcst);
-  const int P1 = L2 + 6, P2 = L4 + 6;
+  const int P1 = (L2 + 6) * VD, P2 = (L4 + 6) * VD;  // rows per K chunk (circular halos of 3 positions)
   uint4* xs = reinterpret_cast<uint4*>(sm + g.dxs + goff);
   uint4* as = reinterpret_cast<uint4*>(sm + g.das + goff);
   float* xf = reinterpret_cast<float*>(sm + g.dxf + goff);
   const uint32_t xbytes = (uint32_t)(g.cin * L * 4);
   unsigned phase = 0, xphase = 0;
   bool xpend = false;  // a bulk copy into xf is in flight
-  // block input x[v][grp*cin + c][pos] (cin*L contiguous floats) -> xf
+  // block input x[v][grp*cin + c][pos] (cin*L contiguous floats) of the
+  // item's vesicles: one vesicle -> xf by bulk copy; a tile of two -> L2
+  // (read by convert_x straight from global memory)
   auto fetch_x = [&](long long item) {
-    if (gt == 0) {
-      const int grp = (int)(item / a.nv);
-      const long long v = item % a.nv;
-      tc_expect_tx(&xbar[wg], xbytes);
-      tc_bulk_g2s(xf, a.x + ((long long)v * a.G + grp) * (long long)g.cin * L, xbytes, &xbar[wg]);
+    const int grp = (int)(item / ntl);
+    const long long t = item % ntl;
+    if (VD == 1) {
+      if (gt == 0) {
+        tc_expect_tx(&xbar[wg], xbytes);
+        tc_bulk_g2s(xf, a.x + ((long long)t * a.G + grp) * (long long)g.cin * L, xbytes, &xbar[wg]);
+      }
+      xpend = true;
+    } else if (gt < VD && t * VD + gt < a.nv) {
+      tc_prefetch_l2(a.x + ((t * VD + gt) * a.G + grp) * (long long)g.cin * L, xbytes);
     }
-    xpend = true;
   };
-  // xf -> parity-split BF16 rows with circular halos of 3; one thread per
-  // (8-channel chunk, position pair 2m, 2m+1)
-  auto convert_x = [&]() {
+  // block input -> parity-split BF16 rows with circular halos of 3
+  // positions, position m of vesicle j at row (m + 3)*VD + j; one thread per
+  // (8-channel chunk, vesicle, position pair 2m, 2m+1)
+  auto convert_x = [&](long long t, int grp) {
     const int lg2 = g.lgL - 1;
-    for (int i = gt; i < g.kcin * L2; i += kGroupThreads) {
-      const int kc = i >> lg2, m = i & (L2 - 1);
+    for (int i = gt; i < g.kcin * VD * L2; i += kGroupThreads) {
+      const int m = i & (L2 - 1), kj = i >> lg2, kc = kj / VD, j = kj - kc * VD;
+      const long long v = t * VD + j;
       float2 y[8];
+      if (VD == 1) {
 #pragma unroll
-      for (int e = 0; e < 8; ++e)
-        y[e] = (8 * kc + e < g.cin) ? *reinterpret_cast<const float2*>(xf + (8 * kc + e) * L + 2 * m)
-                                    : make_float2(0.f, 0.f);
+        for (int e = 0; e < 8; ++e)
+          y[e] = (8 * kc + e < g.cin) ? *reinterpret_cast<const float2*>(xf + (8 * kc + e) * L + 2 * m)
+                                      : make_float2(0.f, 0.f);
+      } else {
+        const float* src = a.x + ((v < a.nv ? v : 0) * a.G + grp) * (long long)g.cin * L;
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+          y[e] = (8 * kc + e < g.cin && v < a.nv) ? __ldg(reinterpret_cast<const float2*>(src + (8 * kc + e) * L + 2 * m))
+                                                  : make_float2(0.f, 0.f);
+      }
       const uint4 v0 = make_uint4(pack_bf2(y[0].x, y[1].x), pack_bf2(y[2].x, y[3].x), pack_bf2(y[4].x, y[5].x),
                                   pack_bf2(y[6].x, y[7].x));
       const uint4 v1 = make_uint4(pack_bf2(y[0].y, y[1].y), pack_bf2(y[2].y, y[3].y), pack_bf2(y[4].y, y[5].y),
                                   pack_bf2(y[6].y, y[7].y));
-      uint4* b0 = xs + (size_t)kc * P1;
-      uint4* b1 = xs + (size_t)(g.kcin + kc) * P1;
-      b0[m + 3] = v0;
-      b1[m + 3] = v1;
+      uint4* b0 = xs + (size_t)kc * P1 + j;
+      uint4* b1 = xs + (size_t)(g.kcin + kc) * P1 + j;
+      b0[(m + 3) * VD] = v0;
+      b1[(m + 3) * VD] = v1;
       if (m >= L2 - 3) {
-        b0[m + 3 - L2] = v0;
-        b1[m + 3 - L2] = v1;
+        b0[(m + 3 - L2) * VD] = v0;
+        b1[(m + 3 - L2) * VD] = v1;
       }
       if (m < 3) {
-        b0[m + 3 + L2] = v0;
-        b1[m + 3 + L2] = v1;
+        b0[(m + 3 + L2) * VD] = v0;
+        b1[(m + 3 + L2) * VD] = v1;
       }
     }
   };
   bool failed = false, stuck = false;  // stuck: this warp group's own MMA wait timed out
   for (long long lo = rg.lo; lo < rg.hi && !failed;) {
-    const Seg sg = next_seg(lo, rg.hi, a.nv);
+    const Seg sg = next_seg(lo, rg.hi, ntl);
     __syncthreads();
     copy16(sm, a.img + (size_t)sg.grp * g.dsize, g.dsize);  // whole CTA
     tc_fence_async_smem();  // weights (and the zeroed padding) -> tensor core, for both groups
     __syncthreads();
     if (sg.lo + wg < sg.hi) fetch_x(sg.lo + wg);
     for (long long it = sg.lo + wg; it < sg.hi; it += NG) {
-      const long long v = it % a.nv;
-      if (!group_wait_one(&xbar[wg], xphase, a.st, 20, wg, gt, &fail[wg])) {
-        failed = true;
-        break;
+      const long long t = it % ntl;
+      if (VD == 1) {
+        if (!group_wait_one(&xbar[wg], xphase, a.st, 20, wg, gt, &fail[wg])) {
+          failed = true;
+          break;
+        }
+        xphase ^= 1;
+        xpend = false;
       }
-      xphase ^= 1;
-      xpend = false;
-      convert_x();
+      convert_x(t, sg.grp);
       group_sync_for_mma(wg);  // xs complete; xf fully read
       if (it + NG < sg.hi) fetch_x(it + NG);
-      // conv pair 1: D1[p][o], p < L/2 on the lanes, o < n1 in the columns
-      const int M1 = (a.m64 && L2 <= 64) ? 64 : 128, M2 = (a.m64 && L4 <= 64) ? 64 : 128;
+      // conv pair 1: D1[r][o], rows r = p*VD + j (p < L/2) on the lanes, o < n1 in the columns
+      const int M1 = (a.m64 && L2 * VD <= 64) ? 64 : 128, M2 = (a.m64 && L4 * VD <= 64) ? 64 : 128;
       if (gt == 0) {
         const uint32_t idesc = tc_idesc_bf16(M1, N1);
         const uint32_t lboA = P1 * 16, lboB = g.n1 * 16;
         const uint64_t a0 = tc_desc(sbase + g.dxs + goff, lboA, 128), b0 = tc_desc(sbase + g.dw1, lboB, 128);
-#define VES_CONV1(NK) issue_conv<NK>(d1, a0, b0, (g.kcin * lboA) >> 4, (g.kcin * lboB) >> 4, (2 * lboA) >> 4, (2 * lboB) >> 4, idesc)
+#define VES_CONV1(NK) issue_conv<NK>(d1, a0, b0, (g.kcin * lboA) >> 4, (g.kcin * lboB) >> 4, (2 * lboA) >> 4, (2 * lboB) >> 4, idesc, (uint32_t)VD)
         VES_TC_NK_SWITCH(g.kcin / 2, VES_CONV1)
 #undef VES_CONV1
         tc_commit(&bar[wg]);
@@ -483,10 +509,12 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
       }
       phase ^= 1;
       tc_fence_after_sync();
+      // the epilogue's row r holds position p = r / VD of the tile's vesicle j = r % VD;
+      // conv pair 2 reads position q of parity par at row (q + 3)*VD + j
       if (KC1 != 0 && M1 == 64) {
         // M = 64: threads 0-15 and 16-31 of a warp take the two halves of the
         // channel chunks of the same 16 rows (16x32bx2 loads)
-        const int p = 16 * qd + (lane & 15), par = p & 1, q = p >> 1;
+        const int r = 16 * qd + (lane & 15), p = r / VD, j = r - p * VD, par = p & 1, q = p >> 1;
         const int kb = (lane >> 4) * (KC1 / 2);
         float vv[32];
         tc_ld16x2_32<4 * KC1>(d1 + ((uint32_t)(32 * qd) << 16), vv);
@@ -495,15 +523,15 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
           for (int k = 0; k < KC1 / 2; ++k) {
             const int kc = kb + k;
             const uint4 val = act8(vv + 8 * k, cst, kc, g.n1, 0, 128, 256);
-            uint4* base = as + (size_t)(par * kc1 + kc) * P2;
-            base[q + 3] = val;
-            if (q >= L4 - 3) base[q + 3 - L4] = val;
-            if (q < 3) base[q + 3 + L4] = val;
+            uint4* base = as + (size_t)(par * kc1 + kc) * P2 + j;
+            base[(q + 3) * VD] = val;
+            if (q >= L4 - 3) base[(q + 3 - L4) * VD] = val;
+            if (q < 3) base[(q + 3 + L4) * VD] = val;
           }
         }
-      } else if (acc_row0(M1, qd) < L2) {  // uniform per warp: the TMEM loads are warp-wide
-        const int p = acc_row(M1, qd, lane);
-        const bool own = p >= 0 && p < L2;
+      } else if (acc_row0(M1, qd) < L2 * VD) {  // uniform per warp: the TMEM loads are warp-wide
+        const int r = acc_row(M1, qd, lane), p = r / VD, j = r - p * VD;
+        const bool own = r >= 0 && p < L2;
         const int par = p & 1, q = p >> 1;
 #pragma unroll
         for (int k0 = 0; k0 < kc1; k0 += 4) {
@@ -515,10 +543,10 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
               const int kc = k0 + k;
               if (kc >= kc1) break;
               const uint4 val = act8(vv + 8 * k, cst, kc, g.n1, 0, 128, 256);
-              uint4* base = as + (size_t)(par * kc1 + kc) * P2;
-              base[q + 3] = val;
-              if (q >= L4 - 3) base[q + 3 - L4] = val;
-              if (q < 3) base[q + 3 + L4] = val;
+              uint4* base = as + (size_t)(par * kc1 + kc) * P2 + j;
+              base[(q + 3) * VD] = val;
+              if (q >= L4 - 3) base[(q + 3 - L4) * VD] = val;
+              if (q < 3) base[(q + 3 + L4) * VD] = val;
             }
           }
         }
@@ -529,7 +557,7 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
         const uint32_t idesc = tc_idesc_bf16(M2, N2);
         const uint32_t lboA = P2 * 16, lboB = g.d * 16;
         const uint64_t a0 = tc_desc(sbase + g.das + goff, lboA, 128), b0 = tc_desc(sbase + g.dw2, lboB, 128);
-#define VES_CONV2(NK) issue_conv<NK>(d2, a0, b0, (kc1 * lboA) >> 4, (kc1 * lboB) >> 4, (2 * lboA) >> 4, (2 * lboB) >> 4, idesc)
+#define VES_CONV2(NK) issue_conv<NK>(d2, a0, b0, (kc1 * lboA) >> 4, (kc1 * lboB) >> 4, (2 * lboA) >> 4, (2 * lboB) >> 4, idesc, (uint32_t)VD)
         VES_TC_NK_SWITCH(kc1 / 2, VES_CONV2)
 #undef VES_CONV2
         tc_commit(&bar[wg]);
@@ -540,29 +568,33 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) down_kernel(KArgs a) {
       }
       phase ^= 1;
       tc_fence_after_sync();
+      // the intermediate goes straight to global memory: row (kc, p) of
+      // vesicle v = t*VD + j sits in its up1 tile (v / v1) at ((kc * L/4 + p) * v1 + v % v1)
       if (KCD != 0 && M2 == 64) {
         // M = 64, the two halves of the chunks on the two half-warps, as above
-        if (16 * qd < L4) {  // uniform per warp
-          const int p = 16 * qd + (lane & 15);
+        if (16 * qd < L4 * VD) {  // uniform per warp
+          const int r = 16 * qd + (lane & 15), p = r / VD, j = r - p * VD;
+          const long long v = t * VD + j;
           const int V1 = g.v1, kb = (lane >> 4) * (KCD / 2);
-          uint4* gmid = reinterpret_cast<uint4*>(a.mid + ((size_t)(v / V1) * a.G + sg.grp) * (size_t)V1 * g.mid_bytes) +
-                        (v % V1);
+          const long long vs = v < a.nv ? v : 0;
+          uint4* gmid = reinterpret_cast<uint4*>(a.mid + ((size_t)(vs / V1) * a.G + sg.grp) * (size_t)V1 * g.mid_bytes) +
+                        (vs % V1);
           float vv[32];
           tc_ld16x2_32<4 * KCD>(d2 + ((uint32_t)(32 * qd) << 16), vv);
-          if (p < L4) {
+          if (p < L4 && v < a.nv) {
 #pragma unroll
             for (int k = 0; k < KCD / 2; ++k)
               gmid[((size_t)(kb + k) * L4 + p) * V1] = act8(vv + 8 * k, cst, kb + k, g.d, 384, 512, 640);
           }
         }
-      } else if (acc_row0(M2, qd) < L4) {
-        // the intermediate goes straight to global memory, row (kc, p) of
-        // vesicle j = v % v1 of its up1 tile at ((kc * L/4 + p) * v1 + j)
-        const int p = acc_row(M2, qd, lane);
-        const bool own = p >= 0 && p < L4;
+      } else if (acc_row0(M2, qd) < L4 * VD) {
+        const int r = acc_row(M2, qd, lane), p = r / VD, j = r - p * VD;
+        const long long v = t * VD + j;
+        const bool own = r >= 0 && p < L4 && v < a.nv;
         const int V1 = g.v1;
-        uint4* gmid = reinterpret_cast<uint4*>(a.mid + ((size_t)(v / V1) * a.G + sg.grp) * (size_t)V1 * g.mid_bytes) +
-                      (v % V1);
+        const long long vs = own ? v : 0;
+        uint4* gmid = reinterpret_cast<uint4*>(a.mid + ((size_t)(vs / V1) * a.G + sg.grp) * (size_t)V1 * g.mid_bytes) +
+                      (vs % V1);
 #pragma unroll
         for (int k0 = 0; k0 < kcd; k0 += 4) {
           float vv[32];
@@ -1237,6 +1269,9 @@ int tcnet_run_block(const TcBlock& tb, int G, int nv, const unsigned char* d_dow
       fn = pick_down(kc1, kcd, ng);
       smem = std::max(g.dxs + ng * g.dgrp + kTail, kMinSmem);
       b.img = d_down;
+      b.per_grp = (nv + g.vd - 1) / g.vd;  // items: (group, tile of vd vesicles)
+      b.items = (long long)G * b.per_grp;
+      nblk = (int)std::min<long long>(b.items, (long long)nsm);
     } else if (which == 1) {
       fn = pick_up1(kcd, ng);
       smem = std::max(g.u1size + ng * g.u1grp + kTail, kMinSmem);

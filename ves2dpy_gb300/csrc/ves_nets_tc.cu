@@ -673,6 +673,27 @@ __device__ __forceinline__ void deconv_epilogue(uint32_t dt, int qd, int lane, i
                                                 int row0, bool allow_split = true, int Mrows = 128) {
   const bool msplit = allow_split && 2 * npos <= 128;
   const int lane0 = 32 * qd;
+  if (!msplit) {
+    // both parities on this lane: one wait for the two parities' columns
+    if (acc_row0(Mrows, qd) >= npos) return;  // uniform per warp
+    const int q = acc_row(Mrows, qd, lane);
+    const bool own = q >= 0 && q < npos;
+#pragma unroll
+    for (int k0 = 0; k0 < (KCD ? KCD : 8); k0 += 4) {
+      if (k0 >= kcd) break;
+      float vv[64];
+      tc_ld32x2(dt + ((uint32_t)lane0 << 16) + 8 * k0, dt + ((uint32_t)lane0 << 16) + Nd + 8 * k0, vv);
+      if (own) {
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            if (k0 + k < kcd)
+              dst[(size_t)(k0 + k) * pitch + 2 * q + r + row0] = act8(vv + 32 * r + 8 * k, cst, k0 + k, nreal, ob, os, ot);
+      }
+    }
+    return;
+  }
 #pragma unroll
   for (int r = 0; r < 2; ++r) {
     int q;
@@ -995,13 +1016,25 @@ __global__ void __launch_bounds__(NG * kGroupThreads, 1) up2_kernel(KArgs a) {
       tc_fence_after_sync();
       // ds is free once the mix has completed: the block input of this group's next item
       if (need_x && it + NG < sg.hi) fetch_x(it + NG);
-      for (int h = 0; h < nh; ++h) {
-        const int p = 128 * h + 32 * qd + lane;
-        float vv[32];
-        tc_ld32(dt + ((uint32_t)(32 * qd) << 16) + mcol + h * Nm, vv);
+      if (nh == 2) {  // both 128-position halves, one wait
+        const int p = 32 * qd + lane;
+        float vv[64];
+        tc_ld32x2(dt + ((uint32_t)(32 * qd) << 16) + mcol, dt + ((uint32_t)(32 * qd) << 16) + mcol + Nm, vv);
 #pragma unroll
         for (int o = 0; o < 32; ++o)
-          if (o < g.cmix) op[(size_t)o * L + p] = vv[o];
+          if (o < g.cmix) {
+            op[(size_t)o * L + p] = vv[o];
+            op[(size_t)o * L + 128 + p] = vv[32 + o];
+          }
+      } else {
+        for (int h = 0; h < nh; ++h) {
+          const int p = 128 * h + 32 * qd + lane;
+          float vv[32];
+          tc_ld32(dt + ((uint32_t)(32 * qd) << 16) + mcol + h * Nm, vv);
+#pragma unroll
+          for (int o = 0; o < 32; ++o)
+            if (o < g.cmix) op[(size_t)o * L + p] = vv[o];
+        }
       }
       tc_fence_before_sync();
       group_sync(wg);

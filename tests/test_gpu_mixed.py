@@ -7,6 +7,8 @@ TStepBiemMixed).
 * Groups of N = 16 and N = 32 close enough for near pairs inside and between
   the groups: against the oracle's multi-group step at 1e-9, the tolerance of
   the MATLAB-scheme step test.
+* The multipole precision (one all-pairs launch over every group) against
+  the FP64 per-pair step of the same suspension.
 * The uneven suspension (3000 vesicles of N = 32 and 1000 of N = 128, reduced
   areas uniform in [0.6, 0.9], 20% area fraction, Poiseuille flow
   u = (1 - y^2 / W^2, 0) with W = 60): GMRES converges at 1e-8 with the FP32
@@ -89,6 +91,30 @@ def test_mixed_two_sizes_vs_oracle():
         assert rel(Xo[g], ref_X[g]) < 1e-9, (g, rel(Xo[g], ref_X[g]))
         assert rel(so[g], ref_s[g]) < 1e-6, (g, rel(so[g], ref_s[g]))
 
+
+
+def test_mixed_fp32m_one_launch_matches_fp64():
+    """With the multipole precision the far field of every group from the
+    sources of every group runs as one launch (farfield_mp_groups_run), and
+    the MATLAB corrections per pair of groups follow; the step agrees with the
+    FP64 step that sums group pair by group pair, to the FP32 accuracy of the
+    sums: velocities (Xnew - X)/dt at 1e-5, GMRES counts within one."""
+    from ves2dpy_gb300.tstep_biem import TStepBiemMixed
+    Xs = _two_sizes()
+    sig = [torch.zeros(X.shape[0] // 2, X.shape[1], dtype=torch.float64, device=DEV) for X in Xs]
+    prams = dict(PRAMS, gmresTol=1e-8)
+    out = {}
+    for prec in ("fp64", "fp32m"):
+        mix = TStepBiemMixed([T(X) for X in Xs], OPTS, prams, near="matlab", farfield_precision=prec,
+                             sl_precision="fp64")
+        Xo, so, it, fl = mix.time_step([T(X) for X in Xs], sig)
+        assert not fl
+        out[prec] = (Xo, mix.last.matvecs)
+    for g in range(2):
+        v64 = (out["fp64"][0][g] - T(Xs[g])) / PRAMS["dt"]
+        v32 = (out["fp32m"][0][g] - T(Xs[g])) / PRAMS["dt"]
+        assert rel(v32, v64) < 1e-5, (g, rel(v32, v64))
+    assert abs(out["fp32m"][1] - out["fp64"][1]) <= 1
 
 def test_uneven_suspension_poiseuille():
     from ves2dpy_gb300.suspension import mixed_suspension

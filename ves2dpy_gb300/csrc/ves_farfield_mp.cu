@@ -205,78 +205,70 @@ __global__ void __launch_bounds__(256) mp_prep_targets_kernel(int ntp, const dou
   }
 }
 
-struct MPArgs {
-  int nsrc, ns, ntp;
-  const float4* rec;
-  const MPSrc* src;
-  const MPMom* mom;
-  const float2* tloc;
-  const float2* thi;
-  const float2* tlo;
-  const int* self_idx;
-  const int* cand_count;
-  const int* cand_src;
-  const uint32_t* excl_mask;
-  int maxc, nwords;
-  double* out;               // [nt][2][ntp], scaled by 1/(4 pi)
-  unsigned long long* work;  // optional: series terms, direct pairs (per target point)
-};
-
 __device__ __forceinline__ void neumaier(float& tot, float& cmp, float v) {
   const float t = tot + v;
   cmp += (fabsf(tot) >= fabsf(v)) ? (tot - t) + v : (v - t) + tot;
   tot = t;
 }
 
-// One CTA per target column (blockDim = ntp rounded up to a warp multiple).
-// Dynamic shared memory: the direct-rule records of one source (ns float4).
-__global__ void __launch_bounds__(128) mp_eval_kernel(MPArgs p) {
-  extern __shared__ __align__(16) float4 drec[];
-  __shared__ MPSrc ssrc[kStage];
-  __shared__ MPMom smom[kStage][kPMax + 1];
-  __shared__ float rmax_w[32];
-  const int col = blockIdx.x, i = threadIdx.x;
-  const bool valid = i < p.ntp;
-  const float2 tl = valid ? p.tloc[(long long)col * p.ntp + i] : make_float2(0.f, 0.f);
-  const float2 thi = p.thi[col], tlo = p.tlo[col];
-  // radius of the target vesicle about its centre
-  float rt = sqrtf(tl.x * tl.x + tl.y * tl.y);
-  for (int o = 16; o > 0; o >>= 1) rt = fmaxf(rt, __shfl_xor_sync(0xffffffffu, rt, o));
-  if ((i & 31) == 0) rmax_w[i >> 5] = rt;
-  __syncthreads();
-  float RT = 0.f;
-  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) RT = fmaxf(RT, rmax_w[w]);
-  RT *= 1.0f + 1e-6f;
-  const int self = p.self_idx ? p.self_idx[col] : -1;
-  const int cend = p.cand_count ? min(p.cand_count[col], p.maxc) : 0;
-  const int* cands = p.cand_src ? p.cand_src + (long long)col * p.maxc : nullptr;
+// One source set (the upsampled points of one group of vesicles).
+struct MPSet {
+  int nsrc, ns;
+  const float4* rec;  // [nsrc][ns] direct-rule records
+  const MPSrc* src;   // [nsrc]
+  const MPMom* mom;   // [nsrc][kPMax + 1]
+};
+
+// The near-candidate list of one target column against one source set.
+struct MPNearCol {
+  int self;              // source index of the target's own vesicle, or -1
+  int cend;              // candidates on the list
+  const int* cands;      // ascending source indices
+  const uint32_t* excl;  // [maxc][nwords] excluded target points per candidate
+  int nwords;
+};
+
+// Per-CTA staging of the source records and moments.
+struct MPStage {
+  MPSrc* src;                 // [kStage]
+  MPMom (*mom)[kPMax + 1];    // [kStage][kPMax + 1]
+  float4* drec;               // [ns] direct-rule records of one source
+};
+
+// Sum over every source of one set onto this thread's target point (tl
+// relative to the target centre thi + tlo, RT the target radius): the
+// expansion for well-separated pairs, the direct rule for the others and for
+// every pair on the near list (excluded points dropped); the target's own
+// vesicle is skipped.  Uniform control flow across the CTA.
+__device__ __forceinline__ void mp_sum_set(const MPSet& S, const MPNearCol& nr, const MPStage& st, int i, bool valid,
+                                           float2 tl, float2 thi, float2 tlo, float RT, float& tot_x, float& tot_y,
+                                           float& cmp_x, float& cmp_y, unsigned long long& terms,
+                                           unsigned long long& ndirect) {
   int cur = 0;
-  float tot_x = 0.f, tot_y = 0.f, cmp_x = 0.f, cmp_y = 0.f;
-  unsigned long long terms = 0, ndirect = 0;  // work of this column (uniform across the CTA)
-  for (int s0 = 0; s0 < p.nsrc; s0 += kStage) {
-    const int nst = min(kStage, p.nsrc - s0);
+  for (int s0 = 0; s0 < S.nsrc; s0 += kStage) {
+    const int nst = min(kStage, S.nsrc - s0);
     __syncthreads();
-    for (int q = i; q < nst; q += blockDim.x) ssrc[q] = p.src[s0 + q];
+    for (int q = i; q < nst; q += blockDim.x) st.src[q] = S.src[s0 + q];
     for (int q = i; q < nst * (kPMax + 1); q += blockDim.x)
-      (&smom[0][0])[q] = p.mom[(long long)s0 * (kPMax + 1) + q];
+      (&st.mom[0][0])[q] = S.mom[(long long)s0 * (kPMax + 1) + q];
     __syncthreads();
     for (int q = 0; q < nst; ++q) {
       const int s = s0 + q;
-      if (s == self) continue;
-      const MPSrc S = ssrc[q];
+      if (s == nr.self) continue;
+      const MPSrc Sq = st.src[q];
       // target relative to the source centre (hi/lo: no cancellation from absolute positions)
-      const float ox = (thi.x - S.chi.x) + (tlo.x - S.clo.x);
-      const float oy = (thi.y - S.chi.y) + (tlo.y - S.clo.y);
+      const float ox = (thi.x - Sq.chi.x) + (tlo.x - Sq.clo.x);
+      const float oy = (thi.y - Sq.chi.y) + (tlo.y - Sq.clo.y);
       // near-candidate list of this column: ascending source indices
       bool cand = false;
       int cidx = 0;
-      if (cend > 0) {
-        while (cur < cend && cands[cur] < s) ++cur;
-        cand = cur < cend && cands[cur] == s;
+      if (nr.cend > 0) {
+        while (cur < nr.cend && nr.cands[cur] < s) ++cur;
+        cand = cur < nr.cend && nr.cands[cur] == s;
         cidx = cur;
       }
       const float dc = sqrtf(ox * ox + oy * oy) - RT;
-      const float rp = dc > 0.f ? S.R / dc : 2.f;
+      const float rp = dc > 0.f ? Sq.R / dc : 2.f;
       if (!cand && rp <= kRhoMax) {
         // expansion of order P: rp^(P+1) / (1 - rp) <= kEps
         int P = rp > 0.f ? (int)ceilf(__logf(kEps * (1.f - rp)) / __logf(rp)) - 1 : 1;
@@ -285,10 +277,10 @@ __global__ void __launch_bounds__(128) mp_eval_kernel(MPArgs p) {
         const float tx = tl.x + ox, ty = tl.y + oy;  // omega
         const float om2 = fmaf(tx, tx, ty * ty);
         const float iom2 = mufu_rcp(om2);
-        const float ur = S.R * tx * iom2, ui = -S.R * ty * iom2;  // tau = R / omega
-        float2 hA = smom[q][P].al, hB = smom[q][P].bc, hC = smom[q][P].ac, hE = smom[q][P].ec;
+        const float ur = Sq.R * tx * iom2, ui = -Sq.R * ty * iom2;  // tau = R / omega
+        float2 hA = st.mom[q][P].al, hB = st.mom[q][P].bc, hC = st.mom[q][P].ac, hE = st.mom[q][P].ec;
         for (int k = P - 1; k >= 0; --k) {
-          const MPMom m = smom[q][k];
+          const MPMom m = st.mom[q][k];
           float2 n;
           n.x = fmaf(hA.x, ur, fmaf(-hA.y, ui, m.al.x));
           n.y = fmaf(hA.x, ui, fmaf(hA.y, ur, m.al.y));
@@ -308,8 +300,8 @@ __global__ void __launch_bounds__(128) mp_eval_kernel(MPArgs p) {
         const float qr = (tx * tx - ty * ty) * iom2, qi = 2.f * tx * ty * iom2;
         const float wcr = qr * hC.x + qi * hC.y, wci = qi * hC.x - qr * hC.y;
         const float ter = ur * hE.x - ui * hE.y, tei = -(ur * hE.y + ui * hE.x);
-        const float px = fmaf(-lnom, S.f0.x, 0.5f * S.f0.x) + hA.x + hB.x + 0.5f * (wcr - ter);
-        const float py = fmaf(-lnom, S.f0.y, 0.5f * S.f0.y) + hA.y - hB.y + 0.5f * (wci - tei);
+        const float px = fmaf(-lnom, Sq.f0.x, 0.5f * Sq.f0.x) + hA.x + hB.x + 0.5f * (wcr - ter);
+        const float py = fmaf(-lnom, Sq.f0.y, 0.5f * Sq.f0.y) + hA.y - hB.y + 0.5f * (wci - tei);
         if (valid) {
           neumaier(tot_x, cmp_x, px);
           neumaier(tot_y, cmp_y, py);
@@ -318,12 +310,12 @@ __global__ void __launch_bounds__(128) mp_eval_kernel(MPArgs p) {
         // direct rule over the upsampled points (FP32, log relative to the source centre)
         ++ndirect;
         __syncthreads();
-        const float4* R4 = p.rec + (long long)s * p.ns;
-        for (int j = i; j < p.ns; j += blockDim.x) drec[j] = R4[j];
+        const float4* R4 = S.rec + (long long)s * S.ns;
+        for (int j = i; j < S.ns; j += blockDim.x) st.drec[j] = R4[j];
         __syncthreads();
         bool excl = false;
         if (cand && valid) {
-          const uint32_t w = p.excl_mask[((long long)col * p.maxc + cidx) * p.nwords + (i >> 5)];
+          const uint32_t w = nr.excl[(long long)cidx * nr.nwords + (i >> 5)];
           excl = (w >> (i & 31)) & 1u;
         }
         const float tx = tl.x + ox, ty = tl.y + oy;
@@ -331,8 +323,8 @@ __global__ void __launch_bounds__(128) mp_eval_kernel(MPArgs p) {
         const float irc2 = mufu_rcp(rc2);
         float acx = 0.f, acy = 0.f, alx = 0.f, aly = 0.f;
 #pragma unroll 4
-        for (int j = 0; j < p.ns; ++j) {
-          const float4 r = drec[j];
+        for (int j = 0; j < S.ns; ++j) {
+          const float4 r = st.drec[j];
           const float dx = tx - r.x, dy = ty - r.y;
           const float r2 = fmaf(dx, dx, dy * dy);
           const float inv = mufu_rcp(r2);
@@ -345,14 +337,67 @@ __global__ void __launch_bounds__(128) mp_eval_kernel(MPArgs p) {
         }
         if (valid && !excl) {
           const float lgc = mufu_lg2(rc2);
-          const float px = acx - (float)kHalfLn2 * fmaf(lgc, S.f0.x, alx);
-          const float py = acy - (float)kHalfLn2 * fmaf(lgc, S.f0.y, aly);
+          const float px = acx - (float)kHalfLn2 * fmaf(lgc, Sq.f0.x, alx);
+          const float py = acy - (float)kHalfLn2 * fmaf(lgc, Sq.f0.y, aly);
           neumaier(tot_x, cmp_x, px);
           neumaier(tot_y, cmp_y, py);
         }
       }
     }
   }
+}
+
+// radius of the target vesicle about its centre (max over the CTA's valid points)
+__device__ __forceinline__ float mp_target_radius(float2 tl, int i, float* rmax_w) {
+  float rt = sqrtf(tl.x * tl.x + tl.y * tl.y);
+  for (int o = 16; o > 0; o >>= 1) rt = fmaxf(rt, __shfl_xor_sync(0xffffffffu, rt, o));
+  if ((i & 31) == 0) rmax_w[i >> 5] = rt;
+  __syncthreads();
+  float RT = 0.f;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) RT = fmaxf(RT, rmax_w[w]);
+  return RT * (1.0f + 1e-6f);
+}
+
+struct MPArgs {
+  int nsrc, ns, ntp;
+  const float4* rec;
+  const MPSrc* src;
+  const MPMom* mom;
+  const float2* tloc;
+  const float2* thi;
+  const float2* tlo;
+  const int* self_idx;
+  const int* cand_count;
+  const int* cand_src;
+  const uint32_t* excl_mask;
+  int maxc, nwords;
+  double* out;               // [nt][2][ntp], scaled by 1/(4 pi)
+  unsigned long long* work;  // optional: series terms, direct pairs (per target point)
+};
+
+// One CTA per target column (blockDim = ntp rounded up to a warp multiple).
+// Dynamic shared memory: the direct-rule records of one source (ns float4).
+__global__ void __launch_bounds__(128) mp_eval_kernel(MPArgs p) {
+  extern __shared__ __align__(16) float4 drec[];
+  __shared__ MPSrc ssrc[kStage];
+  __shared__ MPMom smom[kStage][kPMax + 1];
+  __shared__ float rmax_w[32];
+  const int col = blockIdx.x, i = threadIdx.x;
+  const bool valid = i < p.ntp;
+  const float2 tl = valid ? p.tloc[(long long)col * p.ntp + i] : make_float2(0.f, 0.f);
+  const float2 thi = p.thi[col], tlo = p.tlo[col];
+  const float RT = mp_target_radius(tl, i, rmax_w);
+  MPSet S{p.nsrc, p.ns, p.rec, p.src, p.mom};
+  MPNearCol nr;
+  nr.self = p.self_idx ? p.self_idx[col] : -1;
+  nr.cend = p.cand_count ? min(p.cand_count[col], p.maxc) : 0;
+  nr.cands = p.cand_src ? p.cand_src + (long long)col * p.maxc : nullptr;
+  nr.excl = p.excl_mask ? p.excl_mask + (long long)col * p.maxc * p.nwords : nullptr;
+  nr.nwords = p.nwords;
+  MPStage st{ssrc, smom, drec};
+  float tot_x = 0.f, tot_y = 0.f, cmp_x = 0.f, cmp_y = 0.f;
+  unsigned long long terms = 0, ndirect = 0;  // work of this column (uniform across the CTA)
+  mp_sum_set(S, nr, st, i, valid, tl, thi, tlo, RT, tot_x, tot_y, cmp_x, cmp_y, terms, ndirect);
   if (p.work && i == 0) {
     atomicAdd(&p.work[0], terms * (unsigned long long)p.ntp);
     atomicAdd(&p.work[1], ndirect * (unsigned long long)p.ntp * (unsigned long long)p.ns);
@@ -361,6 +406,62 @@ __global__ void __launch_bounds__(128) mp_eval_kernel(MPArgs p) {
     const double scale = 1.0 / (4.0 * VES_PI);
     p.out[(long long)col * 2 * p.ntp + i] = ((double)tot_x + (double)cmp_x) * scale;
     p.out[(long long)col * 2 * p.ntp + p.ntp + i] = ((double)tot_y + (double)cmp_y) * scale;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Several point sets (a suspension of vesicles with different point counts)
+// in one launch: every target column of every set against every source set.
+constexpr int kMPSets = 4;
+
+struct MPGroupArgs {
+  int ng;
+  MPSet set[kMPSets];            // source sets
+  int col0[kMPSets + 1];         // first target column of each target set
+  int ntp[kMPSets];
+  const float2* tloc[kMPSets];   // [nt][ntp] per target set
+  const float2* thi;             // [total columns]
+  const float2* tlo;
+  double* out[kMPSets];          // [nt][2][ntp] per target set
+  // near lists of target set g against source set q, [g][q]
+  const int* cand_count[kMPSets][kMPSets];
+  const int* cand_src[kMPSets][kMPSets];
+  const uint32_t* excl_mask[kMPSets][kMPSets];
+  int maxc[kMPSets][kMPSets];
+  int nwords[kMPSets];
+};
+
+__global__ void __launch_bounds__(128) mp_eval_groups_kernel(MPGroupArgs p) {
+  extern __shared__ __align__(16) float4 drec[];
+  __shared__ MPSrc ssrc[kStage];
+  __shared__ MPMom smom[kStage][kPMax + 1];
+  __shared__ float rmax_w[32];
+  const int col = blockIdx.x, i = threadIdx.x;
+  int g = 0;
+  while (g + 1 < p.ng && col >= p.col0[g + 1]) ++g;
+  const int lc = col - p.col0[g], ntp = p.ntp[g];
+  const bool valid = i < ntp;
+  const float2 tl = valid ? p.tloc[g][(long long)lc * ntp + i] : make_float2(0.f, 0.f);
+  const float2 thi = p.thi[col], tlo = p.tlo[col];
+  const float RT = mp_target_radius(tl, i, rmax_w);
+  MPStage st{ssrc, smom, drec};
+  float tot_x = 0.f, tot_y = 0.f, cmp_x = 0.f, cmp_y = 0.f;
+  unsigned long long terms = 0, ndirect = 0;
+  for (int q = 0; q < p.ng; ++q) {
+    MPNearCol nr;
+    nr.self = q == g ? lc : -1;
+    const int mc = p.maxc[g][q];
+    nr.cend = p.cand_count[g][q] ? min(p.cand_count[g][q][lc], mc) : 0;
+    nr.cands = p.cand_src[g][q] ? p.cand_src[g][q] + (long long)lc * mc : nullptr;
+    nr.excl = p.excl_mask[g][q] ? p.excl_mask[g][q] + (long long)lc * mc * p.nwords[g] : nullptr;
+    nr.nwords = p.nwords[g];
+    mp_sum_set(p.set[q], nr, st, i, valid, tl, thi, tlo, RT, tot_x, tot_y, cmp_x, cmp_y, terms, ndirect);
+  }
+  if (valid) {
+    const double scale = 1.0 / (4.0 * VES_PI);
+    double* o = p.out[g] + (long long)lc * 2 * ntp;
+    o[i] = ((double)tot_x + (double)cmp_x) * scale;
+    o[ntp + i] = ((double)tot_y + (double)cmp_y) * scale;
   }
 }
 
@@ -427,4 +528,78 @@ int farfield_mp_run(const FFEnv& env, int nsrc, int ns, const double* Xsrc, cons
   mp_eval_kernel<<<nt, threads, dsmem, s>>>(a);
   if (env.timing) ves_ff_timing_end(env.timing, s, (double)total_pts * ns * (double)nsrc);
   return ves_launch_check("farfield multipole");
+}
+
+int farfield_mp_groups_run(const FFEnv& env, int ng, const int* nsrc, const int* ns, const double* const* Xsrc,
+                           const double* const* den, const int* nt, const int* ntp, const double* const* Xtar,
+                           const ves_near_lists* const* nl, double* const* out, WsCarver& ws, cudaStream_t s) {
+  (void)env;
+  if (ng < 1 || ng > kMPSets) {
+    if (!ws.sizing) ves_record_error(VES_ERR_ARG, "farfield groups: 1 to %d point sets", kMPSets);
+    return VES_ERR_ARG;
+  }
+  float4* rec[kMPSets];
+  MPSrc* src[kMPSets];
+  MPMom* mom[kMPSets];
+  float2* tloc[kMPSets];
+  long long cols = 0;
+  int nsmax = 0, ntpmax = 0;
+  for (int g = 0; g < ng; ++g) {
+    rec[g] = ws.take<float4>((size_t)nsrc[g] * ns[g]);
+    src[g] = ws.take<MPSrc>(nsrc[g]);
+    mom[g] = ws.take<MPMom>((size_t)nsrc[g] * (kPMax + 1));
+    tloc[g] = ws.take<float2>((size_t)nt[g] * ntp[g]);
+    cols += nt[g];
+    nsmax = std::max(nsmax, ns[g]);
+    ntpmax = std::max(ntpmax, ntp[g]);
+  }
+  float2* thi = ws.take<float2>((size_t)cols);
+  float2* tlo = ws.take<float2>((size_t)cols);
+  if (ws.sizing) return VES_OK;
+  if (!ws.ok()) {
+    ves_record_error(VES_ERR_WORKSPACE, "farfield groups: workspace too small");
+    return VES_ERR_WORKSPACE;
+  }
+  if (cols == 0) return VES_OK;
+  if (ntpmax > 128 || (size_t)nsmax * sizeof(float4) > 160 * 1024) {
+    ves_record_error(VES_ERR_SHAPE, "farfield groups: at most 128 target points and 10240 source points per vesicle");
+    return VES_ERR_SHAPE;
+  }
+  MPGroupArgs a;
+  memset(&a, 0, sizeof(a));
+  a.ng = ng;
+  a.thi = thi;
+  a.tlo = tlo;
+  a.col0[0] = 0;
+  for (int g = 0; g < ng; ++g) {
+    if (nsrc[g] > 0) {
+      ves_count_launch();
+      mp_prep_kernel<<<nsrc[g], 256, 0, s>>>(ns[g], Xsrc[g], den[g], rec[g], src[g], mom[g]);
+    }
+    if (nt[g] > 0) {
+      ves_count_launch();
+      mp_prep_targets_kernel<<<nt[g], 256, 0, s>>>(ntp[g], Xtar[g], tloc[g], thi + a.col0[g], tlo + a.col0[g]);
+    }
+    a.set[g] = MPSet{nsrc[g], ns[g], rec[g], src[g], mom[g]};
+    a.col0[g + 1] = a.col0[g] + nt[g];
+    a.ntp[g] = ntp[g];
+    a.tloc[g] = tloc[g];
+    a.out[g] = out[g];
+    a.nwords[g] = (ntp[g] + 31) / 32;
+    for (int q = 0; q < ng; ++q) {
+      const ves_near_lists* L = nl ? nl[g * ng + q] : nullptr;
+      a.cand_count[g][q] = L ? L->cand_count : nullptr;
+      a.cand_src[g][q] = L ? L->cand_src : nullptr;
+      a.excl_mask[g][q] = L ? L->excl_mask : nullptr;
+      a.maxc[g][q] = L ? L->maxc : 0;
+    }
+  }
+  const size_t dsmem = (size_t)nsmax * sizeof(float4);
+  if (dsmem > 32 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(mp_eval_groups_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem);
+    if (e != cudaSuccess) return ves_cuda_status(e, "farfield groups smem attribute");
+  }
+  ves_count_launch();
+  mp_eval_groups_kernel<<<(unsigned)cols, ((ntpmax + 31) / 32) * 32, dsmem, s>>>(a);
+  return ves_launch_check("farfield groups");
 }

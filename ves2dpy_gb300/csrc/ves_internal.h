@@ -154,6 +154,16 @@ int farfield_run_env(const FFEnv& env, int precision, int nsrc, int ns, const do
 int farfield_mp_run(const FFEnv& env, int nsrc, int ns, const double* Xsrc, const double* den, int nt, int ntp,
                     const double* Xtar, const int* self_idx, const ves_near_lists* nl, double* out, WsCarver& ws,
                     cudaStream_t s);
+// Every target vesicle of ng point sets (ng <= 4) against every source
+// vesicle of the ng sets in one launch (precision VES_PREC_FP32M): targets of
+// set g are nt[g] vesicles of ntp[g] points Xtar[g]; sources of set q are
+// nsrc[q] vesicles of ns[q] upsampled points Xsrc[q] with densities den[q];
+// nl[g*ng + q] is the near list of targets g against sources q (nullptr:
+// none); a target's own vesicle (q == g) is skipped; out[g] [nt][2][ntp]
+// (overwritten), scaled like farfield_run's.
+int farfield_mp_groups_run(const FFEnv& env, int ng, const int* nsrc, const int* ns, const double* const* Xsrc,
+                           const double* const* den, const int* nt, const int* ntp, const double* const* Xtar,
+                           const ves_near_lists* const* nl, double* const* out, WsCarver& ws, cudaStream_t s);
 int farfield_run(ves_ctx* c, int precision, int nsrc, int ns, const double* Xsrc, const double* den,
                  int nt, int ntp, const double* Xtar, const int* self_idx, const ves_near_lists* nl,
                  double* out, WsCarver& ws, cudaStream_t s);
@@ -170,6 +180,14 @@ int near_sing_int_run(ves_ctx* c, int scheme, int precision, int nv, const doubl
 // between two vesicle sets (targets: ct, Xt; sources: cs, Xs / Xup_s, den_s, vself_s)
 int near_zone_matlab_cross(ves_ctx* ct, ves_ctx* cs, int nvt, const double* Xt, int nvs, const double* Xs, double h,
                            const ves_near_lists* nl, WsCarver& ws, cudaStream_t s);
+// the MATLAB near-singular correction alone, added to LP (the far field
+// computed elsewhere); ct == cs for a set against itself
+int near_correct_matlab(ves_ctx* ct, ves_ctx* cs, const double* Xt, const double* Xup_s, const double* den_s,
+                        const double* vself_s, const ves_near_lists* nl, double h, double* LP, cudaStream_t s);
+// several MATLAB corrections (np <= 16 pairs of point sets) in one launch
+int near_correct_matlab_pairs(int np, ves_ctx* const* ct, ves_ctx* const* cs, const double* const* Xt,
+                              const double* const* Xup_s, const double* const* den_s, const double* const* vself_s,
+                              const ves_near_lists* const* nl, const double* h, double* const* LP, cudaStream_t s);
 int near_sing_int_cross_add(ves_ctx* ct, ves_ctx* cs, int scheme, int precision, int nvt, const double* Xt, int nvs,
                             const double* Xup_s, const double* den_s, const double* vself_s,
                             const ves_near_lists* nl, double h, double* LP, WsCarver& ws, cudaStream_t s);

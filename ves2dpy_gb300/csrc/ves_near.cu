@@ -482,41 +482,47 @@ __global__ void __launch_bounds__(128) matlab_zone_kernel(int Nt, int Ns, int ma
 // den already scaled by (1 - visc); otherwise the single layer.
 // Targets Xt and LP with Nt points per vesicle; sources with Ns points (vself)
 // and Nup upsampled points (Xup, tang_up, den).
+// One MATLAB-scheme correction problem: targets of a point set with Nt
+// points per vesicle against the sources (Ns points, Nup upsampled) of
+// another set or of itself, with the near entries of its lists.
+struct MatlabPair {
+  int Nt, Ns, Nup;
+  double h;
+  const double *Xt, *Xup, *tang_up, *den, *vself, *lag;
+  const int* n_entries;
+  int max_entries;
+  const int *ent_tsj, *ent_icp;
+  const double* ent_geo;
+  double *LP, *near_only;
+};
+
+// Near entry e of one correction problem, one warp (lane = its lane).
 template <bool DL>
-__global__ void matlab_correct_kernel(int Nt, int Ns, int Nup, double h, const double* __restrict__ Xt,
-                                      const double* __restrict__ Xup, const double* __restrict__ tang_up,
-                                      const double* __restrict__ den,
-                                      const double* __restrict__ vself, const double* __restrict__ lag,
-                                      const int* __restrict__ n_entries, int max_entries,
-                                      const int* __restrict__ ent_tsj, const int* __restrict__ ent_icp,
-                                      const double* __restrict__ ent_geo, double* __restrict__ LP,
-                                      double* __restrict__ near_only) {
-  const int e = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
-  const int lane = threadIdx.x % 32;
-  const int ne = min(*n_entries, max_entries);
+__device__ __forceinline__ void matlab_correct_entry(const MatlabPair& a, int e, int lane) {
+  const int ne = min(*a.n_entries, a.max_entries);
   if (e >= ne) return;
-  const int t = ent_tsj[3 * e], s = ent_tsj[3 * e + 1], j = ent_tsj[3 * e + 2];
-  const int icp = ent_icp[e];
-  const double dist = ent_geo[4 * e], nxp = ent_geo[4 * e + 1], nyp = ent_geo[4 * e + 2], th = ent_geo[4 * e + 3];
+  const int t = a.ent_tsj[3 * e], s = a.ent_tsj[3 * e + 1], j = a.ent_tsj[3 * e + 2];
+  const int icp = a.ent_icp[e];
+  const double dist = a.ent_geo[4 * e], nxp = a.ent_geo[4 * e + 1], nyp = a.ent_geo[4 * e + 2], th = a.ent_geo[4 * e + 3];
   const double beta = 1.1;
-  const double xt = Xt[(long long)t * 2 * Nt + j], yt = Xt[(long long)t * 2 * Nt + Nt + j];
+  const double xt = a.Xt[(long long)t * 2 * a.Nt + j], yt = a.Xt[(long long)t * 2 * a.Nt + a.Nt + j];
   const double ux = (xt - nxp) / dist, uy = (yt - nyp) / dist;
   // layer potential of source vesicle s at the 6 Lagrange points
   double ax[6], ay[6];
 #pragma unroll
   for (int m = 0; m < 6; ++m) ax[m] = ay[m] = 0.0;
-  const double* xs = Xup + (long long)s * 2 * Nup;
-  const double* ds = den + (long long)s * 2 * Nup;
-  for (int u = lane; u < Nup; u += 32) {
-    const double sxu = xs[u], syu = xs[Nup + u], dxu = ds[u], dyu = ds[Nup + u];
+  const double* xs = a.Xup + (long long)s * 2 * a.Nup;
+  const double* ds = a.den + (long long)s * 2 * a.Nup;
+  for (int u = lane; u < a.Nup; u += 32) {
+    const double sxu = xs[u], syu = xs[a.Nup + u], dxu = ds[u], dyu = ds[a.Nup + u];
     double nxu = 0.0, nyu = 0.0;
     if (DL) {
-      nxu = tang_up[(long long)s * 2 * Nup + Nup + u];
-      nyu = -tang_up[(long long)s * 2 * Nup + u];
+      nxu = a.tang_up[(long long)s * 2 * a.Nup + a.Nup + u];
+      nyu = -a.tang_up[(long long)s * 2 * a.Nup + u];
     }
 #pragma unroll
     for (int m = 0; m < 6; ++m) {
-      const double px = nxp + beta * h * ux * (m + 1), py = nyp + beta * h * uy * (m + 1);
+      const double px = nxp + beta * a.h * ux * (m + 1), py = nyp + beta * a.h * uy * (m + 1);
       const double rx = px - sxu, ry = py - syu;
       const double r2 = rx * rx + ry * ry;
       if (DL) {
@@ -545,29 +551,61 @@ __global__ void matlab_correct_kernel(int Nt, int Ns, int Nup, double h, const d
   for (int comp = 0; comp < 2; ++comp) {
     // on-curve value: Lagrange interpolant of vself around icp at theta
     double coef[7], stencil[7];
-    for (int q = 0; q < 7; ++q) stencil[q] = vself[(long long)s * 2 * Ns + comp * Ns + ((icp - 3 + q) % Ns + Ns) % Ns];
+    for (int q = 0; q < 7; ++q) stencil[q] = a.vself[(long long)s * 2 * a.Ns + comp * a.Ns + ((icp - 3 + q) % a.Ns + a.Ns) % a.Ns];
     for (int r = 0; r < 7; ++r) {
-      double a = 0;
-      for (int q = 0; q < 7; ++q) a = fma(lag[r * 7 + q], stencil[q], a);
-      coef[r] = a;
+      double acc = 0;
+      for (int q = 0; q < 7; ++q) acc = fma(a.lag[r * 7 + q], stencil[q], acc);
+      coef[r] = acc;
     }
     const double vel = horner7(coef, th);
     double pts[7];
     pts[0] = vel;
     for (int m = 0; m < 6; ++m) pts[m + 1] = (comp == 0 ? ax[m] : ay[m]) * kscale;
     for (int r = 0; r < 7; ++r) {
-      double a = 0;
-      for (int q = 0; q < 7; ++q) a = fma(lag[r * 7 + q], pts[q], a);
-      coef[r] = a;
+      double acc = 0;
+      for (int q = 0; q < 7; ++q) acc = fma(a.lag[r * 7 + q], pts[q], acc);
+      coef[r] = acc;
     }
-    vals[comp] = horner7(coef, dist / (beta * h * 6.0));
+    vals[comp] = horner7(coef, dist / (beta * a.h * 6.0));
   }
-  atomicAdd(&LP[(long long)t * 2 * Nt + j], vals[0]);
-  atomicAdd(&LP[(long long)t * 2 * Nt + Nt + j], vals[1]);
-  if (near_only) {
-    atomicAdd(&near_only[(long long)t * 2 * Nt + j], vals[0]);
-    atomicAdd(&near_only[(long long)t * 2 * Nt + Nt + j], vals[1]);
+  atomicAdd(&a.LP[(long long)t * 2 * a.Nt + j], vals[0]);
+  atomicAdd(&a.LP[(long long)t * 2 * a.Nt + a.Nt + j], vals[1]);
+  if (a.near_only) {
+    atomicAdd(&a.near_only[(long long)t * 2 * a.Nt + j], vals[0]);
+    atomicAdd(&a.near_only[(long long)t * 2 * a.Nt + a.Nt + j], vals[1]);
   }
+}
+
+template <bool DL>
+__global__ void matlab_correct_kernel(int Nt, int Ns, int Nup, double h, const double* __restrict__ Xt,
+                                      const double* __restrict__ Xup, const double* __restrict__ tang_up,
+                                      const double* __restrict__ den,
+                                      const double* __restrict__ vself, const double* __restrict__ lag,
+                                      const int* __restrict__ n_entries, int max_entries,
+                                      const int* __restrict__ ent_tsj, const int* __restrict__ ent_icp,
+                                      const double* __restrict__ ent_geo, double* __restrict__ LP,
+                                      double* __restrict__ near_only) {
+  const MatlabPair a{Nt, Ns, Nup, h, Xt, Xup, tang_up, den, vself, lag, n_entries, max_entries,
+                     ent_tsj, ent_icp, ent_geo, LP, near_only};
+  matlab_correct_entry<DL>(a, (blockIdx.x * blockDim.x + threadIdx.x) / 32, threadIdx.x % 32);
+}
+
+// Several correction problems (every pair of point sets of a suspension with
+// several point counts) in one launch: problem k owns the warps
+// [warp0[k], warp0[k+1]), one per near-entry slot.
+constexpr int kMatlabPairs = 16;
+struct MatlabPairs {
+  int np;
+  long long warp0[kMatlabPairs + 1];
+  MatlabPair pair[kMatlabPairs];
+};
+
+__global__ void matlab_correct_pairs_kernel(MatlabPairs P) {
+  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+  if (w >= P.warp0[P.np]) return;
+  int k = 0;
+  while (k + 1 < P.np && w >= P.warp0[k + 1]) ++k;
+  matlab_correct_entry<false>(P.pair[k], (int)(w - P.warp0[k]), threadIdx.x % 32);
 }
 
 __global__ void min_reduce_kernel(int n, const double* __restrict__ a, double* __restrict__ out) {
@@ -842,6 +880,65 @@ int near_zone_matlab_cross(ves_ctx* ct, ves_ctx* cs, int nvt, const double* Xt, 
                                            nl->excl_mask, nl->max_entries, nl->n_entries, nl->ent_tsj, nl->ent_icp,
                                            nl->ent_geo, ct->status);
   return ves_launch_check("near_zone_cross");
+}
+
+// The MATLAB near-singular correction alone (nearSingInt with the far field
+// computed elsewhere, matlab/poten_py.m:495-692): targets Xt of context ct,
+// sources Xup_s of context cs (ct == cs for a set against itself, with the
+// self-vesicle entries of its own lists) with densities den_s and self
+// velocities vself_s; the near entries of nl; added to LP.
+int near_correct_matlab(ves_ctx* ct, ves_ctx* cs, const double* Xt, const double* Xup_s, const double* den_s,
+                        const double* vself_s, const ves_near_lists* nl, double h, double* LP, cudaStream_t s) {
+  const long long warps = nl->max_entries;
+  if (warps <= 0) return VES_OK;
+  ves_count_launch();
+  matlab_correct_kernel<false><<<ceil_div(warps * 32, 256), 256, 0, s>>>(
+      ct->N, cs->N, cs->Nup, h, Xt, Xup_s, nullptr, den_s, vself_s, ct->lag, nl->n_entries, nl->max_entries,
+      nl->ent_tsj, nl->ent_icp, nl->ent_geo, LP, nullptr);
+  return ves_launch_check("near_correct_matlab");
+}
+
+// Several MATLAB corrections in one launch (np <= 16): problem k has targets
+// Xt[k] of context ct[k], sources Xup_s[k] of context cs[k] with densities
+// den_s[k] and self velocities vself_s[k], near entries nl[k], zone width
+// h[k], and adds to LP[k].
+int near_correct_matlab_pairs(int np, ves_ctx* const* ct, ves_ctx* const* cs, const double* const* Xt,
+                              const double* const* Xup_s, const double* const* den_s, const double* const* vself_s,
+                              const ves_near_lists* const* nl, const double* h, double* const* LP, cudaStream_t s) {
+  if (np < 1 || np > kMatlabPairs) {
+    ves_record_error(VES_ERR_ARG, "near_correct_matlab_pairs: 1 to %d problems", kMatlabPairs);
+    return VES_ERR_ARG;
+  }
+  MatlabPairs P;
+  memset(&P, 0, sizeof(P));
+  P.np = np;
+  P.warp0[0] = 0;
+  for (int k = 0; k < np; ++k) {
+    MatlabPair& a = P.pair[k];
+    a.Nt = ct[k]->N;
+    a.Ns = cs[k]->N;
+    a.Nup = cs[k]->Nup;
+    a.h = h[k];
+    a.Xt = Xt[k];
+    a.Xup = Xup_s[k];
+    a.tang_up = nullptr;
+    a.den = den_s[k];
+    a.vself = vself_s[k];
+    a.lag = ct[k]->lag;
+    a.n_entries = nl[k]->n_entries;
+    a.max_entries = nl[k]->max_entries;
+    a.ent_tsj = nl[k]->ent_tsj;
+    a.ent_icp = nl[k]->ent_icp;
+    a.ent_geo = nl[k]->ent_geo;
+    a.LP = LP[k];
+    a.near_only = nullptr;
+    P.warp0[k + 1] = P.warp0[k] + nl[k]->max_entries;
+  }
+  const long long warps = P.warp0[np];
+  if (warps <= 0) return VES_OK;
+  ves_count_launch();
+  matlab_correct_pairs_kernel<<<(unsigned)ceil_div(warps * 32, 256), 256, 0, s>>>(P);
+  return ves_launch_check("near_correct_matlab_pairs");
 }
 
 int near_sing_int_cross_add(ves_ctx* ct, ves_ctx* cs, int scheme, int precision, int nvt, const double* Xt, int nvs,

@@ -293,6 +293,36 @@ struct MixedState {
   int matvecs;
 };
 
+// The far field of every group from every group's upsampled sources (the
+// densities M.den of the current matvec), one launch (VES_PREC_FP32M), into
+// each group's LP; near-pair exclusions follow the lists of the MATLAB scheme.
+int mixed_farfield_merged(MixedState& M, bool sizing = false) {
+  int nsrc[kMaxGroups], ns[kMaxGroups], nt[kMaxGroups], ntp[kMaxGroups];
+  const double *Xsrc[kMaxGroups], *den[kMaxGroups], *Xtar[kMaxGroups];
+  const ves_near_lists* nl[kMaxGroups * kMaxGroups];
+  double* out[kMaxGroups];
+  const bool lists = M.prm->near_scheme == VES_NEAR_MATLAB;
+  for (int g = 0; g < M.ng; ++g) {
+    StepState& S = M.g[g];
+    nsrc[g] = nt[g] = S.nv;
+    ns[g] = S.Nup;
+    ntp[g] = S.N;
+    Xsrc[g] = S.Xup;
+    den[g] = M.den[g];
+    Xtar[g] = S.X;
+    out[g] = S.LP;
+    for (int q = 0; q < M.ng; ++q) nl[g * M.ng + q] = lists ? (q == g ? &S.nl : &M.xl[g][q]) : nullptr;
+  }
+  FFEnv env;
+  env.status = M.g[0].c->status;
+  env.N = M.g[0].N;
+  env.timing = nullptr;
+  WsCarver sub(sizing ? nullptr : M.scratch, sizing ? 0 : M.scratch_bytes);
+  const int rc = farfield_mp_groups_run(env, M.ng, nsrc, ns, Xsrc, den, nt, ntp, Xtar, nl, out, sub, M.s);
+  if (sizing) M.scratch_bytes = std::max(M.scratch_bytes, sub.off);
+  return rc;
+}
+
 int matvec(MixedState& M, const double* v, double* out) {
   M.matvecs++;
   const ves_step_params* prm = M.prm;
@@ -308,6 +338,46 @@ int matvec(MixedState& M, const double* v, double* out) {
     }
   }
   int rc;
+  if (M.ng > 1 && prm->farfield_precision == VES_PREC_FP32M) {
+    // every group's far field from every group's sources in one launch, then
+    // the near corrections of every (target group, source group) pair in one
+    if ((rc = mixed_farfield_merged(M))) return rc;
+    if (prm->near_scheme == VES_NEAR_MATLAB) {
+      ves_ctx *ct[kMaxGroups * kMaxGroups], *cs[kMaxGroups * kMaxGroups];
+      const double *Xt[kMaxGroups * kMaxGroups], *Xs[kMaxGroups * kMaxGroups], *dn[kMaxGroups * kMaxGroups],
+          *vs[kMaxGroups * kMaxGroups];
+      const ves_near_lists* nl[kMaxGroups * kMaxGroups];
+      double hh[kMaxGroups * kMaxGroups];
+      double* lp[kMaxGroups * kMaxGroups];
+      int np = 0;
+      for (int g = 0; g < M.ng; ++g)
+        for (int q = 0; q < M.ng; ++q, ++np) {
+          StepState& S = M.g[g];
+          const StepState& Q = M.g[q];
+          ct[np] = S.c;
+          cs[np] = Q.c;
+          Xt[np] = S.X;
+          Xs[np] = Q.Xup;
+          dn[np] = M.den[q];
+          vs[np] = Q.Gf;
+          nl[np] = q == g ? &S.nl : &M.xl[g][q];
+          hh[np] = q == g ? S.h : M.h[q];
+          lp[np] = S.LP;
+        }
+      if ((rc = near_correct_matlab_pairs(np, ct, cs, Xt, Xs, dn, vs, nl, hh, lp, M.s))) return rc;
+    }
+    for (int g = 0; g < M.ng; ++g) {
+      StepState& S = M.g[g];
+      const int nv = S.nv, N = S.N;
+      const double* vg = v + M.off[g];
+      double* og = out + M.off[g];
+      ves_count_launch();
+      combine_pos_kernel<<<ceil_div((long long)nv * 2 * N, 256), 256, 0, M.s>>>(nv, N, prm->dt, vg, S.Gf, S.LP, nullptr,
+                                                                                nullptr, nullptr, og);
+      launch_surface_div(S.c, nv, S.isa, S.tang, vg, 3LL * N, og + 2 * N, 3LL * N, M.s);
+    }
+    return ves_launch_check("matvec mixed");
+  }
   for (int g = 0; g < M.ng; ++g) {
     StepState& S = M.g[g];
     {
@@ -914,6 +984,17 @@ static int biem_step_mixed_impl(int ng, ves_ctx* const* ctx, const ves_step_para
                               nullptr, nullptr, nullptr, 1.0, nullptr, w2, s);
       scratch = std::max(scratch, w2.off);
     }
+  }
+  if (ng > 1 && prm->farfield_precision == VES_PREC_FP32M) {
+    for (int g = 0; g < ng; ++g) {  // shapes only: the sizing pass reads no pointer
+      M.g[g].nv = nvs[g];
+      M.g[g].N = ctx[g]->N;
+      M.g[g].Nup = ctx[g]->Nup;
+      M.g[g].c = ctx[g];
+    }
+    M.scratch_bytes = 0;
+    mixed_farfield_merged(M, true);
+    scratch = std::max(scratch, M.scratch_bytes);
   }
   M.scratch = ws.take<char>(scratch + 1024);
   M.scratch_bytes = scratch + 1024;

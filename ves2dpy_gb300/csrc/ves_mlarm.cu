@@ -329,42 +329,64 @@ __global__ void prep_xy_kernel(int nv, int N, const double* __restrict__ Xs, con
 template <typename Real>
 __global__ void prep_modes_kernel(int nv, int N, int modes, const double* __restrict__ Xs,
                                   const double* __restrict__ p, Real* __restrict__ out) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (long long)nv * modes * 2 * N) return;
-  const int j = (int)(i % N);
-  const long long r = i / N;
-  const int c = (int)(r % 2);
-  const int kk = (int)((r / 2) % modes);
-  const long long v = r / (2LL * modes);
-  out[i] = (Real)((Xs[v * 2 * N + c * N + j] - p[4 * kk + 2 * c]) / p[4 * kk + 2 * c + 1]);
+  // one vesicle per blockIdx.y (strided past the grid), [modes][2][N] along x
+  const int per = modes * 2 * N;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= per) return;
+  const int j = i % N, c = (i / N) & 1, kk = i / (2 * N);
+  const double mean = p[4 * kk + 2 * c], sd = p[4 * kk + 2 * c + 1];
+  for (long long v = blockIdx.y; v < nv; v += gridDim.y) {
+    const double x = Xs[v * 2 * N + c * N + j];
+    Real val;
+    if (sizeof(Real) == 8)
+      val = (Real)((x - mean) / sd);
+    else  // FP32 networks: the quotient in FP32 (within an ulp of the rounded FP64 one)
+      val = (Real)((float)(x - mean) / (float)sd);
+    out[v * per + i] = val;
+  }
 }
 
 // MergedAdvNetwork.forward input (:150-190): for mode k (Fourier index k+1),
 // channel 2k = [x normalised ++ y normalised] (length 2N), channel 2k+1 =
 // [cos((2 pi j / N)(k+1)) / N ++ sin(...) / N]; the statistics of mode 63
-// (the Nyquist index) have unit std.
+// (the Nyquist index) have unit std.  FP64 networks: the reference's FP64
+// arithmetic; FP32 networks: the quotient in FP32 and the basis from
+// sincospif of the exactly reduced argument 2 ((j (k+1)) mod N) / N.
 template <typename Real>
 __global__ void prep_adv_kernel(int nv, int N, const double* __restrict__ Xs, const double* __restrict__ p,
                                 Real* __restrict__ out) {
   const int L = 2 * N;
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (long long)nv * kModes * 2 * L) return;
-  const int jj = (int)(i % L);
-  const long long r = i / L;
-  const int ch = (int)(r % 2);
-  const int kk = (int)((r / 2) % kModes);
-  const long long v = r / (2LL * kModes);
+  const int per = kModes * 2 * L;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= per) return;
+  const int jj = i % L, ch = (i / L) & 1, kk = i / (2 * L);
   const int comp = jj >= N, j = jj - comp * N;
-  double val;
-  if (ch == 0) {
-    const double sd = (kk == 63) ? 1.0 : p[4 * kk + 2 * comp + 1];
-    val = (Xs[v * 2 * N + comp * N + j] - p[4 * kk + 2 * comp]) / sd;
-  } else {
-    const double th = ((double)j / N) * (2.0 * VES_PI);
-    const double arg = th * (double)(kk + 1);
-    val = (comp ? sin(arg) : cos(arg)) * (1.0 / N);
+  if (ch == 1) {  // the mode's basis function: the same for every vesicle
+    Real val;
+    if (sizeof(Real) == 8) {
+      const double th = ((double)j / N) * (2.0 * VES_PI);
+      const double arg = th * (double)(kk + 1);
+      val = (Real)((comp ? sin(arg) : cos(arg)) * (1.0 / N));
+    } else {
+      const int m = (int)(((long long)j * (kk + 1)) % N);
+      float sv, cv;
+      sincospif(2.0f * (float)m / (float)N, &sv, &cv);
+      val = (Real)((comp ? sv : cv) / (float)N);
+    }
+    for (long long v = blockIdx.y; v < nv; v += gridDim.y) out[v * per + i] = val;
+    return;
   }
-  out[i] = (Real)val;
+  const double mean = p[4 * kk + 2 * comp];
+  const double sd = (kk == 63) ? 1.0 : p[4 * kk + 2 * comp + 1];
+  for (long long v = blockIdx.y; v < nv; v += gridDim.y) {
+    const double x = Xs[v * 2 * N + comp * N + j];
+    Real val;
+    if (sizeof(Real) == 8)
+      val = (Real)((x - mean) / sd);
+    else
+      val = (Real)((float)(x - mean) / (float)sd);
+    out[v * per + i] = val;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -861,8 +883,8 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
   // near network (predictNearLayers :1726-1812) on request
   if (prm->eval_near_net && m->near) {
     ves_count_launch();
-    prep_modes_kernel<Real><<<ceil_div((long long)nv * kNearModes * 2 * N, 256), 256, 0, s>>>(nv, N, kNearModes, Xs,
-                                                                                             m->near_in, nin);
+    prep_modes_kernel<Real><<<dim3(ceil_div(kNearModes * 2 * N, 256), std::min(nv, 65535)), 256, 0, s>>>(
+        nv, N, kNearModes, Xs, m->near_in, nin);
     WsCarver w = sub();
     ves_net_timing_begin(c, s);
     if ((rc = net_forward_run(m->near, nv, nin, nout, w, c->status, s))) return rc;
@@ -891,8 +913,8 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
   filter_kernel<<<nv, 128, shf, s>>>(N, m->filt, far, vback, vsum);
   // tension solves (:1099-1113)
   ves_count_launch();
-  prep_modes_kernel<Real><<<ceil_div((long long)nv * kModes * 2 * N, 256), 256, 0, s>>>(nv, N, kModes, Xs,
-                                                                                       m->advten_in, nin);
+  prep_modes_kernel<Real><<<dim3(ceil_div(kModes * 2 * N, 256), std::min(nv, 65535)), 256, 0, s>>>(
+      nv, N, kModes, Xs, m->advten_in, nin);
   {
     WsCarver w = sub();
     ves_net_timing_begin(c, s);
@@ -921,7 +943,8 @@ int mlarm_step_t(ves_mlarm* m, const ves_mlarm_params* prm, int nv, const double
   filter_kernel<<<nv, 128, shf, s>>>(N, m->filt, far, vback, vsum);
   // advection (:1150-1160)
   ves_count_launch();
-  prep_adv_kernel<Real><<<ceil_div((long long)nv * kModes * 2 * 2 * N, 256), 256, 0, s>>>(nv, N, Xs, m->adv_in, nin);
+  prep_adv_kernel<Real><<<dim3(ceil_div(kModes * 2 * 2 * N, 256), std::min(nv, 65535)), 256, 0, s>>>(nv, N, Xs,
+                                                                                                  m->adv_in, nin);
   {
     WsCarver w = sub();
     ves_net_timing_begin(c, s);

@@ -41,6 +41,7 @@ constexpr int kPMax = 24;                 // highest expansion order
 constexpr float kRhoMax = 0.35f;          // 0.35^25 / 0.65 < 1e-11
 constexpr float kEps = 1e-10f;            // truncation bound relative to sum |f_j|
 constexpr int kStage = 16;                // source vesicles per shared-memory stage
+constexpr int kDrecChunk = 512;           // direct-rule points per shared-memory stage (8 KB)
 constexpr double kHalfLn2 = 0.34657359027997264;
 
 struct __align__(16) MPSrc {
@@ -307,12 +308,11 @@ __device__ __forceinline__ void mp_sum_set(const MPSet& S, const MPNearCol& nr, 
           neumaier(tot_y, cmp_y, py);
         }
       } else {
-        // direct rule over the upsampled points (FP32, log relative to the source centre)
+        // direct rule over the upsampled points (FP32, log relative to the
+        // source centre), staged kDrecChunk points at a time (the same order
+        // of summation as one stage)
         ++ndirect;
-        __syncthreads();
         const float4* R4 = S.rec + (long long)s * S.ns;
-        for (int j = i; j < S.ns; j += blockDim.x) st.drec[j] = R4[j];
-        __syncthreads();
         bool excl = false;
         if (cand && valid) {
           const uint32_t w = nr.excl[(long long)cidx * nr.nwords + (i >> 5)];
@@ -322,18 +322,24 @@ __device__ __forceinline__ void mp_sum_set(const MPSet& S, const MPNearCol& nr, 
         const float rc2 = fmaf(tx, tx, ty * ty);
         const float irc2 = mufu_rcp(rc2);
         float acx = 0.f, acy = 0.f, alx = 0.f, aly = 0.f;
+        for (int j0 = 0; j0 < S.ns; j0 += kDrecChunk) {
+          const int nj = min(kDrecChunk, S.ns - j0);
+          __syncthreads();
+          for (int j = i; j < nj; j += blockDim.x) st.drec[j] = R4[j0 + j];
+          __syncthreads();
 #pragma unroll 4
-        for (int j = 0; j < S.ns; ++j) {
-          const float4 r = st.drec[j];
-          const float dx = tx - r.x, dy = ty - r.y;
-          const float r2 = fmaf(dx, dx, dy * dy);
-          const float inv = mufu_rcp(r2);
-          const float lg = mufu_lg2(r2 * irc2);
-          const float cc = fmaf(dx, r.z, dy * r.w) * inv;
-          acx = fmaf(cc, dx, acx);
-          acy = fmaf(cc, dy, acy);
-          alx = fmaf(lg, r.z, alx);
-          aly = fmaf(lg, r.w, aly);
+          for (int j = 0; j < nj; ++j) {
+            const float4 r = st.drec[j];
+            const float dx = tx - r.x, dy = ty - r.y;
+            const float r2 = fmaf(dx, dx, dy * dy);
+            const float inv = mufu_rcp(r2);
+            const float lg = mufu_lg2(r2 * irc2);
+            const float cc = fmaf(dx, r.z, dy * r.w) * inv;
+            acx = fmaf(cc, dx, acx);
+            acy = fmaf(cc, dy, acy);
+            alx = fmaf(lg, r.z, alx);
+            aly = fmaf(lg, r.w, aly);
+          }
         }
         if (valid && !excl) {
           const float lgc = mufu_lg2(rc2);
@@ -376,7 +382,8 @@ struct MPArgs {
 };
 
 // One CTA per target column (blockDim = ntp rounded up to a warp multiple).
-// Dynamic shared memory: the direct-rule records of one source (ns float4).
+// Dynamic shared memory: direct-rule records of one source, min(ns,
+// kDrecChunk) float4.
 __global__ void __launch_bounds__(128) mp_eval_kernel(MPArgs p) {
   extern __shared__ __align__(16) float4 drec[];
   __shared__ MPSrc ssrc[kStage];
@@ -492,11 +499,7 @@ int farfield_mp_run(const FFEnv& env, int nsrc, int ns, const double* Xsrc, cons
     ves_record_error(VES_ERR_SHAPE, "farfield: near lists need N target points per column");
     return VES_ERR_SHAPE;
   }
-  const size_t dsmem = (size_t)ns * sizeof(float4);
-  if (dsmem > 160 * 1024) {
-    ves_record_error(VES_ERR_SHAPE, "farfield: %d source points per vesicle exceed the multipole path", ns);
-    return VES_ERR_SHAPE;
-  }
+  const size_t dsmem = (size_t)std::min(ns, kDrecChunk) * sizeof(float4);
   ves_count_launch(2);
   mp_prep_kernel<<<nsrc, 256, 0, s>>>(ns, Xsrc, den, rec, src, mom);
   mp_prep_targets_kernel<<<nt, 256, 0, s>>>(ntp, Xtar, tloc, thi, tlo);
@@ -561,8 +564,8 @@ int farfield_mp_groups_run(const FFEnv& env, int ng, const int* nsrc, const int*
     return VES_ERR_WORKSPACE;
   }
   if (cols == 0) return VES_OK;
-  if (ntpmax > 128 || (size_t)nsmax * sizeof(float4) > 160 * 1024) {
-    ves_record_error(VES_ERR_SHAPE, "farfield groups: at most 128 target points and 10240 source points per vesicle");
+  if (ntpmax > 128) {
+    ves_record_error(VES_ERR_SHAPE, "farfield groups: at most 128 target points per vesicle");
     return VES_ERR_SHAPE;
   }
   MPGroupArgs a;
@@ -594,7 +597,7 @@ int farfield_mp_groups_run(const FFEnv& env, int ng, const int* nsrc, const int*
       a.maxc[g][q] = L ? L->maxc : 0;
     }
   }
-  const size_t dsmem = (size_t)nsmax * sizeof(float4);
+  const size_t dsmem = (size_t)std::min(nsmax, kDrecChunk) * sizeof(float4);
   if (dsmem > 32 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(mp_eval_groups_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsmem);
     if (e != cudaSuccess) return ves_cuda_status(e, "farfield groups smem attribute");

@@ -80,20 +80,74 @@ __global__ void bend_up_kernel(int N, int Nup, int m, const double* __restrict__
   for (int i = threadIdx.x; i < 2 * N; i += blockDim.x) xy[i] = Xk[i];
   __syncthreads();
   // the interpolant and |dXup/dtheta| on the Nup grid
-  for (int u = threadIdx.x; u < Nup; u += blockDim.x) {
-    double x = 0, y = 0, dx = 0, dy = 0;
-    int r = u;
-    for (int i = 0; i < N; ++i) {
-      x = fma(pc[r], xy[i], x);
-      y = fma(pc[r], xy[N + i], y);
-      dx = fma(pcd[r], xy[i], dx);
-      dy = fma(pcd[r], xy[N + i], dy);
-      r -= m;
-      if (r < 0) r += Nup;
+  if (ves_fft_size_ok(N) && Nup % N == 0) {
+    // spectral: z = x + i y, FFT of length N (the Nup table read with stride
+    // Nup/N), the spectrum zero-padded to Nup with the Nyquist mode split
+    // between +N/2 and -N/2 (interpft), inverse FFTs of length Nup of the
+    // spectrum times i k (the derivative) and of the spectrum itself
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      zr[i] = xy[i];
+      zi[i] = xy[N + i];
     }
-    zr[u] = x;
-    zi[u] = y;
-    is[u] = 1.0 / sqrt(dx * dx + dy * dy);
+    ves_fft(zr, zi, tre, tim, N, cosU, sinU, -1, Nup / N);
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+      xy[i] = zr[i];  // the spectrum, modes 0..N-1
+      xy[N + i] = zi[i];
+    }
+    __syncthreads();
+    const int h = N / 2, top = Nup - N;
+    for (int pass = 0; pass < 2; ++pass) {
+      for (int u = threadIdx.x; u < Nup; u += blockDim.x) {
+        double vr = 0.0, vi = 0.0, kk = 0.0;
+        if (u < h) {
+          vr = xy[u];
+          vi = xy[N + u];
+          kk = u;
+        } else if (u == h || u == Nup - h) {
+          vr = 0.5 * xy[h];
+          vi = 0.5 * xy[N + h];
+          kk = (u == h) ? (double)h : -(double)h;
+        } else if (u > Nup - h) {
+          vr = xy[u - top];
+          vi = xy[N + u - top];
+          kk = (double)(u - Nup);
+        }
+        if (pass == 0) {  // i k (vr + i vi)
+          zr[u] = -kk * vi;
+          zi[u] = kk * vr;
+        } else {
+          zr[u] = vr;
+          zi[u] = vi;
+        }
+      }
+      ves_fft(zr, zi, tre, tim, Nup, cosU, sinU, +1);
+      for (int u = threadIdx.x; u < Nup; u += blockDim.x) {
+        if (pass == 0) {
+          const double dx = zr[u] / N, dy = zi[u] / N;
+          is[u] = 1.0 / sqrt(dx * dx + dy * dy);
+        } else {
+          zr[u] /= N;
+          zi[u] /= N;
+        }
+      }
+      __syncthreads();
+    }
+  } else {
+    for (int u = threadIdx.x; u < Nup; u += blockDim.x) {
+      double x = 0, y = 0, dx = 0, dy = 0;
+      int r = u;
+      for (int i = 0; i < N; ++i) {
+        x = fma(pc[r], xy[i], x);
+        y = fma(pc[r], xy[N + i], y);
+        dx = fma(pcd[r], xy[i], dx);
+        dy = fma(pcd[r], xy[N + i], dy);
+        r -= m;
+        if (r < 0) r += Nup;
+      }
+      zr[u] = x;
+      zi[u] = y;
+      is[u] = 1.0 / sqrt(dx * dx + dy * dy);
+    }
   }
   // four arc derivatives: z <- isa * ifft(i k fft(z)), Nyquist zeroed
   for (int it = 0; it < 4; ++it) {

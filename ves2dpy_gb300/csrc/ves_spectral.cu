@@ -157,6 +157,80 @@ __global__ void upsample_deriv_kernel(int N, int Nup, int m, const double* __res
   }
 }
 
+// The same by FFT (N power of two or three times one, Nup a multiple of N):
+// z = x + i y, FFT of length N (the Nup table read with stride Nup/N), the
+// spectrum zero-padded to Nup with the Nyquist mode split between +N/2 and
+// -N/2 (interpft), inverse FFTs of length Nup of the spectrum times i k (the
+// derivative and the speed) and of the spectrum (the curve).
+__global__ void __launch_bounds__(256) upsample_deriv_fft_kernel(int N, int Nup, const double* __restrict__ cosU,
+                                                                 const double* __restrict__ sinU,
+                                                                 const double* __restrict__ X,
+                                                                 double* __restrict__ Xup, double* __restrict__ dXup,
+                                                                 double* __restrict__ sa_up) {
+  extern __shared__ double sh[];
+  double* zr = sh;
+  double* zi = zr + Nup;
+  double* tre = zi + Nup;
+  double* tim = tre + Nup;
+  double* spr = tim + Nup;  // [N] the spectrum
+  double* spi = spr + N;
+  const int k = blockIdx.x;
+  const double* Xk = X + (long long)k * 2 * N;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    zr[i] = Xk[i];
+    zi[i] = Xk[N + i];
+  }
+  ves_fft(zr, zi, tre, tim, N, cosU, sinU, -1, Nup / N);
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    spr[i] = zr[i];
+    spi[i] = zi[i];
+  }
+  __syncthreads();
+  const int h = N / 2, top = Nup - N;
+  const long long o = (long long)k * 2 * Nup;
+  for (int pass = 0; pass < 2; ++pass) {
+    if (pass == 1 && !Xup) break;
+    for (int u = threadIdx.x; u < Nup; u += blockDim.x) {
+      double vr = 0.0, vi = 0.0, kk = 0.0;
+      if (u < h) {
+        vr = spr[u];
+        vi = spi[u];
+        kk = u;
+      } else if (u == h || u == Nup - h) {
+        vr = 0.5 * spr[h];
+        vi = 0.5 * spi[h];
+        kk = (u == h) ? (double)h : -(double)h;
+      } else if (u > Nup - h) {
+        vr = spr[u - top];
+        vi = spi[u - top];
+        kk = (double)(u - Nup);
+      }
+      if (pass == 0) {
+        zr[u] = -kk * vi;
+        zi[u] = kk * vr;
+      } else {
+        zr[u] = vr;
+        zi[u] = vi;
+      }
+    }
+    ves_fft(zr, zi, tre, tim, Nup, cosU, sinU, +1);
+    for (int u = threadIdx.x; u < Nup; u += blockDim.x) {
+      const double a = zr[u] / N, b = zi[u] / N;
+      if (pass == 0) {
+        if (dXup) {
+          dXup[o + u] = a;
+          dXup[o + Nup + u] = b;
+        }
+        if (sa_up) sa_up[(long long)k * Nup + u] = sqrt(a * a + b * b);
+      } else {
+        Xup[o + u] = a;
+        Xup[o + Nup + u] = b;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // Geometry of the upsampled curve from the first and second derivatives of
 // the trig interpolant at the Nup grid.  They equal the FFT derivatives of
 // interpft(X, Nup) on its own grid (diffProp of capsules(Xup),
@@ -224,9 +298,21 @@ void launch_upsample_geom(const ves_ctx* c, int nv, const double* X, double* Xup
 void launch_upsample_deriv(const ves_ctx* c, int nv, const double* X, double* Xup, double* dXup,
                            double* sa_up, cudaStream_t s) {
   if (nv <= 0) return;
-  size_t sh = (size_t)(2 * c->N + 2 * c->Nup) * sizeof(double);
+  const int N = c->N, Nup = c->Nup;
+  if (N % 2 == 0 && Nup > N && Nup % N == 0 && ves_fft_size_ok(N) && ves_fft_size_ok(Nup)) {
+    const size_t shf = (size_t)(4 * Nup + 2 * N) * sizeof(double);
+    if (shf <= 48 * 1024 ||
+        cudaFuncSetAttribute(upsample_deriv_fft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shf) ==
+            cudaSuccess) {
+      ves_count_launch();
+      upsample_deriv_fft_kernel<<<nv, 256, shf, s>>>(N, Nup, c->cosU, c->sinU, X, Xup, dXup, sa_up);
+      return;
+    }
+    cudaGetLastError();  // the dense sums below need no opt-in
+  }
+  size_t sh = (size_t)(2 * N + 2 * Nup) * sizeof(double);
   ves_count_launch();
-  upsample_deriv_kernel<<<nv, 256, sh, s>>>(c->N, c->Nup, c->m, c->pc, c->pcd, X, Xup, dXup, sa_up);
+  upsample_deriv_kernel<<<nv, 256, sh, s>>>(N, Nup, c->m, c->pc, c->pcd, X, Xup, dXup, sa_up);
 }
 
 // ----------------------------------------------------------------------------

@@ -498,6 +498,13 @@ def run_gb300(a, rank, world):
     # the network kernels are timed inside a step of about a second: the
     # sustained BF16 figure is their denominator
     bf16_peak = peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops", 1700.0))
+    if "bf16_tflops_sustained" in peaks:
+        bf16_src = ("MEASURED_PEAKS.json bf16_tflops_sustained (cuBLAS BF16 GEMM looped for seconds under the power "
+                    "cap), of measured")
+    elif "bf16_tflops" in peaks:
+        bf16_src = "MEASURED_PEAKS.json bf16_tflops (burst; no sustained figure), of measured"
+    else:
+        bf16_src = "no MEASURED_PEAKS.json: 1.7 PFLOP/s, the sustained BF16 figure of an earlier GB300 measurement, of fallback"
     flops = {n: net_flops(NETS[n]) * a.nv for n in NETS}
     net_total_ms = sum(r["net_ms"].values())
     net_tflops = sum(flops.values()) / (net_total_ms * 1e-3) / 1e12 if net_total_ms > 0 else None
@@ -508,13 +515,12 @@ def run_gb300(a, rank, world):
                 "achieved": nl_tflops, "peak": bf16_peak, "unit": "TFLOP/s",
                 "frac": nl_tflops / bf16_peak if nl_tflops else None, "traffic": None,
                 "traffic_note": "ncu (profiles/tcnet_blocks_nv64_full.md): the down + up1 + up2 launches of one "
-                                "advection-network block at nv=64 move 25 + 99 + 250 MB of DRAM (the FP32 block "
+                                "advection-network block at nv=64 move 22 + 108 + 250 MB of DRAM (the FP32 block "
                                 "input read by down and up2, the output written by up2, the BF16 intermediates "
-                                "written and read once; no re-reads), at most 20% of the DRAM peak",
+                                "written and read once; no re-reads), at most 26% of the DRAM peak",
                 "flops_per_step": st.networks_flops / a.steps, "ms_per_step": st.networks_ms / a.steps,
                 "passes_per_step": st.networks_launches / a.steps,
-                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (cuBLAS BF16 GEMM looped for seconds "
-                               "under the power cap), of measured",
+                "peak_source": bf16_src,
                 "share_of_step": st.networks_ms / r["ms"] if r["ms"] else None}
     # all-pairs sums
     sm_mhz = (r["clocks"] or {}).get("sm_max_mhz") or 2070.0
